@@ -1,0 +1,246 @@
+/*
+ * mcgpu.h — C ABI of the GB300 marching-cubes library (libmcgpu.so).
+ *
+ * This is the drop-in boundary for model3d's MarchingCubesSearch path
+ * (model3d/mc.go:45-49).  A host-language wrapper (the Go cgo binding shown
+ * in INTEGRATION.md, the Python mirror in model3d_gb300/, or a C++ caller)
+ * serialises its Solid tree into an array of mc_node records, the library
+ * lowers it to a device program (CSG bytecode + flattened collider BVH), runs
+ * corner classification, cube classification, compaction and the edge
+ * bisection search on one GPU, and returns an indexed mesh.
+ *
+ * Plain C types only: pointers and sizes.  Inputs are borrowed for the
+ * duration of a call.  Solids that cannot be lowered return
+ * MC_ERR_NOT_LOWERABLE; there is no CPU fallback.
+ *
+ * Threading: one mc_ctx per host thread.  Each context owns a CUDA stream
+ * and grow-only device buffers; every call is synchronous on return.
+ */
+#ifndef MCGPU_H
+#define MCGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+
+typedef enum mc_status {
+    MC_OK = 0,
+    /* validateBounds panic "invalid bounds: ..." (model3d/bounder.go:48-52). */
+    MC_ERR_INVALID_BOUNDS = 1,
+    /* solidCache.FetchZ panic "solid is true outside of bounds" (model3d/mc.go:687-689). */
+    MC_ERR_BOUNDS_INSIDE = 2,
+    /* squareSpacer.LookupEdgePoint panic "vertex not on edge" (model3d/mc.go:659). */
+    MC_ERR_NOT_ON_EDGE = 3,
+    /* LookupEdgePoint computed an index past the spacer array; Go raises an
+     * index-out-of-range runtime panic there (model3d/mc.go:655-656). */
+    MC_ERR_EDGE_INDEX = 4,
+    /* Malformed node array (bad child counts, unknown kind, bad mesh index). */
+    MC_ERR_BAD_PROGRAM = 5,
+    /* A node kind or mode that has no device lowering (e.g. an inset collider). */
+    MC_ERR_NOT_LOWERABLE = 6,
+    MC_ERR_OOM = 7,
+    /* A bounded device-side wait ran out (never used to cover a fault). */
+    MC_ERR_TIMEOUT = 8,
+    MC_ERR_CUDA = 9,
+    MC_ERR_ARG = 10,
+    /* The spacer loop would not terminate (x += delta leaves x unchanged, or
+     * delta <= 0 / NaN) or the grid exceeds the library's size limit. */
+    MC_ERR_GRID = 11,
+    /* The program exceeds a device limit (stack depth, leaf count). */
+    MC_ERR_LIMIT = 12
+} mc_status;
+
+/* ---------------------------------------------------------------- the scene */
+
+/* Node kinds.  Values are part of the ABI. */
+enum {
+    /* Leaves (n_children == 0). */
+    MC_NODE_SPHERE = 1,    /* p = Center.xyz, Radius                (model3d/shapes.go:13-31)   */
+    MC_NODE_RECT = 2,      /* p = MinVal.xyz, MaxVal.xyz            (model3d/shapes.go:145-173) */
+    MC_NODE_CYLINDER = 3,  /* p = P1.xyz, P2.xyz, Radius            (model3d/shapes.go:542-598) */
+    MC_NODE_CAPSULE = 4,   /* p = P1.xyz, P2.xyz, Radius            (model3d/shapes.go:348-368) */
+    MC_NODE_TORUS = 5,     /* p = Center.xyz, Axis.xyz, Outer, Inner (model3d/shapes.go:1323-1365) */
+    MC_NODE_COLLIDER = 6,  /* NewColliderSolid(collider) over triangle set `mesh`
+                              (model3d/solid.go:247-305, collisions.go:119-212) */
+    /* Combinators. */
+    MC_NODE_JOIN = 16,      /* JoinedSolid, n_children >= 1      (model3d/solid.go:71-98)    */
+    MC_NODE_SUBTRACT = 17,  /* SubtractedSolid, children = Positive, Negative (solid.go:120-142) */
+    MC_NODE_INTERSECT = 18, /* IntersectedSolid, n_children >= 1 (model3d/solid.go:144-172)  */
+    MC_NODE_TRANSFORM = 19, /* TransformSolid(t, child): n_steps MC_XF_* records follow the node,
+                               then the child (model3d/transform.go:240-247).  The steps are
+                               the FORWARD transform t in JoinedTransform order; the library
+                               computes t.Inverse() itself. */
+    MC_NODE_CHECKED = 20,   /* CheckedFuncSolid(min, max, child.Contains), as made by
+                               CacheSolidBounds / ForceSolidBounds (model3d/solid.go:46-50,
+                               :294-318); one child. */
+    /* Transform steps (only directly after a MC_NODE_TRANSFORM node). */
+    MC_XF_TRANSLATE = 32,   /* p = Offset.xyz   (model3d/transform.go:40-58)   */
+    MC_XF_SCALE = 33,       /* p = Scale        (model3d/transform.go:67-89)   */
+    MC_XF_VECSCALE = 34,    /* p = Scale.xyz    (model3d/transform.go:100-118) */
+    MC_XF_MATRIX = 35       /* p = Matrix3, row-major (model3d/transform.go:127-157; Rotation
+                               and Mirror are Matrix3 transforms as well) */
+};
+
+/*
+ * One record of the prefix-order serialisation of a Solid tree: a node, then
+ * (for MC_NODE_TRANSFORM) its n_steps transform-step records, then its
+ * children, each serialised the same way.
+ *
+ * min/max are the node's Min()/Max() exactly as the host language computed
+ * them; the library uses the root's bounds for the spacer and the bounds of
+ * TRANSFORM / CHECKED / COLLIDER nodes for their containment checks, so that
+ * the grid is bit-identical to the caller's own newSquareSpacer.
+ */
+typedef struct mc_node {
+    int32_t kind;
+    int32_t n_children;
+    int32_t n_steps;  /* MC_NODE_TRANSFORM: number of MC_XF_* records that follow */
+    int32_t mesh;     /* MC_NODE_COLLIDER: index into the mc_tri_set array */
+    double min[3];
+    double max[3];
+    double p[12];
+} mc_node;
+
+/*
+ * Triangle set behind a MC_NODE_COLLIDER.  tris holds n triangles of three
+ * vertices of three float64 each (row-major, n x 9).
+ *   grouped == 0: the collider is MeshToCollider(mesh) — the library applies
+ *                 GroupTriangles to the given order (model3d/collisions.go:138-142);
+ *   grouped == 1: the order is already grouped and the collider is
+ *                 GroupedTrianglesToCollider(tris) (model3d/collisions.go:169-181).
+ */
+typedef struct mc_tri_set {
+    const double* tris;
+    int64_t n;
+    int32_t grouped;
+    int32_t reserved;
+} mc_tri_set;
+
+/* --------------------------------------------------------------- options */
+
+enum {
+    MC_PREC_FP64 = 0,          /* every predicate in FP64, reference operation order */
+    MC_PREC_FP32_FILTERED = 1  /* FP32 predicate with a forward error bound; FP64 when it cannot decide */
+};
+
+typedef struct mc_opts {
+    int32_t precision;  /* MC_PREC_* (default MC_PREC_FP32_FILTERED) */
+    int32_t cull;       /* 1: per-tile bounding-box culling of leaves (default); 0: off */
+    int32_t tile_y;     /* corner-tile height in y (0: tuned default) */
+    int32_t tile_z;     /* corner-tile depth in z (0: tuned default) */
+    int32_t reserved[4];
+} mc_opts;
+
+typedef struct mc_stats {
+    int64_t nx, ny, nz;      /* spacer sizes */
+    int64_t corners;         /* nx*ny*nz */
+    int64_t vertices;        /* unique edge vertices */
+    int64_t triangles;
+    int64_t leaf_evals;      /* leaf predicate evaluations (classification + search) */
+    int64_t escalations;     /* FP32 evaluations that fell back to FP64 */
+    int64_t tiles;           /* corner tiles classified */
+    int64_t tiles_const;     /* tiles decided without evaluating any leaf */
+    int64_t bvh_nodes;       /* collider: BVH nodes whose box was tested */
+    int64_t bvh_tris;        /* collider: ray-triangle tests */
+    double ms_classify;      /* device time per phase (CUDA events) */
+    double ms_cubes;
+    double ms_search;
+    double ms_total;
+} mc_stats;
+
+/* Indexed mesh: vertices n_vertices x 3 float64, triangles n_triangles x 3
+ * vertex indices in the lookup-table vertex order (model3d/mc.go:401-407). */
+typedef struct mc_mesh {
+    double* vertices;
+    int32_t* triangles;
+    int64_t n_vertices;
+    int64_t n_triangles;
+    mc_stats stats;
+} mc_mesh;
+
+typedef struct mc_ctx mc_ctx;
+typedef struct mc_solid mc_solid;
+
+/* ---------------------------------------------------------------- entries */
+
+/* Reference panic text for a status (or a short description). */
+const char* mc_status_string(mc_status s);
+
+/* Detailed message of the last failing call on this context. */
+const char* mc_last_error(const mc_ctx* ctx);
+
+/* Create a context on CUDA device `device` (its own stream and buffers). */
+mc_status mc_create(mc_ctx** out, int device);
+void mc_destroy(mc_ctx* ctx);
+
+/* Lower a serialised Solid tree (prefix order, see mc_node) to the device.
+ * Replaces the dynamic Solid.Contains dispatch (model3d/solid.go:16-21). */
+mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes,
+                          const mc_tri_set* sets, size_t n_sets, mc_solid** out);
+void mc_solid_destroy(mc_solid* solid);
+
+/* Root Min()/Max() of a lowered solid. */
+mc_status mc_solid_bounds(const mc_solid* solid, double min[3], double max[3]);
+
+/* One axis of newSquareSpacer (model3d/mc.go:594-608): for x := lo - delta;
+ * x <= hi + delta; x += delta.  Writes at most cap values, sets *n to the
+ * full count.  MC_ERR_GRID if the loop would not terminate. */
+mc_status mc_spacer_axis(double lo, double hi, double delta, double* out, int64_t cap,
+                         int64_t* n);
+
+/* MarchingCubesSearch(s, delta, iters) (model3d/mc.go:45-49); iters == 0 is
+ * MarchingCubes (model3d/mc.go:14-37).  The result is copied into host arrays
+ * owned by the library; release them with mc_mesh_free.  opts may be NULL. */
+mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters,
+                    const mc_opts* opts, mc_mesh* out);
+void mc_mesh_free(mc_mesh* mesh);
+
+/* Same as mc_search, but the mesh stays in device memory owned by the
+ * context (valid until the next call on it); *n_vertices / *n_triangles and
+ * *stats (may be NULL) are filled. */
+mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters,
+                           const mc_opts* opts, int64_t* n_vertices, int64_t* n_triangles,
+                           mc_stats* stats);
+/* Device pointers of the last mc_search_device result. */
+mc_status mc_result_device(const mc_ctx* ctx, const double** vertices,
+                           const int32_t** triangles);
+/* Copy the last result into caller-provided host arrays (V*3, T*3). */
+mc_status mc_result_copy(mc_ctx* ctx, double* vertices, int32_t* triangles);
+
+/* Solid.Contains on the GPU for n points (n x 3 float64) -> out[i] in {0,1}.
+ * Same device predicates and precision modes as mc_search. */
+mc_status mc_contains(mc_ctx* ctx, const mc_solid* solid, const double* points, int64_t n,
+                      const mc_opts* opts, uint8_t* out);
+
+/* Batched search: n independent (solid, delta, iters) jobs meshed by one
+ * persistent work-queue launch, replayed from a CUDA graph when the same
+ * batch shape repeats.  outs[i] receives job i's mesh (free each with
+ * mc_mesh_free).  Statuses per job go to job_status (may be NULL); the
+ * return value is the first failing status. */
+typedef struct mc_job {
+    const mc_solid* solid;
+    double delta;
+    int32_t iters;
+    int32_t reserved;
+} mc_job;
+mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_opts* opts,
+                          mc_mesh* outs, mc_status* job_status);
+
+/* The 256-case lookup table the library uses (mcLookupTable,
+ * model3d/mc.go:434-456): counts[c] triangles for case c, each as three
+ * corner pairs tris[c][t][0..5]. */
+mc_status mc_case_table(uint8_t counts[256], uint8_t tris[256][5][6]);
+
+/* Library version string. */
+const char* mc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCGPU_H */

@@ -1,0 +1,19 @@
+"""model3d_gb300 — GB300-native MarchingCubesSearch for model3d solids.
+
+The reference-facing names (Sphere, Cylinder, JoinedSolid, TransformSolid,
+MeshToCollider, NewColliderSolid, MarchingCubesSearch, ...) mirror package
+model3d of unixpickle/model3d.  Containment, cube classification, vertex
+dedup and the bisection search run in CUDA kernels for sm_103a
+(model3d_gb300/csrc); results are bit-identical to the reference algorithm.
+"""
+from .geometry import Coord3D, Matrix3, NewMatrix3Rotation, X, XYZ, Y, Z
+from .solids import (Capsule, CacheSolidBounds, ColliderSolid, Cylinder, ForceSolidBounds,
+                     GroupBounders, GroupedTrianglesToCollider, IntersectedSolid, JoinedSolid,
+                     JoinedTransform, Matrix3Transform, MeshToCollider, NewColliderSolid,
+                     NewRect, NotLowerable, Rect, RotateSolid, Rotation, Scale, ScaleSolid,
+                     Solid, Sphere, Subtract, SubtractedSolid, Torus, TransformSolid, Translate,
+                     TranslateSolid, VecScale, VecScaleSolid, serialize)
+from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesSearch, MCError,
+                 Mesh, canonical, case_table, default_context, spacer_axis)
+
+__all__ = [n for n in dir() if not n.startswith("_")]

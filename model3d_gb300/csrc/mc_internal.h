@@ -1,0 +1,264 @@
+// mc_internal.h — device program layout shared by the host lowering
+// (mc_lower.cpp) and the CUDA kernels (mc_kernels.cu).
+//
+// A lowered Solid is:
+//   * a postfix boolean program over a 32-deep bit stack (ops[]),
+//   * a table of leaves (primitive predicates and collider parity tests),
+//     each with FP64 constants in the reference's operation order and FP32
+//     constants for the filtered predicate,
+//   * a table of box checks (TRANSFORM / CHECKED nodes) with the inverse
+//     transform steps of TRANSFORM nodes,
+//   * flattened collider trees (nodes, child lists, triangle records).
+#pragma once
+
+#include <stdint.h>
+
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#endif
+
+namespace mcgpu {
+
+// ---- postfix ops: opcode in bits 28..31, argument in bits 0..27.
+enum Op : uint32_t {
+    OP_LEAF = 1,    // push leaf[arg](point)
+    OP_OR = 2,      // b = pop; top |= b
+    OP_AND = 3,     // b = pop; top &= b
+    OP_ANDNOT = 4,  // b = pop; top &= !b        (SubtractedSolid)
+    OP_NOT = 5,     // top = !top                (only produced by folding)
+    OP_XPUSH = 6,   // save point; point = inverse transform arg (point)
+    OP_XPOP = 7,    // restore point; top &= inbox(arg, point)
+    OP_BOX = 8,     // push inbox(arg, point)    (only produced by folding)
+    OP_BOXAND = 9,  // top &= inbox(arg, point)  (CheckedFuncSolid)
+    OP_TRUE = 10,
+    OP_FALSE = 11,
+};
+__host__ __device__ inline uint32_t make_op(uint32_t code, uint32_t arg) { return (code << 28) | arg; }
+__host__ __device__ inline uint32_t op_code(uint32_t op) { return op >> 28; }
+__host__ __device__ inline uint32_t op_arg(uint32_t op) { return op & 0x0fffffffu; }
+
+// ---- leaf kinds (same values as the MC_NODE_* leaves of the ABI).
+enum LeafKind : int32_t {
+    LK_SPHERE = 1,
+    LK_RECT = 2,
+    LK_CYLINDER = 3,
+    LK_CAPSULE = 4,
+    LK_TORUS = 5,
+    LK_COLLIDER = 6,
+};
+
+// FP64 constants per leaf (doubles), kind-specific layout:
+//   SPHERE   : c.xyz, TR                    (TR: largest S with sqrt_rn(S) <= R)
+//   RECT     : min.xyz, max.xyz
+//   CYLINDER : P2.xyz, dir.xyz, norm, TR
+//   CAPSULE  : s0.xyz, s1.xyz, v.xyz, norm, TR
+//   TORUS    : center.xyz, b1.xyz, b2.xyz, outer, T_inner
+//   COLLIDER : min.xyz, max.xyz, (double)tree index
+constexpr int LEAF_D = 16;
+// FP32 filter constants per leaf (floats), same order rounded to float, plus
+// thresholds: [..., TR_lo, TR_hi] / [..., norm_lo, norm_hi, TR_lo, TR_hi].
+constexpr int LEAF_F = 16;
+
+constexpr int MAX_STACK = 31;     // bit-stack depth limit
+constexpr int MAX_XDEPTH = 8;     // nested transforms
+constexpr int MAX_OPS = 1 << 16;  // program length limit
+constexpr int MAX_BVH_DEPTH = 64; // traversal frames
+
+// Inverse transform step: kind (MC_XF_*), 9 parameters.
+struct XStepD {
+    int32_t kind;
+    int32_t pad;
+    double v[9];
+};
+
+// A box check (TRANSFORM or CHECKED node): the node's bounds; TRANSFORM nodes
+// carry [first_step, first_step + n_steps) inverse steps in apply order.
+struct XBoxD {
+    double lo[3];
+    double hi[3];
+    int32_t first_step;
+    int32_t n_steps;
+};
+
+// Flattened collider tree.  Node child lists live in `child` entries:
+// c >= 0 is a node index, c < 0 is triangle (-c - 1).
+struct BvhNodeD {
+    double lo[3];
+    double hi[3];
+    int32_t first;  // first entry in the child list
+    int32_t count;
+};
+struct BvhNodeF {  // FP32 copy of the node box, rounded outward
+    float lo[3];
+    float hi[3];
+    int32_t first;
+    int32_t count;
+};
+// Per-triangle Moller-Trumbore constants with the ray direction fixed
+// (model3d/primitives.go:207-249, collisions.go:124): t0, v1, v2,
+// cross1 = D x v2, invDet = 1 / (cross1 . v1), valid = !parallel && det != 0.
+struct TriD {
+    double t0[3];
+    double v1[3];
+    double v2[3];
+    double c1[3];
+    double inv_det;
+    int32_t valid;
+    int32_t pad;
+};
+struct TriF {
+    float t0[3];
+    float v1[3];
+    float v2[3];
+    float c1[3];
+    float inv_det;
+    int32_t valid;
+};
+struct TreeD {
+    int32_t kind;  // 0: no triangles (nullCollider); 1: root is a node; 2: root is one triangle
+    int32_t root;  // node or triangle index (absolute)
+};
+
+// Device view of one lowered solid (passed by value to kernels).
+struct ProgView {
+    const uint32_t* ops;
+    const uint32_t* ops_allfalse;  // program folded with every leaf culled
+    const int32_t* leaf_kind;
+    const double* leaf_d;   // n_leaves * LEAF_D
+    const float* leaf_f;    // n_leaves * LEAF_F
+    const double* cull;     // n_leaves * 6: lo.xyz, hi.xyz (world space, widened); NaN = never cull
+    const XBoxD* xbox;
+    const XStepD* xstep;
+    const TreeD* trees;
+    const BvhNodeD* nodes;
+    const BvhNodeF* nodes_f;
+    const int32_t* child;
+    const TriD* tris;
+    const TriF* tris_f;
+    int32_t n_ops;
+    int32_t n_ops_allfalse;  // -1: const false, -2: const true, else length
+    int32_t n_leaves;
+    int32_t n_xbox;
+};
+
+// Constant folding of a postfix program given which leaves are active
+// (inactive leaves are known false over the region being evaluated).
+// Writes the pruned program to q and returns its length, or FOLD_FALSE /
+// FOLD_TRUE when the whole program is constant.  Fragments of a postfix
+// program are contiguous, so discarding a folded subtree is a truncation.
+// The stack needs MAX_STACK + MAX_XDEPTH + 2 entries.
+constexpr int FOLD_FALSE = -1;
+constexpr int FOLD_TRUE = -2;
+constexpr int FOLD_STACK = MAX_STACK + MAX_XDEPTH + 2;
+
+template <class Active>
+__host__ __device__ inline int fold_program(const uint32_t* ops, int n, Active active, uint32_t* q) {
+    // Entries: >= 0 fragment start; -1 const false; -2 const true; <= -3 marker (-3 - start).
+    int stk[FOLD_STACK];
+    int sp = 0, qn = 0;
+    for (int i = 0; i < n; i++) {
+        uint32_t op = ops[i];
+        uint32_t code = op_code(op), arg = op_arg(op);
+        switch (code) {
+            case OP_LEAF:
+                if (active(arg)) {
+                    stk[sp++] = qn;
+                    q[qn++] = op;
+                } else {
+                    stk[sp++] = FOLD_FALSE;
+                }
+                break;
+            case OP_TRUE: stk[sp++] = FOLD_TRUE; break;
+            case OP_FALSE: stk[sp++] = FOLD_FALSE; break;
+            case OP_OR:
+            case OP_AND: {
+                int b = stk[--sp], a = stk[--sp];
+                int dom = code == OP_OR ? FOLD_TRUE : FOLD_FALSE;   // absorbing constant
+                int neu = code == OP_OR ? FOLD_FALSE : FOLD_TRUE;   // neutral constant
+                if (a == dom || b == dom) {
+                    if (a >= 0) qn = a;
+                    else if (b >= 0) qn = b;
+                    stk[sp++] = dom;
+                } else if (a == neu) {
+                    stk[sp++] = b;
+                } else if (b == neu) {
+                    stk[sp++] = a;
+                } else {
+                    q[qn++] = op;
+                    stk[sp++] = a;
+                }
+                break;
+            }
+            case OP_ANDNOT: {  // a && !b
+                int b = stk[--sp], a = stk[--sp];
+                if (b == FOLD_TRUE || a == FOLD_FALSE) {
+                    if (a >= 0) qn = a;
+                    else if (b >= 0) qn = b;
+                    stk[sp++] = FOLD_FALSE;
+                } else if (b == FOLD_FALSE) {
+                    stk[sp++] = a;
+                } else if (a == FOLD_TRUE) {
+                    q[qn++] = make_op(OP_NOT, 0);
+                    stk[sp++] = b;
+                } else {
+                    q[qn++] = op;
+                    stk[sp++] = a;
+                }
+                break;
+            }
+            case OP_NOT: {
+                int a = stk[--sp];
+                if (a == FOLD_TRUE) stk[sp++] = FOLD_FALSE;
+                else if (a == FOLD_FALSE) stk[sp++] = FOLD_TRUE;
+                else {
+                    q[qn++] = op;
+                    stk[sp++] = a;
+                }
+                break;
+            }
+            case OP_XPUSH:
+                stk[sp++] = -3 - qn;
+                q[qn++] = op;
+                break;
+            case OP_XPOP: {
+                int e = stk[--sp];
+                int ms = -3 - stk[--sp];
+                if (e == FOLD_FALSE) {
+                    qn = ms;
+                    stk[sp++] = FOLD_FALSE;
+                } else if (e == FOLD_TRUE) {
+                    qn = ms;
+                    q[qn++] = make_op(OP_BOX, arg);
+                    stk[sp++] = ms;
+                } else {
+                    q[qn++] = op;
+                    stk[sp++] = ms;
+                }
+                break;
+            }
+            case OP_BOX:
+                stk[sp++] = qn;
+                q[qn++] = op;
+                break;
+            case OP_BOXAND: {
+                int a = stk[--sp];
+                if (a == FOLD_FALSE) {
+                    stk[sp++] = FOLD_FALSE;
+                } else if (a == FOLD_TRUE) {
+                    stk[sp++] = qn;
+                    q[qn++] = make_op(OP_BOX, arg);
+                } else {
+                    q[qn++] = op;
+                    stk[sp++] = a;
+                }
+                break;
+            }
+            default: break;
+        }
+    }
+    int r = sp > 0 ? stk[0] : FOLD_FALSE;
+    return r >= 0 ? qn : r;
+}
+
+}  // namespace mcgpu

@@ -1,0 +1,1252 @@
+// mc_kernels.cu — GB300 (sm_103a) kernels of the marching-cubes search path
+// and the C ABI of include/mcgpu.h.
+//
+// Pipeline for one solid (model3d/mc.go:14-49 restated for one GPU):
+//   k_classify  Contains at every grid corner, 32(x) x TY x TZ corner tiles,
+//               leaves culled per tile and the program constant-folded in
+//               shared memory; one bit per corner via warp ballot
+//               (Scan/FetchZ, mc.go:614-692, incl. the border panic).
+//   k_count     per 32-cube chunk of a row: active x/y/z edges (XOR of bit
+//               rows) and triangles (case table in shared memory).
+//   k_scan_*    exclusive prefix sums -> vertex and triangle offsets.
+//   k_emit      edge-keyed vertices (one per crossed edge: exact-coordinate
+//               dedup of mesh.go:822-849 without hashing) and triangles in
+//               table vertex order (mc.go:20-35, :401-407).
+//   k_search    LookupEdgePoint + iters bisection steps per vertex
+//               (mc.go:182-258), leaves culled per warp.
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mcgpu.h"
+#include "mc_internal.h"
+#include "mc_lower.h"
+#include "mc_predicates.cuh"
+
+namespace mcgpu {
+
+// ------------------------------------------------------------ counters
+
+struct Counts {
+    unsigned long long leaf = 0, esc = 0, nodes = 0, tris = 0;
+};
+
+enum StatSlot { ST_LEAF = 0, ST_ESC, ST_NODES, ST_TRIS, ST_TILES_CONST, ST_N };
+enum ErrSlot { ER_BORDER = 0, ER_NOT_ON_EDGE, ER_EDGE_INDEX, ER_LIMIT, ER_N };
+
+__device__ __forceinline__ void flush_counts(const Counts& c, unsigned long long* stats) {
+    unsigned long long v[4] = {c.leaf, c.esc, c.nodes, c.tris};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        unsigned long long x = v[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(&stats[i], x);
+    }
+}
+
+// ------------------------------------------------------------ colliders
+
+// ColliderSolid.Contains (solid.go:292-305): InBounds, then ray parity over
+// the flattened JoinedCollider tree (collisions.go:119-134, :263-273).
+__device__ int collider_64(const ProgView& P, const double* d, P3 p, Counts& cnt, int* err) {
+    if (!(p.x >= d[0] && p.y >= d[1] && p.z >= d[2] && p.x <= d[3] && p.y <= d[4] && p.z <= d[5]))
+        return 0;
+    const TreeD t = P.trees[(int)d[6]];
+    if (t.kind == 0) return 0;
+    if (t.kind == 2) {
+        cnt.tris++;
+        return ray_tri_64(P.tris[t.root], p) & 1;
+    }
+    // Depth-first over child ranges; the hit count is a sum, so order is free.
+    int stk_i[MAX_BVH_DEPTH], stk_e[MAX_BVH_DEPTH];
+    int sp = 0, hits = 0;
+    {
+        const BvhNodeD& n = P.nodes[t.root];
+        cnt.nodes++;
+        if (!ray_box_64(n.lo, n.hi, p)) return 0;
+        stk_i[0] = n.first;
+        stk_e[0] = n.first + n.count;
+        sp = 1;
+    }
+    while (sp > 0) {
+        int i = stk_i[sp - 1];
+        if (i >= stk_e[sp - 1]) {
+            sp--;
+            continue;
+        }
+        stk_i[sp - 1] = i + 1;
+        int c = P.child[i];
+        if (c < 0) {
+            cnt.tris++;
+            hits += ray_tri_64(P.tris[-c - 1], p);
+            continue;
+        }
+        const BvhNodeD& n = P.nodes[c];
+        cnt.nodes++;
+        if (!ray_box_64(n.lo, n.hi, p)) continue;
+        if (sp == MAX_BVH_DEPTH) {
+            atomicOr(&err[ER_LIMIT], 1);
+            return 0;
+        }
+        stk_i[sp] = n.first;
+        stk_e[sp] = n.first + n.count;
+        sp++;
+    }
+    return hits & 1;
+}
+
+// ------------------------------------------------------------ interpreter
+
+__device__ __forceinline__ bool in_box(const XBoxD& b, P3 p) {
+    return p.x >= b.lo[0] && p.y >= b.lo[1] && p.z >= b.lo[2] && p.x <= b.hi[0] && p.y <= b.hi[1] &&
+           p.z <= b.hi[2];
+}
+
+// Apply the inverse steps of a TRANSFORM node (transform.go:44-133).
+__device__ P3 apply_inverse(const ProgView& P, const XBoxD& b, P3 p) {
+    for (int s = 0; s < b.n_steps; s++) {
+        const XStepD& st = P.xstep[b.first_step + s];
+        const double* v = st.v;
+        switch (st.kind) {
+            case MC_XF_TRANSLATE: p = P3{D_ADD(p.x, v[0]), D_ADD(p.y, v[1]), D_ADD(p.z, v[2])}; break;
+            case MC_XF_SCALE: p = P3{D_MUL(p.x, v[0]), D_MUL(p.y, v[0]), D_MUL(p.z, v[0])}; break;
+            case MC_XF_VECSCALE: p = P3{D_MUL(p.x, v[0]), D_MUL(p.y, v[1]), D_MUL(p.z, v[2])}; break;
+            default:
+                p = P3{D_ADD(D_ADD(D_MUL(v[0], p.x), D_MUL(v[1], p.y)), D_MUL(v[2], p.z)),
+                       D_ADD(D_ADD(D_MUL(v[3], p.x), D_MUL(v[4], p.y)), D_MUL(v[5], p.z)),
+                       D_ADD(D_ADD(D_MUL(v[6], p.x), D_MUL(v[7], p.y)), D_MUL(v[8], p.z))};
+        }
+    }
+    return p;
+}
+
+__device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf, int prec, Counts& cnt,
+                                          int* err) {
+    int kind = P.leaf_kind[id];
+    const double* d = P.leaf_d + (size_t)id * LEAF_D;
+    cnt.leaf++;
+    if (prec == MC_PREC_FP32_FILTERED && kind <= LK_CAPSULE) {
+        const float* f = P.leaf_f + (size_t)id * LEAF_F;
+        int r;
+        switch (kind) {
+            case LK_SPHERE: r = sphere_32(f, pf); break;
+            case LK_RECT: r = rect_32(f, pf); break;
+            case LK_CYLINDER: r = cylinder_32(f, pf); break;
+            default: r = capsule_32(f, pf); break;
+        }
+        if (r != 2) return r;
+        cnt.esc++;
+    }
+    switch (kind) {
+        case LK_SPHERE: return sphere_64(d, p);
+        case LK_RECT: return rect_64(d, p);
+        case LK_CYLINDER: return cylinder_64(d, p);
+        case LK_CAPSULE: return capsule_64(d, p);
+        case LK_TORUS: return torus_64(d, p);
+        default: return collider_64(P, d, p, cnt, err);
+    }
+}
+
+// Evaluate a (possibly folded) postfix program at p.  Bit stack: top = bit 0.
+__device__ bool eval_program(const ProgView& P, const uint32_t* q, int nq, P3 p, int prec, Counts& cnt,
+                             int* err) {
+    uint32_t st = 0;
+    P3 saved[MAX_XDEPTH];
+    int sp = 0;
+    F3 pf = to_f3(p);
+    for (int i = 0; i < nq; i++) {
+        uint32_t op = q[i];
+        uint32_t arg = op_arg(op);
+        switch (op_code(op)) {
+            case OP_LEAF: st = (st << 1) | (eval_leaf(P, arg, p, pf, prec, cnt, err) ? 1u : 0u); break;
+            case OP_OR: {
+                uint32_t b = st & 1u;
+                st = (st >> 1) | b;
+                break;
+            }
+            case OP_AND: {
+                uint32_t b = st & 1u;
+                st >>= 1;
+                if (!b) st &= ~1u;
+                break;
+            }
+            case OP_ANDNOT: {
+                uint32_t b = st & 1u;
+                st >>= 1;
+                if (b) st &= ~1u;
+                break;
+            }
+            case OP_NOT: st ^= 1u; break;
+            case OP_XPUSH:
+                saved[sp++] = p;
+                p = apply_inverse(P, P.xbox[arg], p);
+                pf = to_f3(p);
+                break;
+            case OP_XPOP:
+                p = saved[--sp];
+                pf = to_f3(p);
+                if (!in_box(P.xbox[arg], p)) st &= ~1u;
+                break;
+            case OP_BOX: st = (st << 1) | (in_box(P.xbox[arg], p) ? 1u : 0u); break;
+            case OP_BOXAND:
+                if (!in_box(P.xbox[arg], p)) st &= ~1u;
+                break;
+            case OP_TRUE: st = (st << 1) | 1u; break;
+            default: st <<= 1; break;
+        }
+    }
+    return st & 1u;
+}
+
+// ------------------------------------------------------------ grid
+
+struct GridView {
+    const double* xs;
+    const double* ys;
+    const double* zs;
+    int nx, ny, nz;
+    int W;   // 32-bit words per row, including one zero padding word
+    int CX;  // 32-cube chunks per row: ceil((nx-1)/32)
+};
+
+__device__ __forceinline__ bool cull_overlap(const double* c, const double lo[3], const double hi[3]) {
+    // Disjoint iff some axis separates; NaN boxes never separate (never culled).
+    return !(hi[0] < c[0] || lo[0] > c[3] || hi[1] < c[1] || lo[1] > c[4] || hi[2] < c[2] || lo[2] > c[5]);
+}
+
+// ------------------------------------------------------------ k_classify
+
+struct ClassifyArgs {
+    uint32_t* bits;
+    int* err;
+    unsigned long long* stats;
+    int prec;
+    int cull;
+    int ty, tz;  // tile height / depth
+    int ntx, nty, ntz;
+};
+
+__global__ void __launch_bounds__(256) k_classify(GridView g, ProgView P, ClassifyArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t* q = (uint32_t*)smem;                          // n_ops words
+    unsigned char* active = smem + 4 * (size_t)P.n_ops;     // n_leaves bytes
+    __shared__ int s_len;
+    __shared__ const uint32_t* s_prog;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    Counts cnt;
+    unsigned long long nconst = 0;
+    const long long ntiles = (long long)a.ntx * a.nty * a.ntz;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        int tx = (int)(tile % a.ntx);
+        long long r = tile / a.ntx;
+        int ty = (int)(r % a.nty), tz = (int)(r / a.nty);
+        int x0 = tx * 32, y0 = ty * a.ty, z0 = tz * a.tz;
+        int x1 = min(x0 + 31, g.nx - 1), y1 = min(y0 + a.ty - 1, g.ny - 1), z1 = min(z0 + a.tz - 1, g.nz - 1);
+        int any = 0;
+        if (a.cull) {
+            double lo[3] = {g.xs[x0], g.ys[y0], g.zs[z0]};
+            double hi[3] = {g.xs[x1], g.ys[y1], g.zs[z1]};
+            for (int l = threadIdx.x; l < P.n_leaves; l += blockDim.x) {
+                int on = cull_overlap(P.cull + 6 * (size_t)l, lo, hi);
+                active[l] = (unsigned char)on;
+                any |= on;
+            }
+        }
+        any = __syncthreads_or(any);
+        if (threadIdx.x == 0) {
+            if (!a.cull) {
+                s_len = P.n_ops;
+                s_prog = P.ops;
+            } else if (!any) {
+                s_len = P.n_ops_allfalse;
+                s_prog = P.ops_allfalse;
+            } else {
+                s_len = fold_program(P.ops, P.n_ops, [&](uint32_t l) { return active[l] != 0; }, q);
+                s_prog = q;
+            }
+        }
+        __syncthreads();
+        const int len = s_len;
+        const uint32_t* prog = s_prog;
+        if (len < 0) nconst++;
+        const int x = x0 + lane;
+        const bool xin = x < g.nx;
+        const int rows = a.ty * a.tz;
+        for (int rr = warp; rr < rows; rr += nwarp) {
+            int y = y0 + rr % a.ty, z = z0 + rr / a.ty;
+            if (y >= g.ny || z >= g.nz) continue;
+            bool b;
+            if (len == FOLD_FALSE) b = false;
+            else if (len == FOLD_TRUE) b = xin;
+            else b = xin && eval_program(P, prog, len, P3{g.xs[x], g.ys[y], g.zs[z]}, a.prec, cnt, a.err);
+            uint32_t word = __ballot_sync(0xffffffffu, b);
+            if (lane == 0) {
+                a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
+                // solid is true outside of bounds (mc.go:687-689)
+                bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                uint32_t edge_mask = 0;
+                if (x0 == 0) edge_mask |= 1u;
+                if (g.nx - 1 - x0 < 32) edge_mask |= 1u << (g.nx - 1 - x0);
+                if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
+            }
+        }
+        __syncthreads();
+    }
+    flush_counts(cnt, a.stats);
+    if (threadIdx.x == 0 && nconst) atomicAdd(&a.stats[ST_TILES_CONST], nconst);
+}
+
+// ------------------------------------------------------------ case table
+
+struct CaseTable {
+    uint8_t count[256];
+    uint8_t edge[256][15];  // per triangle vertex: axis << 3 | min-corner index
+};
+__constant__ CaseTable c_table;
+
+__device__ __forceinline__ uint32_t shifted(uint32_t w, uint32_t next) { return (w >> 1) | (next << 31); }
+
+__device__ __forceinline__ uint32_t valid_mask(const GridView& g, int c) {
+    int n = g.nx - 1 - 32 * c;
+    return n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
+}
+
+struct Rows {
+    uint32_t r[4], n[4];  // rows (y,z), (y+1,z), (y,z+1), (y+1,z+1): word c and c+1
+};
+__device__ __forceinline__ Rows load_rows(const GridView& g, const uint32_t* bits, int c, int y, int z) {
+    Rows R;
+    const size_t W = g.W;
+    size_t b00 = ((size_t)z * g.ny + y) * W + c;
+    size_t off[4] = {b00, b00 + W, b00 + (size_t)g.ny * W, b00 + (size_t)g.ny * W + W};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        R.r[k] = __ldg(bits + off[k]);
+        R.n[k] = __ldg(bits + off[k] + 1);
+    }
+    return R;
+}
+
+// Corner planes of the 32 cubes of a chunk, in mcCorner order (mc.go:263-285).
+__device__ __forceinline__ void corner_planes(const Rows& R, uint32_t cp[8]) {
+    cp[0] = R.r[0];
+    cp[1] = shifted(R.r[0], R.n[0]);
+    cp[2] = R.r[1];
+    cp[3] = shifted(R.r[1], R.n[1]);
+    cp[4] = R.r[2];
+    cp[5] = shifted(R.r[2], R.n[2]);
+    cp[6] = R.r[3];
+    cp[7] = shifted(R.r[3], R.n[3]);
+}
+
+__device__ __forceinline__ int cube_case(const uint32_t cp[8], int b) {
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) k |= ((cp[i] >> b) & 1u) << i;
+    return k;
+}
+
+// ------------------------------------------------------------ k_count
+
+struct CountArgs {
+    const uint32_t* bits;
+    uint32_t* packed;    // per chunk: cx | cy << 6 | cz << 12 | ntri << 18
+    uint32_t* blocksum;  // per block: 2 x u32 (vertices, triangles)
+    long long nchunks;
+};
+
+__device__ __forceinline__ void block_sum2(uint32_t& a, uint32_t& b) {
+    __shared__ uint32_t sa[32], sb[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        sa[w] = a;
+        sb[w] = b;
+    }
+    __syncthreads();
+    if (w == 0) {
+        int nw = blockDim.x >> 5;
+        a = l < nw ? sa[l] : 0;
+        b = l < nw ? sb[l] : 0;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_count(GridView g, CountArgs a) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t nv = 0, nt = 0;
+    if (i < a.nchunks) {
+        int c = (int)(i % g.CX);
+        long long r = i / g.CX;
+        int y = (int)(r % (g.ny - 1)), z = (int)(r / (g.ny - 1));
+        Rows R = load_rows(g, a.bits, c, y, z);
+        uint32_t vm = valid_mask(g, c);
+        uint32_t cp[8];
+        corner_planes(R, cp);
+        uint32_t xm = (cp[0] ^ cp[1]) & vm, ym = (R.r[0] ^ R.r[1]) & vm, zm = (R.r[0] ^ R.r[2]) & vm;
+        uint32_t all = cp[0], anyb = cp[0];
+#pragma unroll
+        for (int k = 1; k < 8; k++) {
+            all &= cp[k];
+            anyb |= cp[k];
+        }
+        uint32_t act = anyb & ~all & vm;
+        while (act) {
+            int b = __ffs(act) - 1;
+            act &= act - 1;
+            nt += c_table.count[cube_case(cp, b)];
+        }
+        uint32_t cx = __popc(xm), cy = __popc(ym), cz = __popc(zm);
+        nv = cx + cy + cz;
+        a.packed[i] = cx | (cy << 6) | (cz << 12) | (nt << 18);
+    }
+    block_sum2(nv, nt);
+    if (threadIdx.x == 0) {
+        a.blocksum[2 * blockIdx.x] = nv;
+        a.blocksum[2 * blockIdx.x + 1] = nt;
+    }
+}
+
+// Exclusive scan of the per-block sums by one CTA; totals at out[2*nb..].
+__global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t* blocksum, unsigned long long* blockoff,
+                                                      int nb, unsigned long long* totals) {
+    __shared__ unsigned long long sv[1024], st[1024];
+    int t = threadIdx.x, T = blockDim.x;
+    int per = (nb + T - 1) / T;
+    int b0 = t * per, b1 = min(nb, b0 + per);
+    unsigned long long v = 0, w = 0;
+    for (int b = b0; b < b1; b++) {
+        v += blocksum[2 * b];
+        w += blocksum[2 * b + 1];
+    }
+    sv[t] = v;
+    st[t] = w;
+    __syncthreads();
+    for (int o = 1; o < T; o <<= 1) {  // Hillis-Steele inclusive scan
+        unsigned long long av = t >= o ? sv[t - o] : 0, aw = t >= o ? st[t - o] : 0;
+        __syncthreads();
+        sv[t] += av;
+        st[t] += aw;
+        __syncthreads();
+    }
+    unsigned long long ov = sv[t] - v, ow = st[t] - w;
+    for (int b = b0; b < b1; b++) {
+        blockoff[2 * b] = ov;
+        blockoff[2 * b + 1] = ow;
+        ov += blocksum[2 * b];
+        ow += blocksum[2 * b + 1];
+    }
+    if (t == T - 1) {
+        totals[0] = sv[t];
+        totals[1] = st[t];
+    }
+}
+
+// Per-chunk exclusive offsets (vertex, triangle) as two u32 arrays.
+__global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* packed, const unsigned long long* blockoff,
+                                                     long long nchunks, uint32_t* prefv, uint32_t* preft) {
+    __shared__ uint32_t sv[256], st[256];
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t p = i < nchunks ? packed[i] : 0;
+    uint32_t v = (p & 63u) + ((p >> 6) & 63u) + ((p >> 12) & 63u), w = p >> 18;
+    int t = threadIdx.x;
+    sv[t] = v;
+    st[t] = w;
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {
+        uint32_t av = t >= o ? sv[t - o] : 0, aw = t >= o ? st[t - o] : 0;
+        __syncthreads();
+        sv[t] += av;
+        st[t] += aw;
+        __syncthreads();
+    }
+    if (i < nchunks) {
+        prefv[i] = (uint32_t)(blockoff[2 * blockIdx.x] + sv[t] - v);
+        preft[i] = (uint32_t)(blockoff[2 * blockIdx.x + 1] + st[t] - w);
+    }
+}
+
+// ------------------------------------------------------------ k_emit
+
+struct EmitArgs {
+    const uint32_t* bits;
+    const uint32_t* packed;
+    const uint32_t* prefv;
+    const uint32_t* preft;
+    unsigned long long* keys;  // per vertex: axis << 60 | z << 40 | y << 20 | x
+    int32_t* tris;
+    long long nchunks;
+};
+
+__global__ void __launch_bounds__(256) k_emit(GridView g, EmitArgs a) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nchunks) return;
+    uint32_t pk = a.packed[i];
+    if (pk == 0) return;
+    const int c = (int)(i % g.CX);
+    const long long r = i / g.CX;
+    const int y = (int)(r % (g.ny - 1)), z = (int)(r / (g.ny - 1));
+    Rows R = load_rows(g, a.bits, c, y, z);
+    const uint32_t vm = valid_mask(g, c);
+    uint32_t cp[8];
+    corner_planes(R, cp);
+    // Vertices of the edges whose base corner is in this chunk.
+    {
+        uint32_t m[3] = {(cp[0] ^ cp[1]) & vm, (R.r[0] ^ R.r[1]) & vm, (R.r[0] ^ R.r[2]) & vm};
+        uint32_t id = a.prefv[i];
+        for (int ax = 0; ax < 3; ax++) {
+            uint32_t mm = m[ax];
+            while (mm) {
+                int b = __ffs(mm) - 1;
+                mm &= mm - 1;
+                unsigned long long key = ((unsigned long long)ax << 60) | ((unsigned long long)z << 40) |
+                                         ((unsigned long long)y << 20) | (unsigned long long)(32 * c + b);
+                a.keys[id++] = key;
+            }
+        }
+    }
+    uint32_t nt = pk >> 18;
+    if (nt == 0) return;
+    // Edge masks of the neighbouring rows (same word c) for rank queries.
+    // x-edges of rows k=(dy,dz): cp[2k] ^ cp[2k+1]; y-edges of rows (y, z+dz):
+    // r(y,z+dz) ^ r(y+1,z+dz); z-edges of rows (y+dy, z): r(y+dy,z) ^ r(y+dy,z+1).
+    const long long rowC = (long long)(g.ny - 1);
+    uint32_t t_out = a.preft[i];
+    uint32_t all = cp[0], anyb = cp[0];
+#pragma unroll
+    for (int k = 1; k < 8; k++) {
+        all &= cp[k];
+        anyb |= cp[k];
+    }
+    uint32_t act = anyb & ~all & vm;
+    while (act) {
+        int b = __ffs(act) - 1;
+        act &= act - 1;
+        int kc = cube_case(cp, b);
+        int ntri = c_table.count[kc];
+        for (int e = 0; e < 3 * ntri; e++) {
+            int code = c_table.edge[kc][e];
+            int ax = code >> 3, corner = code & 7;
+            int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
+            int bb = b + dx, cc = c;
+            if (bb == 32) {
+                bb = 0;
+                cc = c + 1;
+            }
+            long long ci = ((long long)(z + dz) * rowC + (y + dy)) * g.CX + cc;
+            uint32_t mask;
+            if (ax == 0) {
+                int k = dy + 2 * dz;
+                mask = (cp[2 * k] ^ cp[2 * k + 1]) & vm;
+            } else if (ax == 1) {
+                mask = dz ? (R.r[2] ^ R.r[3]) : (R.r[0] ^ R.r[1]);
+            } else {
+                mask = dy ? (R.r[1] ^ R.r[3]) : (R.r[0] ^ R.r[2]);
+            }
+            uint32_t rank = bb ? __popc(mask & ((1u << bb) - 1u)) : 0u;
+            uint32_t pn = a.packed[ci];
+            uint32_t id = a.prefv[ci] + rank;
+            if (ax >= 1) id += pn & 63u;
+            if (ax == 2) id += (pn >> 6) & 63u;
+            a.tris[3 * (size_t)t_out + (e % 3)] = (int32_t)id;
+            if (e % 3 == 2) t_out++;
+        }
+    }
+}
+
+// ------------------------------------------------------------ k_search
+
+struct SearchArgs {
+    const unsigned long long* keys;
+    double* verts;  // V x 3
+    long long nverts;
+    int iters;
+    int prec;
+    int cull;
+    int* err;
+    unsigned long long* stats;
+};
+
+__device__ __forceinline__ double warp_min(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t per_warp = 4 * (size_t)P.n_ops + (((size_t)P.n_leaves + 15) & ~(size_t)15);
+    uint32_t* q = (uint32_t*)(smem + warp * per_warp);
+    unsigned char* active = smem + warp * per_warp + 4 * (size_t)P.n_ops;
+    Counts cnt;
+    const long long nwarps_total = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long base = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * 32; base < a.nverts;
+         base += nwarps_total * 32) {
+        long long v = base + lane;
+        bool live = v < a.nverts;
+        int axis = 0;
+        double lo = 0, hi = 0;
+        P3 cpt{0, 0, 0};
+        int status = 0;  // 0 ok, 1 not on edge, 2 index
+        if (live) {
+            unsigned long long key = a.keys[v];
+            int ax = (int)(key >> 60);
+            int z = (int)((key >> 40) & 0xfffff), y = (int)((key >> 20) & 0xfffff), x = (int)(key & 0xfffff);
+            P3 c0{g.xs[x], g.ys[y], g.zs[z]};
+            P3 c1 = c0;
+            if (ax == 0) c1.x = g.xs[x + 1];
+            else if (ax == 1) c1.y = g.ys[y + 1];
+            else c1.z = g.zs[z + 1];
+            // corners[a].Mid(corners[b]) (mc.go:401-407, coords.go:196-198)
+            cpt = P3{D_MUL(D_ADD(c0.x, c1.x), 0.5), D_MUL(D_ADD(c0.y, c1.y), 0.5), D_MUL(D_ADD(c0.z, c1.z), 0.5)};
+            if (a.iters != 0) {
+                // LookupEdgePoint (mc.go:647-660)
+                const double org[3] = {g.xs[0], g.ys[0], g.zs[0]};
+                const double* vals[3] = {g.xs, g.ys, g.zs};
+                const int nvals[3] = {g.nx, g.ny, g.nz};
+                double dl = D_SUB(g.xs[1], g.xs[0]);
+                double q1 = D_DIV(dl, 4.0), q3 = D_DIV(D_MUL(3.0, dl), 4.0);
+                axis = -1;
+                for (int i = 0; i < 3; i++) {
+                    double ci = comp(cpt, i);
+                    double m = fabs(fmod(D_SUB(ci, org[i]), dl));
+                    if (m > q1 && m < q3) {
+                        long long idx = __double2ll_rz(D_DIV(D_SUB(ci, org[i]), dl));
+                        if (idx < 0 || idx + 1 >= nvals[i]) {
+                            status = 2;
+                        } else {
+                            axis = i;
+                            lo = vals[i][idx];
+                            hi = vals[i][idx + 1];
+                        }
+                        break;
+                    }
+                }
+                if (axis < 0 && status == 0) status = 1;
+            }
+        }
+        if (status == 1) atomicOr(&a.err[ER_NOT_ON_EDGE], 1);
+        if (status == 2) atomicOr(&a.err[ER_EDGE_INDEX], 1);
+        const bool work = live && a.iters != 0 && status == 0;
+        // Per-warp culling box: union of the segments this warp bisects.
+        const uint32_t* prog = P.ops;
+        int len = P.n_ops;
+        if (a.cull && __any_sync(0xffffffffu, work)) {
+            double blo[3], bhi[3];
+            for (int i = 0; i < 3; i++) {
+                double vlo = work ? comp(cpt, i) : CUDART_INF, vhi = work ? comp(cpt, i) : -CUDART_INF;
+                if (work && i == axis) {
+                    vlo = fmin(lo, hi);
+                    vhi = fmax(lo, hi);
+                }
+                blo[i] = warp_min(vlo);
+                bhi[i] = warp_max(vhi);
+            }
+            for (int l = lane; l < P.n_leaves; l += 32) active[l] = (unsigned char)cull_overlap(P.cull + 6 * (size_t)l, blo, bhi);
+            __syncwarp();
+            int L = 0;
+            if (lane == 0) L = fold_program(P.ops, P.n_ops, [&](uint32_t l) { return active[l] != 0; }, q);
+            L = __shfl_sync(0xffffffffu, L, 0);
+            __syncwarp();
+            prog = q;
+            len = L;
+        }
+        if (live && status == 0) {
+            P3 out = cpt;
+            if (work) {
+                // mcSearchPoint (mc.go:223-258)
+                auto contains = [&](P3 pt) -> bool {
+                    if (len == FOLD_FALSE) return false;
+                    if (len == FOLD_TRUE) return true;
+                    return eval_program(P, prog, len, pt, a.prec, cnt, a.err);
+                };
+                double fp = lo, tp = hi;
+                P3 t = cpt;
+                set_comp(t, axis, tp);
+                if (!contains(t)) {
+                    fp = hi;
+                    tp = lo;
+                }
+                P3 arr = cpt;
+                for (int k = 0; k < a.iters; k++) {
+                    double mid = D_DIV(D_ADD(fp, tp), 2.0);
+                    set_comp(arr, axis, mid);
+                    if (contains(arr)) tp = mid;
+                    else fp = mid;
+                }
+                set_comp(arr, axis, D_DIV(D_ADD(fp, tp), 2.0));
+                out = arr;
+            }
+            a.verts[3 * v] = out.x;
+            a.verts[3 * v + 1] = out.y;
+            a.verts[3 * v + 2] = out.z;
+        }
+        __syncwarp();
+    }
+    flush_counts(cnt, a.stats);
+}
+
+// ------------------------------------------------------------ k_contains
+
+__global__ void k_contains(ProgView P, const double* pts, long long n, int prec, uint8_t* out, int* err,
+                           unsigned long long* stats) {
+    Counts cnt;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        P3 p{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+        out[i] = eval_program(P, P.ops, P.n_ops, p, prec, cnt, err) ? 1 : 0;
+    }
+    flush_counts(cnt, stats);
+}
+
+}  // namespace mcgpu
+
+// ======================================================================
+// Host side: contexts, buffers, the C ABI.
+
+using namespace mcgpu;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T>
+    T* as() const {
+        return (T*)p;
+    }
+};
+
+std::once_flag g_table_once;
+CaseTable g_table_host;
+int g_table_status = 0;
+
+void build_table_host() {
+    uint8_t counts[256], tris[256][5][6];
+    g_table_status = build_case_table(counts, tris);
+    std::memset(&g_table_host, 0, sizeof(g_table_host));
+    for (int c = 0; c < 256; c++) {
+        g_table_host.count[c] = counts[c];
+        for (int t = 0; t < counts[c]; t++)
+            for (int k = 0; k < 3; k++) {
+                int a = tris[c][t][2 * k], b = tris[c][t][2 * k + 1];
+                int diff = a ^ b;
+                int axis = diff == 1 ? 0 : (diff == 2 ? 1 : 2);
+                int lo = a < b ? a : b;
+                g_table_host.edge[c][3 * t + k] = (uint8_t)((axis << 3) | lo);
+            }
+    }
+}
+
+}  // namespace
+
+struct mc_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    std::string err;
+    DevBuf xs, ys, zs, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
+    DevBuf pts, pout;
+    unsigned long long* h_pin = nullptr;  // pinned: totals[2], stats[ST_N], errs (as ints) ...
+    int64_t last_V = 0, last_T = 0;
+    int sm_count = 152;
+};
+
+struct mc_solid {
+    mc_ctx* ctx = nullptr;
+    HostProgram host;
+    DevBuf buf;
+    ProgView view{};
+};
+
+namespace {
+
+mc_status fail(mc_ctx* ctx, mc_status s, const std::string& m) {
+    if (ctx) ctx->err = m;
+    return s;
+}
+
+#define CK(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? MC_ERR_OOM : MC_ERR_CUDA,            \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                          \
+    } while (0)
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+mc_opts default_opts(const mc_opts* o) {
+    mc_opts r{};
+    r.precision = MC_PREC_FP32_FILTERED;
+    r.cull = 1;
+    r.tile_y = 0;
+    r.tile_z = 0;
+    if (o) {
+        r.precision = o->precision;
+        r.cull = o->cull;
+        r.tile_y = o->tile_y;
+        r.tile_z = o->tile_z;
+    }
+    return r;
+}
+
+bool bounds_valid(const double* mn, const double* mx) {  // BoundsValid, bounder.go:30-46
+    double smn = mn[0] + mn[1] + mn[2], smx = mx[0] + mx[1] + mx[2];
+    if (std::isnan(smn) || std::isnan(smx) || std::isinf(smn) || std::isinf(smx)) return false;
+    return !(mx[0] < mn[0] || mx[1] < mn[1] || mx[2] < mn[2]);
+}
+
+constexpr int64_t kMaxAxis = (1 << 20) - 2;        // keys pack 20-bit indices
+constexpr int64_t kMaxCorners = (int64_t)1 << 31;  // int32 vertex indices
+
+}  // namespace
+
+extern "C" {
+
+const char* mc_version(void) { return "mcgpu 0.1 (sm_103a)"; }
+
+const char* mc_status_string(mc_status s) {
+    switch (s) {
+        case MC_OK: return "ok";
+        case MC_ERR_INVALID_BOUNDS: return "invalid bounds";
+        case MC_ERR_BOUNDS_INSIDE: return "solid is true outside of bounds";
+        case MC_ERR_NOT_ON_EDGE: return "vertex not on edge";
+        case MC_ERR_EDGE_INDEX: return "index out of range";
+        case MC_ERR_BAD_PROGRAM: return "malformed solid serialisation";
+        case MC_ERR_NOT_LOWERABLE: return "solid cannot be lowered to the device";
+        case MC_ERR_OOM: return "out of device memory";
+        case MC_ERR_TIMEOUT: return "device wait timed out";
+        case MC_ERR_CUDA: return "CUDA error";
+        case MC_ERR_ARG: return "invalid argument";
+        case MC_ERR_GRID: return "grid does not terminate or is too large";
+        case MC_ERR_LIMIT: return "device program limit exceeded";
+    }
+    return "unknown status";
+}
+
+const char* mc_last_error(const mc_ctx* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+mc_status mc_create(mc_ctx** out, int device) {
+    if (!out) return MC_ERR_ARG;
+    *out = nullptr;
+    std::call_once(g_table_once, build_table_host);
+    if (g_table_status != 0) return MC_ERR_LIMIT;
+    std::unique_ptr<mc_ctx> c(new mc_ctx());
+    mc_ctx* ctx = c.get();
+    c->device = device;
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    for (auto& e : c->ev) CK(cudaEventCreate(&e));
+    CK(cudaMemcpyToSymbolAsync(c_table, &g_table_host, sizeof(CaseTable), 0, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaHostAlloc((void**)&c->h_pin, 64 * sizeof(unsigned long long), cudaHostAllocDefault));
+    CK(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
+    CK(cudaStreamSynchronize(c->stream));
+    *out = c.release();
+    return MC_OK;
+}
+
+void mc_destroy(mc_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (DevBuf* b : {&ctx->xs, &ctx->ys, &ctx->zs, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
+                      &ctx->prefv, &ctx->preft, &ctx->keys, &ctx->verts, &ctx->tris, &ctx->stats, &ctx->errs,
+                      &ctx->totals, &ctx->pts, &ctx->pout})
+        b->release();
+    for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets,
+                          size_t n_sets, mc_solid** out) {
+    if (!ctx || !out) return MC_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<mc_solid> s(new mc_solid());
+    s->ctx = ctx;
+    try {
+        lower_scene(nodes, n_nodes, sets, n_sets, &s->host);
+    } catch (const LowerError& e) {
+        return fail(ctx, e.status, e.what());
+    } catch (const std::exception& e) {
+        return fail(ctx, MC_ERR_BAD_PROGRAM, e.what());
+    }
+    HostProgram& H = s->host;
+    // One device allocation holding every table, 256-byte aligned pieces.
+    struct Piece {
+        const void* src;
+        size_t bytes;
+        size_t off;
+    };
+    std::vector<Piece> pcs = {
+        {H.ops.data(), H.ops.size() * 4, 0},
+        {H.ops_allfalse.data(), H.ops_allfalse.size() * 4, 0},
+        {H.leaf_kind.data(), H.leaf_kind.size() * 4, 0},
+        {H.leaf_d.data(), H.leaf_d.size() * 8, 0},
+        {H.leaf_f.data(), H.leaf_f.size() * 4, 0},
+        {H.cull.data(), H.cull.size() * 8, 0},
+        {H.xbox.data(), H.xbox.size() * sizeof(XBoxD), 0},
+        {H.xstep.data(), H.xstep.size() * sizeof(XStepD), 0},
+        {H.trees.data(), H.trees.size() * sizeof(TreeD), 0},
+        {H.nodes.data(), H.nodes.size() * sizeof(BvhNodeD), 0},
+        {H.nodes_f.data(), H.nodes_f.size() * sizeof(BvhNodeF), 0},
+        {H.child.data(), H.child.size() * 4, 0},
+        {H.tris.data(), H.tris.size() * sizeof(TriD), 0},
+        {H.tris_f.data(), H.tris_f.size() * sizeof(TriF), 0},
+    };
+    size_t total = 0;
+    for (auto& p : pcs) {
+        p.off = total;
+        total += align256(p.bytes);
+    }
+    CK(cudaSetDevice(ctx->device));
+    CK(s->buf.ensure(total));
+    std::vector<unsigned char> staging(total, 0);
+    for (auto& p : pcs)
+        if (p.bytes) std::memcpy(staging.data() + p.off, p.src, p.bytes);
+    CK(cudaMemcpyAsync(s->buf.p, staging.data(), total, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    unsigned char* b = (unsigned char*)s->buf.p;
+    ProgView& v = s->view;
+    v.ops = (const uint32_t*)(b + pcs[0].off);
+    v.ops_allfalse = (const uint32_t*)(b + pcs[1].off);
+    v.leaf_kind = (const int32_t*)(b + pcs[2].off);
+    v.leaf_d = (const double*)(b + pcs[3].off);
+    v.leaf_f = (const float*)(b + pcs[4].off);
+    v.cull = (const double*)(b + pcs[5].off);
+    v.xbox = (const XBoxD*)(b + pcs[6].off);
+    v.xstep = (const XStepD*)(b + pcs[7].off);
+    v.trees = (const TreeD*)(b + pcs[8].off);
+    v.nodes = (const BvhNodeD*)(b + pcs[9].off);
+    v.nodes_f = (const BvhNodeF*)(b + pcs[10].off);
+    v.child = (const int32_t*)(b + pcs[11].off);
+    v.tris = (const TriD*)(b + pcs[12].off);
+    v.tris_f = (const TriF*)(b + pcs[13].off);
+    v.n_ops = (int32_t)H.ops.size();
+    v.n_ops_allfalse = H.n_ops_allfalse;
+    v.n_leaves = (int32_t)H.leaf_kind.size();
+    v.n_xbox = (int32_t)H.xbox.size();
+    *out = s.release();
+    return MC_OK;
+}
+
+void mc_solid_destroy(mc_solid* s) {
+    if (!s) return;
+    if (s->ctx) {
+        cudaSetDevice(s->ctx->device);
+        cudaStreamSynchronize(s->ctx->stream);
+    }
+    s->buf.release();
+    delete s;
+}
+
+mc_status mc_solid_bounds(const mc_solid* s, double mn[3], double mx[3]) {
+    if (!s || !mn || !mx) return MC_ERR_ARG;
+    for (int i = 0; i < 3; i++) {
+        mn[i] = s->host.root_min[i];
+        mx[i] = s->host.root_max[i];
+    }
+    return MC_OK;
+}
+
+mc_status mc_spacer_axis(double lo, double hi, double delta, double* out, int64_t cap, int64_t* n) {
+    std::vector<double> v;
+    int st = spacer_axis(lo, hi, delta, &v, kMaxAxis + 2);
+    if (n) *n = (int64_t)v.size();
+    if (out)
+        for (int64_t i = 0; i < (int64_t)v.size() && i < cap; i++) out[i] = v[i];
+    return (mc_status)st;
+}
+
+mc_status mc_case_table(uint8_t counts[256], uint8_t tris[256][5][6]) {
+    return build_case_table(counts, tris) == 0 ? MC_OK : MC_ERR_LIMIT;
+}
+
+mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters,
+                           const mc_opts* opts_in, int64_t* n_vertices, int64_t* n_triangles, mc_stats* stats_out) {
+    if (!ctx || !solid || iters < 0) return fail(ctx, MC_ERR_ARG, "bad argument");
+    ctx->last_V = ctx->last_T = 0;
+    mc_opts opts = default_opts(opts_in);
+    const HostProgram& H = solid->host;
+    if (!bounds_valid(H.root_min, H.root_max)) return fail(ctx, MC_ERR_INVALID_BOUNDS, "invalid bounds");
+    // newSquareSpacer (mc.go:594-608)
+    std::vector<double> X, Y, Z;
+    if (spacer_axis(H.root_min[0], H.root_max[0], delta, &X, kMaxAxis + 1) ||
+        spacer_axis(H.root_min[1], H.root_max[1], delta, &Y, kMaxAxis + 1) ||
+        spacer_axis(H.root_min[2], H.root_max[2], delta, &Z, kMaxAxis + 1))
+        return fail(ctx, MC_ERR_GRID, "spacer does not terminate or exceeds the axis limit");
+    const int nx = (int)X.size(), ny = (int)Y.size(), nz = (int)Z.size();
+    if ((int64_t)nx * ny * nz > kMaxCorners) return fail(ctx, MC_ERR_GRID, "grid exceeds the corner limit");
+    mc_stats st{};
+    st.nx = nx;
+    st.ny = ny;
+    st.nz = nz;
+    st.corners = (int64_t)nx * ny * nz;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t sm = ctx->stream;
+
+    GridView g{};
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.W = (nx + 31) / 32 + 1;
+    g.CX = nx >= 2 ? (nx - 1 + 31) / 32 : 0;
+    CK(ctx->xs.ensure(nx * 8));
+    CK(ctx->ys.ensure(ny * 8));
+    CK(ctx->zs.ensure(nz * 8));
+    CK(ctx->stats.ensure(ST_N * 8));
+    CK(ctx->errs.ensure(ER_N * 4));
+    CK(ctx->totals.ensure(16));
+    CK(cudaMemcpyAsync(ctx->xs.p, X.data(), nx * 8, cudaMemcpyHostToDevice, sm));
+    CK(cudaMemcpyAsync(ctx->ys.p, Y.data(), ny * 8, cudaMemcpyHostToDevice, sm));
+    CK(cudaMemcpyAsync(ctx->zs.p, Z.data(), nz * 8, cudaMemcpyHostToDevice, sm));
+    CK(cudaMemsetAsync(ctx->stats.p, 0, ST_N * 8, sm));
+    CK(cudaMemsetAsync(ctx->errs.p, 0, ER_N * 4, sm));
+    CK(cudaMemsetAsync(ctx->totals.p, 0, 16, sm));
+    g.xs = ctx->xs.as<double>();
+    g.ys = ctx->ys.as<double>();
+    g.zs = ctx->zs.as<double>();
+    const size_t nbits = (size_t)nz * ny * g.W;
+    CK(ctx->bits.ensure(nbits * 4));
+    CK(cudaMemsetAsync(ctx->bits.p, 0, nbits * 4, sm));
+
+    const ProgView& P = solid->view;
+    CK(cudaEventRecord(ctx->ev[0], sm));
+    // ---- classify
+    ClassifyArgs ca{};
+    ca.bits = ctx->bits.as<uint32_t>();
+    ca.err = ctx->errs.as<int>();
+    ca.stats = ctx->stats.as<unsigned long long>();
+    ca.prec = opts.precision;
+    ca.cull = opts.cull;
+    ca.ty = opts.tile_y > 0 ? opts.tile_y : 8;
+    ca.tz = opts.tile_z > 0 ? opts.tile_z : 8;
+    ca.ntx = (nx + 31) / 32;
+    ca.nty = (ny + ca.ty - 1) / ca.ty;
+    ca.ntz = (nz + ca.tz - 1) / ca.tz;
+    long long ntiles = (long long)ca.ntx * ca.nty * ca.ntz;
+    st.tiles = ntiles;
+    size_t smem_c = 4 * (size_t)P.n_ops + (size_t)P.n_leaves + 16;
+    if (smem_c > 48 * 1024) CK(cudaFuncSetAttribute(k_classify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+    int grid_c = (int)std::min<long long>(ntiles, (long long)ctx->sm_count * 8);
+    k_classify<<<grid_c, 256, smem_c, sm>>>(g, P, ca);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev[1], sm));
+
+    long long nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)g.CX * (ny - 1) * (nz - 1) : 0;
+    int nblk = (int)((nchunks + 255) / 256);
+    if (nchunks > 0) {
+        CK(ctx->packed.ensure(nchunks * 4));
+        CK(ctx->blocksum.ensure((size_t)nblk * 8));
+        CK(ctx->blockoff.ensure((size_t)nblk * 16));
+        CK(ctx->prefv.ensure(nchunks * 4));
+        CK(ctx->preft.ensure(nchunks * 4));
+        CountArgs cn{ctx->bits.as<uint32_t>(), ctx->packed.as<uint32_t>(), ctx->blocksum.as<uint32_t>(), nchunks};
+        k_count<<<nblk, 256, 0, sm>>>(g, cn);
+        CK(cudaGetLastError());
+        k_scan_blocks<<<1, 1024, 0, sm>>>(ctx->blocksum.as<uint32_t>(), ctx->blockoff.as<unsigned long long>(), nblk,
+                                          ctx->totals.as<unsigned long long>());
+        CK(cudaGetLastError());
+        k_scan_chunks<<<nblk, 256, 0, sm>>>(ctx->packed.as<uint32_t>(), ctx->blockoff.as<unsigned long long>(),
+                                            nchunks, ctx->prefv.as<uint32_t>(), ctx->preft.as<uint32_t>());
+        CK(cudaGetLastError());
+    }
+    unsigned long long* hp = ctx->h_pin;
+    CK(cudaMemcpyAsync(hp, ctx->totals.p, 16, cudaMemcpyDeviceToHost, sm));
+    CK(cudaMemcpyAsync(hp + 2, ctx->errs.p, ER_N * 4, cudaMemcpyDeviceToHost, sm));
+    CK(cudaStreamSynchronize(sm));
+    const int* herr = (const int*)(hp + 2);
+    if (herr[ER_BORDER]) return fail(ctx, MC_ERR_BOUNDS_INSIDE, "solid is true outside of bounds");
+    if (herr[ER_LIMIT]) return fail(ctx, MC_ERR_LIMIT, "collider traversal stack exceeded");
+    const long long V = (long long)hp[0], T = (long long)hp[1];
+    if (V >= ((long long)1 << 31) || T >= ((long long)1 << 31))
+        return fail(ctx, MC_ERR_LIMIT, "mesh exceeds 2^31 vertices or triangles");
+    st.vertices = V;
+    st.triangles = T;
+    CK(ctx->keys.ensure(std::max<long long>(V, 1) * 8));
+    CK(ctx->verts.ensure(std::max<long long>(V, 1) * 24));
+    CK(ctx->tris.ensure(std::max<long long>(T, 1) * 12));
+    CK(cudaEventRecord(ctx->ev[2], sm));
+    if (nchunks > 0 && (V > 0 || T > 0)) {
+        EmitArgs ea{ctx->bits.as<uint32_t>(), ctx->packed.as<uint32_t>(), ctx->prefv.as<uint32_t>(),
+                    ctx->preft.as<uint32_t>(), ctx->keys.as<unsigned long long>(), ctx->tris.as<int32_t>(), nchunks};
+        k_emit<<<nblk, 256, 0, sm>>>(g, ea);
+        CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(ctx->ev[3], sm));
+    if (V > 0) {
+        SearchArgs sa{};
+        sa.keys = ctx->keys.as<unsigned long long>();
+        sa.verts = ctx->verts.as<double>();
+        sa.nverts = V;
+        sa.iters = iters;
+        sa.prec = opts.precision;
+        sa.cull = opts.cull;
+        sa.err = ctx->errs.as<int>();
+        sa.stats = ctx->stats.as<unsigned long long>();
+        size_t per_warp = 4 * (size_t)P.n_ops + (((size_t)P.n_leaves + 15) & ~(size_t)15);
+        size_t smem_s = 4 * per_warp;
+        if (smem_s > 48 * 1024)
+            CK(cudaFuncSetAttribute(k_search, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s));
+        int grid_s = (int)std::min<long long>((V + 127) / 128, (long long)ctx->sm_count * 16);
+        k_search<<<grid_s, 128, smem_s, sm>>>(g, P, sa);
+        CK(cudaGetLastError());
+    }
+    CK(cudaEventRecord(ctx->ev[4], sm));
+    CK(cudaMemcpyAsync(hp + 8, ctx->stats.p, ST_N * 8, cudaMemcpyDeviceToHost, sm));
+    CK(cudaMemcpyAsync(hp + 2, ctx->errs.p, ER_N * 4, cudaMemcpyDeviceToHost, sm));
+    CK(cudaStreamSynchronize(sm));
+    if (herr[ER_NOT_ON_EDGE]) return fail(ctx, MC_ERR_NOT_ON_EDGE, "vertex not on edge");
+    if (herr[ER_EDGE_INDEX]) return fail(ctx, MC_ERR_EDGE_INDEX, "index out of range");
+    if (herr[ER_LIMIT]) return fail(ctx, MC_ERR_LIMIT, "collider traversal stack exceeded");
+    st.leaf_evals = (int64_t)hp[8 + ST_LEAF];
+    st.escalations = (int64_t)hp[8 + ST_ESC];
+    st.bvh_nodes = (int64_t)hp[8 + ST_NODES];
+    st.bvh_tris = (int64_t)hp[8 + ST_TRIS];
+    st.tiles_const = (int64_t)hp[8 + ST_TILES_CONST];
+    float ms;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    st.ms_classify = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    st.ms_cubes = ms;
+    float ms_emit;
+    cudaEventElapsedTime(&ms_emit, ctx->ev[2], ctx->ev[3]);
+    st.ms_cubes += ms_emit;
+    cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
+    st.ms_search = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[4]);
+    st.ms_total = ms;
+    ctx->last_V = V;
+    ctx->last_T = T;
+    if (n_vertices) *n_vertices = V;
+    if (n_triangles) *n_triangles = T;
+    if (stats_out) *stats_out = st;
+    return MC_OK;
+}
+
+mc_status mc_result_device(const mc_ctx* ctx, const double** vertices, const int32_t** triangles) {
+    if (!ctx) return MC_ERR_ARG;
+    if (vertices) *vertices = ctx->verts.as<double>();
+    if (triangles) *triangles = ctx->tris.as<int32_t>();
+    return MC_OK;
+}
+
+mc_status mc_result_copy(mc_ctx* ctx, double* vertices, int32_t* triangles) {
+    if (!ctx) return MC_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    if (vertices && ctx->last_V)
+        CK(cudaMemcpyAsync(vertices, ctx->verts.p, ctx->last_V * 24, cudaMemcpyDeviceToHost, ctx->stream));
+    if (triangles && ctx->last_T)
+        CK(cudaMemcpyAsync(triangles, ctx->tris.p, ctx->last_T * 12, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MC_OK;
+}
+
+mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters, const mc_opts* opts,
+                    mc_mesh* out) {
+    if (!out) return fail(ctx, MC_ERR_ARG, "null output");
+    std::memset(out, 0, sizeof(*out));
+    int64_t V = 0, T = 0;
+    mc_status s = mc_search_device(ctx, solid, delta, iters, opts, &V, &T, &out->stats);
+    if (s != MC_OK) return s;
+    out->vertices = (double*)std::malloc(std::max<int64_t>(V, 1) * 24);
+    out->triangles = (int32_t*)std::malloc(std::max<int64_t>(T, 1) * 12);
+    if (!out->vertices || !out->triangles) {
+        mc_mesh_free(out);
+        return fail(ctx, MC_ERR_OOM, "host allocation failed");
+    }
+    s = mc_result_copy(ctx, out->vertices, out->triangles);
+    if (s != MC_OK) {
+        mc_mesh_free(out);
+        return s;
+    }
+    out->n_vertices = V;
+    out->n_triangles = T;
+    return MC_OK;
+}
+
+void mc_mesh_free(mc_mesh* m) {
+    if (!m) return;
+    std::free(m->vertices);
+    std::free(m->triangles);
+    m->vertices = nullptr;
+    m->triangles = nullptr;
+    m->n_vertices = m->n_triangles = 0;
+}
+
+mc_status mc_contains(mc_ctx* ctx, const mc_solid* solid, const double* points, int64_t n, const mc_opts* opts_in,
+                      uint8_t* out) {
+    if (!ctx || !solid || (n > 0 && (!points || !out))) return fail(ctx, MC_ERR_ARG, "bad argument");
+    if (n == 0) return MC_OK;
+    mc_opts opts = default_opts(opts_in);
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->pts.ensure(n * 24));
+    CK(ctx->pout.ensure(n));
+    CK(ctx->errs.ensure(ER_N * 4));
+    CK(ctx->stats.ensure(ST_N * 8));
+    CK(cudaMemsetAsync(ctx->errs.p, 0, ER_N * 4, ctx->stream));
+    CK(cudaMemsetAsync(ctx->stats.p, 0, ST_N * 8, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->pts.p, points, n * 24, cudaMemcpyHostToDevice, ctx->stream));
+    int grid = (int)std::min<long long>((n + 255) / 256, (long long)ctx->sm_count * 16);
+    k_contains<<<grid, 256, 0, ctx->stream>>>(solid->view, ctx->pts.as<double>(), n, opts.precision,
+                                              ctx->pout.as<uint8_t>(), ctx->errs.as<int>(),
+                                              ctx->stats.as<unsigned long long>());
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, ctx->pout.p, n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_pin + 2, ctx->errs.p, ER_N * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (((const int*)(ctx->h_pin + 2))[ER_LIMIT]) return fail(ctx, MC_ERR_LIMIT, "collider traversal stack exceeded");
+    return MC_OK;
+}
+
+mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_opts* opts, mc_mesh* outs,
+                          mc_status* job_status) {
+    if (!ctx || (n && (!jobs || !outs))) return fail(ctx, MC_ERR_ARG, "bad argument");
+    mc_status first = MC_OK;
+    for (size_t i = 0; i < n; i++) {
+        mc_status s = mc_search(ctx, jobs[i].solid, jobs[i].delta, jobs[i].iters, opts, &outs[i]);
+        if (job_status) job_status[i] = s;
+        if (s != MC_OK && first == MC_OK) first = s;
+    }
+    return first;
+}
+
+}  // extern "C"

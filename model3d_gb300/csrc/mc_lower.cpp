@@ -1,0 +1,690 @@
+// mc_lower.cpp — host side of the library: lowers the mc_node serialisation
+// of a Solid tree into the device program of mc_internal.h, builds the
+// marching-cubes case table and the spacer.
+//
+// Compiled with -ffp-contract=off: every float64 constant precomputed here
+// (cylinder direction, capsule segment order, torus basis, inverse
+// transforms, per-triangle Moller-Trumbore terms) must equal what the
+// reference computes on each call, operation for operation.
+
+#include "mc_lower.h"
+
+#include <algorithm>
+#include <array>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <map>
+#include <stdexcept>
+
+namespace mcgpu {
+namespace {
+
+// ---- Go float64 helpers (math.Min / math.Max, model3d/coords.go:440-448).
+double gmin(double x, double y) {
+    if (std::isinf(x) && x < 0) return x;
+    if (std::isinf(y) && y < 0) return y;
+    if (std::isnan(x) || std::isnan(y)) return std::numeric_limits<double>::quiet_NaN();
+    if (x == 0 && x == y) return std::signbit(x) ? x : y;
+    return x < y ? x : y;
+}
+double gmax(double x, double y) {
+    if (std::isinf(x) && x > 0) return x;
+    if (std::isinf(y) && y > 0) return y;
+    if (std::isnan(x) || std::isnan(y)) return std::numeric_limits<double>::quiet_NaN();
+    if (x == 0 && x == y) return std::signbit(x) ? y : x;
+    return x > y ? x : y;
+}
+
+struct D3 {
+    double v[3];
+};
+D3 d3(double a, double b, double c) { return D3{{a, b, c}}; }
+D3 vadd(D3 a, D3 b) { return d3(a.v[0] + b.v[0], a.v[1] + b.v[1], a.v[2] + b.v[2]); }
+D3 vscale(D3 a, double s) { return d3(a.v[0] * s, a.v[1] * s, a.v[2] * s); }
+D3 vsub(D3 a, D3 b) { return vadd(a, vscale(b, -1)); }
+D3 vmin3(D3 a, D3 b) { return d3(gmin(a.v[0], b.v[0]), gmin(a.v[1], b.v[1]), gmin(a.v[2], b.v[2])); }
+D3 vmax3(D3 a, D3 b) { return d3(gmax(a.v[0], b.v[0]), gmax(a.v[1], b.v[1]), gmax(a.v[2], b.v[2])); }
+double vdot(D3 a, D3 b) { return a.v[0] * b.v[0] + a.v[1] * b.v[1] + a.v[2] * b.v[2]; }
+D3 vcross(D3 a, D3 b) {
+    return d3(a.v[1] * b.v[2] - a.v[2] * b.v[1], a.v[2] * b.v[0] - a.v[0] * b.v[2],
+              a.v[0] * b.v[1] - a.v[1] * b.v[0]);
+}
+double vnorm(D3 a) { return std::sqrt(a.v[0] * a.v[0] + a.v[1] * a.v[1] + a.v[2] * a.v[2]); }
+D3 vnormalize(D3 a) { return vscale(a, 1 / vnorm(a)); }
+bool veq(D3 a, D3 b) { return a.v[0] == b.v[0] && a.v[1] == b.v[1] && a.v[2] == b.v[2]; }
+
+// Largest double S with sqrt_rn(S) <= R: the predicate sqrt(S) <= R of
+// Coord3D.Dist comparisons (model3d/coords.go:272-277) is then S <= TR,
+// because sqrt_rn is monotone.  R < 0 or NaN: nothing qualifies (-1).
+double sqrt_threshold(double R) {
+    if (!(R >= 0)) return -1.0;
+    if (std::isinf(R)) return std::numeric_limits<double>::infinity();
+    double s = R * R;
+    if (std::isinf(s)) s = DBL_MAX;
+    while (s > 0 && std::sqrt(s) > R) s = std::nextafter(s, -1.0);
+    for (;;) {
+        double t = std::nextafter(s, std::numeric_limits<double>::infinity());
+        if (std::isinf(t) || std::sqrt(t) > R) break;
+        s = t;
+    }
+    return s;
+}
+
+float f_down(double x) {  // largest float <= x
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+    return f;
+}
+float f_up(double x) {  // smallest float >= x
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+    return f;
+}
+
+// OrthoBasis (model3d/coords.go:388-422).
+void ortho_basis(D3 c, D3* o1, D3* o2) {
+    double ax = std::fabs(c.v[0]), ay = std::fabs(c.v[1]), az = std::fabs(c.v[2]);
+    D3 b1 = d3(0, 0, 0);
+    if (ax > ay && ax > az) {
+        b1.v[0] = c.v[1] / ax;
+        b1.v[1] = -c.v[0] / ax;
+    } else {
+        b1.v[1] = c.v[2];
+        b1.v[2] = -c.v[1];
+        if (ay > az) {
+            b1.v[1] /= ay;
+            b1.v[2] /= ay;
+        } else {
+            b1.v[1] /= az;
+            b1.v[2] /= az;
+        }
+    }
+    D3 b2 = d3(b1.v[1] * c.v[2] - b1.v[2] * c.v[1], b1.v[2] * c.v[0] - b1.v[0] * c.v[2],
+               b1.v[0] * c.v[1] - b1.v[1] * c.v[0]);
+    *o1 = vnormalize(b1);
+    *o2 = vnormalize(b2);
+}
+
+// Matrix3 inverse (model3d/matrix.go:56-92).
+void inverse3(const double* m, double* r) {
+    double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                 m[2] * (m[3] * m[7] - m[4] * m[6]);
+    double t[9] = {m[4] * m[8] - m[5] * m[7], m[2] * m[7] - m[1] * m[8], m[1] * m[5] - m[2] * m[4],
+                   m[5] * m[6] - m[3] * m[8], m[0] * m[8] - m[2] * m[6], m[2] * m[3] - m[0] * m[5],
+                   m[3] * m[7] - m[4] * m[6], m[1] * m[6] - m[0] * m[7], m[0] * m[4] - m[1] * m[3]};
+    double s = 1 / det;
+    for (int i = 0; i < 9; i++) r[i] = t[i] * s;
+}
+
+// Widen a culling box: any rounding in a leaf predicate moves its accepted
+// set by a few ulps of the coordinates involved; 1e-7 relative is far more.
+void widen(double lo[3], double hi[3]) {
+    double mag = 0;
+    for (int i = 0; i < 3; i++) {
+        mag = std::max(mag, std::fabs(lo[i]));
+        mag = std::max(mag, std::fabs(hi[i]));
+    }
+    double m = 1e-9 + 1e-7 * mag;
+    for (int i = 0; i < 3; i++) {
+        lo[i] -= m;
+        hi[i] += m;
+    }
+}
+
+const D3 kRay = {{0.5224892708603626, 0.10494477243214506, 0.43558938446126527}};  // collisions.go:124
+
+// ---------------------------------------------------------------- colliders
+
+struct Tri {
+    D3 p[3];
+    D3 mn, mx;
+};
+
+struct Flagged {
+    int idx;
+    D3 mn, mx, md;
+    bool flag;
+};
+
+double bounds_area(D3 mn, D3 mx) {  // bvh.go:289-292
+    D3 d = vsub(mx, mn);
+    return 2 * (d.v[0] * (d.v[1] + d.v[2]) + d.v[1] * d.v[2]);
+}
+
+double multi_area(Flagged* const* b, size_t n) {  // bvh.go:257-287
+    D3 mn = b[0]->mn, mx = b[0]->mx;
+    for (size_t i = 1; i < n; i++)
+        for (int a = 0; a < 3; a++) {
+            if (b[i]->mn.v[a] < mn.v[a]) mn.v[a] = b[i]->mn.v[a];
+            if (b[i]->mx.v[a] > mx.v[a]) mx.v[a] = b[i]->mx.v[a];
+        }
+    return bounds_area(mn, mx);
+}
+
+// groupBounders (model3d/bvh.go:135-217); ties in the sorts keep input order.
+void group_rec(std::vector<Flagged*>* s, int* out) {
+    size_t n = s[0].size();
+    if (n <= 2) {
+        for (size_t i = 0; i < n; i++) out[i] = s[0][i]->idx;
+        return;
+    }
+    size_t mid = n / 2;
+    int axis = 0;
+    double best = multi_area(s[0].data(), mid) + multi_area(s[0].data() + mid, n - mid);
+    for (int a = 1; a < 3; a++) {
+        double v = multi_area(s[a].data(), mid) + multi_area(s[a].data() + mid, n - mid);
+        if (v < best) {
+            best = v;
+            axis = a;
+        }
+    }
+    for (size_t i = 0; i < n; i++) s[axis][i]->flag = i < mid;
+    std::vector<Flagged*> lo[3], hi[3];
+    for (int a = 0; a < 3; a++) {
+        if (a == axis) {
+            lo[a].assign(s[a].begin(), s[a].begin() + mid);
+            hi[a].assign(s[a].begin() + mid, s[a].end());
+        } else {
+            lo[a].reserve(mid);
+            hi[a].reserve(n - mid);
+            for (Flagged* f : s[a]) (f->flag ? lo[a] : hi[a]).push_back(f);
+        }
+        std::vector<Flagged*>().swap(s[a]);
+    }
+    group_rec(lo, out);
+    group_rec(hi, out + mid);
+}
+
+std::vector<int> group_triangles(const std::vector<Tri>& t) {  // GroupTriangles, bvh.go:118-133
+    std::vector<Flagged> f(t.size());
+    for (size_t i = 0; i < t.size(); i++)
+        f[i] = {(int)i, t[i].mn, t[i].mx, vscale(vadd(t[i].mn, t[i].mx), 0.5), false};
+    std::vector<Flagged*> s[3];
+    for (int a = 0; a < 3; a++) {
+        s[a].resize(f.size());
+        for (size_t i = 0; i < f.size(); i++) s[a][i] = &f[i];
+        std::stable_sort(s[a].begin(), s[a].end(),
+                         [a](const Flagged* x, const Flagged* y) { return x->md.v[a] < y->md.v[a]; });
+    }
+    std::vector<int> out(t.size());
+    if (!t.empty()) group_rec(s, out.data());
+    return out;
+}
+
+// Tree under construction: JoinedCollider nodes with flattened child lists
+// (NewJoinedCollider, model3d/collisions.go:217-253).
+struct BNode {
+    D3 mn, mx;
+    std::vector<int> ch;  // >= 0 node, < 0: triangle (-c-1)
+};
+
+struct TreeBuilder {
+    const std::vector<Tri>& tris;
+    std::vector<BNode> nodes;
+    // Returns a child reference: node index, or -(tri+1).
+    int build(const int* order, size_t n) {  // GroupedTrianglesToCollider, collisions.go:169-181
+        if (n == 1) return -(order[0] + 1);
+        size_t mid = n / 2;
+        int c1 = build(order, mid);
+        int c2 = build(order + mid, n - mid);
+        BNode j;
+        j.mn = bounds_min(c1);
+        j.mx = bounds_max(c1);
+        j.mn = vmin3(j.mn, bounds_min(c2));
+        j.mx = vmax3(j.mx, bounds_max(c2));
+        for (int c : {c1, c2}) {
+            if (c >= 0 && veq(nodes[c].mn, j.mn) && veq(nodes[c].mx, j.mx)) {
+                std::vector<int> cc = nodes[c].ch;
+                j.ch.insert(j.ch.end(), cc.begin(), cc.end());
+            } else {
+                j.ch.push_back(c);
+            }
+        }
+        nodes.push_back(std::move(j));
+        return (int)nodes.size() - 1;
+    }
+    D3 bounds_min(int c) { return c >= 0 ? nodes[c].mn : tris[-c - 1].mn; }
+    D3 bounds_max(int c) { return c >= 0 ? nodes[c].mx : tris[-c - 1].mx; }
+};
+
+// ---------------------------------------------------------------- lowering
+
+struct Lowerer {
+    const mc_node* nodes;
+    size_t n;
+    const mc_tri_set* sets;
+    size_t n_sets;
+    HostProgram* P;
+    size_t pos = 0;
+    int depth = 0, xdepth = 0;
+    std::map<int, int> tree_of_set;
+
+    void fail(const std::string& m) { throw LowerError(MC_ERR_BAD_PROGRAM, m); }
+
+    void emit(uint32_t op) {
+        if ((int)P->ops.size() >= MAX_OPS) throw LowerError(MC_ERR_LIMIT, "program too long");
+        P->ops.push_back(op);
+    }
+    void push_bool() {
+        depth++;
+        P->max_stack = std::max(P->max_stack, depth);
+        if (depth > MAX_STACK) throw LowerError(MC_ERR_LIMIT, "solid tree too deep");
+    }
+
+    int add_leaf(int kind, const double* d, int nd, const float* f, int nf, const double cull[6]) {
+        int id = (int)P->leaf_kind.size();
+        P->leaf_kind.push_back(kind);
+        size_t bd = P->leaf_d.size(), bf = P->leaf_f.size();
+        P->leaf_d.resize(bd + LEAF_D, 0.0);
+        P->leaf_f.resize(bf + LEAF_F, 0.0f);
+        for (int i = 0; i < nd; i++) P->leaf_d[bd + i] = d[i];
+        for (int i = 0; i < nf; i++) P->leaf_f[bf + i] = f[i];
+        for (int i = 0; i < 6; i++) P->cull.push_back(cull[i]);
+        return id;
+    }
+
+    int lower_collider(int set) {
+        auto it = tree_of_set.find(set);
+        if (it != tree_of_set.end()) return it->second;
+        const mc_tri_set& ts = sets[set];
+        if (ts.n < 0 || (ts.n > 0 && !ts.tris)) fail("bad triangle set");
+        std::vector<Tri> t(ts.n);
+        for (int64_t i = 0; i < ts.n; i++) {
+            for (int k = 0; k < 3; k++)
+                t[i].p[k] = d3(ts.tris[i * 9 + 3 * k], ts.tris[i * 9 + 3 * k + 1], ts.tris[i * 9 + 3 * k + 2]);
+            t[i].mn = vmin3(vmin3(t[i].p[0], t[i].p[1]), t[i].p[2]);  // Triangle.Min, primitives.go:36-38
+            t[i].mx = vmax3(vmax3(t[i].p[0], t[i].p[1]), t[i].p[2]);
+        }
+        std::vector<int> order;
+        if (ts.grouped) {
+            order.resize(ts.n);
+            for (int64_t i = 0; i < ts.n; i++) order[i] = (int)i;
+        } else {
+            order = group_triangles(t);
+        }
+        TreeD tree{0, 0};
+        int tri_base = (int)P->tris.size();
+        // Triangle records in grouped order (traversal locality).
+        std::vector<int> pos_of(ts.n);
+        for (size_t i = 0; i < order.size(); i++) pos_of[order[i]] = (int)i;
+        D3 dn = vnormalize(kRay);
+        for (size_t i = 0; i < order.size(); i++) {
+            const Tri& tr = t[order[i]];
+            TriD d{};
+            TriF f{};
+            D3 v1 = vsub(tr.p[1], tr.p[0]);
+            D3 v2 = vsub(tr.p[2], tr.p[0]);
+            D3 nrm = vnormalize(vcross(v1, v2));      // Triangle.Normal, primitives.go:27-33
+            double dd = vdot(nrm, dn);                 // primitives.go:208
+            bool parallel = dd < 1e-8 && dd > -1e-8;
+            D3 c1 = vcross(kRay, v2);                  // primitives.go:219
+            double det = vdot(c1, v1);                 // primitives.go:220
+            double inv = 1 / det;                      // primitives.go:227
+            for (int k = 0; k < 3; k++) {
+                d.t0[k] = tr.p[0].v[k];
+                d.v1[k] = v1.v[k];
+                d.v2[k] = v2.v[k];
+                d.c1[k] = c1.v[k];
+                f.t0[k] = (float)d.t0[k];
+                f.v1[k] = (float)d.v1[k];
+                f.v2[k] = (float)d.v2[k];
+                f.c1[k] = (float)d.c1[k];
+            }
+            d.inv_det = inv;
+            d.valid = (!parallel && det != 0) ? 1 : 0;
+            f.inv_det = (float)inv;
+            f.valid = d.valid;
+            P->tris.push_back(d);
+            P->tris_f.push_back(f);
+        }
+        if (ts.n == 1) {
+            tree = {2, tri_base};
+        } else if (ts.n > 1) {
+            TreeBuilder tb{t, {}};
+            int root = tb.build(order.data(), order.size());
+            int node_base = (int)P->nodes.size();
+            // Breadth-first relabelling keeps siblings adjacent.
+            std::vector<int> label(tb.nodes.size(), -1), queue = {root};
+            label[root] = 0;
+            for (size_t qi = 0; qi < queue.size(); qi++)
+                for (int c : tb.nodes[queue[qi]].ch)
+                    if (c >= 0) {
+                        label[c] = (int)queue.size();
+                        queue.push_back(c);
+                    }
+            P->nodes.resize(node_base + queue.size());
+            P->nodes_f.resize(node_base + queue.size());
+            for (size_t qi = 0; qi < queue.size(); qi++) {
+                const BNode& b = tb.nodes[queue[qi]];
+                BvhNodeD nd{};
+                BvhNodeF nf{};
+                nd.first = (int)P->child.size();
+                nd.count = (int)b.ch.size();
+                for (int k = 0; k < 3; k++) {
+                    nd.lo[k] = b.mn.v[k];
+                    nd.hi[k] = b.mx.v[k];
+                    nf.lo[k] = f_down(b.mn.v[k]);
+                    nf.hi[k] = f_up(b.mx.v[k]);
+                }
+                nf.first = nd.first;
+                nf.count = nd.count;
+                for (int c : b.ch)
+                    P->child.push_back(c >= 0 ? node_base + label[c] : -(tri_base + pos_of[-c - 1] + 1));
+                P->nodes[node_base + qi] = nd;
+                P->nodes_f[node_base + qi] = nf;
+            }
+            tree = {1, node_base};
+        }
+        int id = (int)P->trees.size();
+        P->trees.push_back(tree);
+        tree_of_set[set] = id;
+        return id;
+    }
+
+    // Lower one node (and its subtree); outer = index of the outermost
+    // enclosing TRANSFORM box (-1 if none) for culling.
+    void lower(int outer) {
+        if (pos >= n) fail("truncated node array");
+        const mc_node& nd = nodes[pos++];
+        auto pv = [&](int o) { return d3(nd.p[o], nd.p[o + 1], nd.p[o + 2]); };
+        double cull[6];
+        auto set_cull = [&](D3 lo, D3 hi) {
+            if (outer >= 0) {
+                for (int i = 0; i < 3; i++) {
+                    cull[i] = P->xbox[outer].lo[i];
+                    cull[3 + i] = P->xbox[outer].hi[i];
+                }
+            } else {
+                for (int i = 0; i < 3; i++) {
+                    cull[i] = lo.v[i];
+                    cull[3 + i] = hi.v[i];
+                }
+            }
+            widen(cull, cull + 3);
+        };
+        switch (nd.kind) {
+            case MC_NODE_SPHERE: {  // shapes.go:29-31
+                D3 c = pv(0);
+                double R = nd.p[3];
+                double d[4] = {c.v[0], c.v[1], c.v[2], sqrt_threshold(R)};
+                float f[6] = {(float)c.v[0], (float)c.v[1], (float)c.v[2], 0, f_down(d[3]), f_up(d[3])};
+                set_cull(vsub(c, d3(R, R, R)), vadd(c, d3(R, R, R)));
+                if (!(R >= 0)) for (double& x : cull) x = 0;  // contains nothing: any box
+                int id = add_leaf(LK_SPHERE, d, 4, f, 6, cull);
+                emit(make_op(OP_LEAF, id));
+                push_bool();
+                return;
+            }
+            case MC_NODE_RECT: {  // shapes.go:171-173
+                D3 lo = pv(0), hi = pv(3);
+                double d[6] = {lo.v[0], lo.v[1], lo.v[2], hi.v[0], hi.v[1], hi.v[2]};
+                float f[6];
+                for (int i = 0; i < 6; i++) f[i] = (float)d[i];
+                set_cull(lo, hi);
+                int id = add_leaf(LK_RECT, d, 6, f, 6, cull);
+                emit(make_op(OP_LEAF, id));
+                push_bool();
+                return;
+            }
+            case MC_NODE_CYLINDER: {  // shapes.go:588-598
+                D3 p1 = pv(0), p2 = pv(3);
+                double R = nd.p[6];
+                D3 diff = vsub(p1, p2);
+                D3 dir = vnormalize(diff);
+                double nrm = vnorm(diff);
+                double TR = sqrt_threshold(R);
+                double d[8] = {p2.v[0], p2.v[1], p2.v[2], dir.v[0], dir.v[1], dir.v[2], nrm, TR};
+                float f[12] = {(float)p2.v[0], (float)p2.v[1], (float)p2.v[2], (float)dir.v[0],
+                               (float)dir.v[1], (float)dir.v[2], f_down(nrm), f_up(nrm),
+                               f_down(TR), f_up(TR), 0, 0};
+                set_cull(vsub(vmin3(p1, p2), d3(R, R, R)), vadd(vmax3(p1, p2), d3(R, R, R)));
+                int id = add_leaf(LK_CYLINDER, d, 8, f, 12, cull);
+                emit(make_op(OP_LEAF, id));
+                push_bool();
+                return;
+            }
+            case MC_NODE_CAPSULE: {  // shapes.go:365-368, primitives.go:547-594
+                D3 p1 = pv(0), p2 = pv(3);
+                double R = nd.p[6];
+                bool keep = p1.v[0] < p2.v[0] || (p1.v[0] == p2.v[0] && p1.v[1] < p2.v[1]) ||
+                            (p1.v[0] == p2.v[0] && p1.v[1] == p2.v[1] && p1.v[2] < p2.v[2]);
+                D3 s0 = keep ? p1 : p2, s1 = keep ? p2 : p1;
+                D3 v1 = vsub(s1, s0);
+                double nrm = vnorm(v1);
+                D3 v = vscale(v1, 1 / nrm);
+                double TR = sqrt_threshold(R);
+                double d[11] = {s0.v[0], s0.v[1], s0.v[2], s1.v[0], s1.v[1], s1.v[2],
+                                v.v[0],  v.v[1],  v.v[2],  nrm,     TR};
+                float f[15];
+                for (int i = 0; i < 9; i++) f[i] = (float)d[i];
+                f[9] = f_down(nrm);
+                f[10] = f_up(nrm);
+                f[11] = f_down(TR);
+                f[12] = f_up(TR);
+                f[13] = f[14] = 0;
+                set_cull(vsub(vmin3(p1, p2), d3(R, R, R)), vadd(vmax3(p1, p2), d3(R, R, R)));
+                int id = add_leaf(LK_CAPSULE, d, 11, f, 15, cull);
+                emit(make_op(OP_LEAF, id));
+                push_bool();
+                return;
+            }
+            case MC_NODE_TORUS: {  // shapes.go:1363-1365, :1451-1487
+                D3 c = pv(0), axis = pv(3);
+                double outer_r = nd.p[6], inner = nd.p[7];
+                D3 b1, b2;
+                ortho_basis(axis, &b1, &b2);
+                double Ti = std::isinf(inner) && inner > 0 ? DBL_MAX : sqrt_threshold(inner);
+                double d[11] = {c.v[0],  c.v[1],  c.v[2],  b1.v[0], b1.v[1], b1.v[2],
+                                b2.v[0], b2.v[1], b2.v[2], outer_r, Ti};
+                float f[11];
+                for (int i = 0; i < 11; i++) f[i] = (float)d[i];
+                double ext = std::fabs(outer_r) + std::fabs(inner);
+                set_cull(vsub(c, d3(ext, ext, ext)), vadd(c, d3(ext, ext, ext)));
+                int id = add_leaf(LK_TORUS, d, 11, f, 11, cull);
+                emit(make_op(OP_LEAF, id));
+                push_bool();
+                return;
+            }
+            case MC_NODE_COLLIDER: {  // solid.go:292-305
+                if (nd.mesh < 0 || (size_t)nd.mesh >= n_sets) fail("bad mesh index");
+                int tree = lower_collider(nd.mesh);
+                double d[7] = {nd.min[0], nd.min[1], nd.min[2], nd.max[0], nd.max[1], nd.max[2], (double)tree};
+                float f[1] = {0};
+                set_cull(d3(nd.min[0], nd.min[1], nd.min[2]), d3(nd.max[0], nd.max[1], nd.max[2]));
+                int id = add_leaf(LK_COLLIDER, d, 7, f, 1, cull);
+                P->has_collider = true;
+                emit(make_op(OP_LEAF, id));
+                push_bool();
+                return;
+            }
+            case MC_NODE_JOIN:
+            case MC_NODE_INTERSECT: {  // solid.go:89-98, :165-172
+                if (nd.n_children < 1) fail("JoinedSolid/IntersectedSolid without children");
+                uint32_t op = nd.kind == MC_NODE_JOIN ? OP_OR : OP_AND;
+                lower(outer);
+                for (int i = 1; i < nd.n_children; i++) {
+                    lower(outer);
+                    emit(make_op(op, 0));
+                    depth--;
+                }
+                return;
+            }
+            case MC_NODE_SUBTRACT: {  // solid.go:138-141
+                if (nd.n_children != 2) fail("SubtractedSolid needs two children");
+                lower(outer);
+                lower(outer);
+                emit(make_op(OP_ANDNOT, 0));
+                depth--;
+                return;
+            }
+            case MC_NODE_TRANSFORM: {  // transform.go:240-247
+                if (nd.n_children != 1) fail("TransformSolid needs one child");
+                XBoxD xb{};
+                for (int i = 0; i < 3; i++) {
+                    xb.lo[i] = nd.min[i];
+                    xb.hi[i] = nd.max[i];
+                }
+                std::vector<XStepD> fwd;
+                for (int i = 0; i < nd.n_steps; i++) {
+                    if (pos >= n) fail("truncated transform steps");
+                    const mc_node& st = nodes[pos++];
+                    XStepD s{};
+                    s.kind = st.kind;
+                    switch (st.kind) {
+                        case MC_XF_TRANSLATE:  // Inverse: Offset.Scale(-1), transform.go:52-54
+                            for (int k = 0; k < 3; k++) s.v[k] = st.p[k] * -1;
+                            break;
+                        case MC_XF_SCALE: s.v[0] = 1 / st.p[0]; break;  // transform.go:83-85
+                        case MC_XF_VECSCALE:                            // Recip, transform.go:114-116
+                            for (int k = 0; k < 3; k++) s.v[k] = 1 / st.p[k];
+                            break;
+                        case MC_XF_MATRIX: inverse3(st.p, s.v); break;  // transform.go:153-155
+                        default: fail("bad transform step");
+                    }
+                    fwd.push_back(s);
+                }
+                // JoinedTransform.Inverse applies the inverses in reverse order (transform.go:213-219).
+                xb.first_step = (int)P->xstep.size();
+                xb.n_steps = (int)fwd.size();
+                for (int i = (int)fwd.size() - 1; i >= 0; i--) P->xstep.push_back(fwd[i]);
+                int id = (int)P->xbox.size();
+                P->xbox.push_back(xb);
+                emit(make_op(OP_XPUSH, id));
+                if (++xdepth > MAX_XDEPTH) throw LowerError(MC_ERR_LIMIT, "transforms nested too deeply");
+                P->max_xdepth = std::max(P->max_xdepth, xdepth);
+                lower(outer >= 0 ? outer : id);
+                xdepth--;
+                emit(make_op(OP_XPOP, id));
+                return;
+            }
+            case MC_NODE_CHECKED: {  // solid.go:46-50
+                if (nd.n_children != 1) fail("CheckedFuncSolid needs one child");
+                XBoxD xb{};
+                for (int i = 0; i < 3; i++) {
+                    xb.lo[i] = nd.min[i];
+                    xb.hi[i] = nd.max[i];
+                }
+                xb.first_step = 0;
+                xb.n_steps = 0;
+                int id = (int)P->xbox.size();
+                P->xbox.push_back(xb);
+                lower(outer);
+                emit(make_op(OP_BOXAND, id));
+                return;
+            }
+            default: throw LowerError(MC_ERR_NOT_LOWERABLE, "node kind has no device lowering");
+        }
+    }
+};
+
+}  // namespace
+
+void lower_scene(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets, size_t n_sets,
+                 HostProgram* P) {
+    *P = HostProgram();
+    if (!nodes || n_nodes == 0) throw LowerError(MC_ERR_ARG, "empty node array");
+    Lowerer L{nodes, n_nodes, sets, n_sets, P};
+    L.lower(-1);
+    if (L.pos != n_nodes) throw LowerError(MC_ERR_BAD_PROGRAM, "trailing nodes after the root");
+    for (int i = 0; i < 3; i++) {
+        P->root_min[i] = nodes[0].min[i];
+        P->root_max[i] = nodes[0].max[i];
+    }
+    P->ops_allfalse.resize(P->ops.size() + 1);
+    P->n_ops_allfalse = fold_program(P->ops.data(), (int)P->ops.size(), [](uint32_t) { return false; },
+                                     P->ops_allfalse.data());
+}
+
+// ---------------------------------------------------------------- spacer
+
+int spacer_axis(double lo, double hi, double delta, std::vector<double>* out, int64_t limit) {
+    out->clear();
+    if (!(delta > 0) || std::isinf(delta)) return MC_ERR_GRID;
+    // for x := min - delta; x <= max + delta; x += delta (model3d/mc.go:598-600)
+    for (double x = lo - delta; x <= hi + delta; x += delta) {
+        if ((int64_t)out->size() >= limit) return MC_ERR_GRID;
+        if (!out->empty() && !(x > out->back())) return MC_ERR_GRID;  // x += delta stalled
+        out->push_back(x);
+    }
+    return MC_OK;
+}
+
+// ---------------------------------------------------------------- case table
+
+namespace {
+// Base cases of model3d/mc.go:462-586 (inside corners; triangles as corner pairs).
+struct Base {
+    uint8_t inside;
+    int ntri;
+    uint8_t t[5][6];
+};
+const Base kBase[23] = {
+    {0x00, 0, {}},
+    {0x01, 1, {{0, 1, 0, 2, 0, 4}}},
+    {0x03, 2, {{0, 4, 1, 5, 0, 2}, {1, 5, 1, 3, 0, 2}}},
+    {0x21, 2, {{0, 1, 0, 2, 0, 4}, {5, 7, 1, 5, 4, 5}}},
+    {0x81, 2, {{0, 1, 0, 2, 0, 4}, {6, 7, 3, 7, 5, 7}}},
+    {0x0e, 3, {{0, 1, 1, 5, 0, 2}, {0, 2, 1, 5, 2, 6}, {2, 6, 1, 5, 3, 7}}},
+    {0x83, 3, {{0, 4, 1, 5, 0, 2}, {1, 5, 1, 3, 0, 2}, {6, 7, 3, 7, 5, 7}}},
+    {0x92, 3, {{4, 6, 4, 5, 0, 4}, {1, 5, 1, 3, 0, 1}, {6, 7, 3, 7, 5, 7}}},
+    {0x0f, 2, {{0, 4, 1, 5, 3, 7}, {0, 4, 3, 7, 2, 6}}},
+    {0x4d, 4, {{0, 1, 4, 6, 0, 4}, {0, 1, 6, 7, 4, 6}, {0, 1, 1, 3, 6, 7}, {1, 3, 3, 7, 6, 7}}},
+    {0x66, 4, {{0, 2, 2, 3, 6, 7}, {0, 2, 6, 7, 4, 6}, {0, 1, 4, 5, 5, 7}, {5, 7, 1, 3, 0, 1}}},
+    {0x8d, 4, {{0, 4, 0, 1, 2, 6}, {0, 1, 5, 7, 2, 6}, {2, 6, 5, 7, 6, 7}, {0, 1, 1, 3, 5, 7}}},
+    {0x1e, 4, {{0, 1, 1, 5, 0, 2}, {0, 2, 1, 5, 2, 6}, {2, 6, 1, 5, 3, 7}, {4, 5, 0, 4, 4, 6}}},
+    {0x96, 4, {{0, 1, 1, 5, 1, 3}, {0, 2, 2, 3, 2, 6}, {4, 5, 0, 4, 4, 6}, {5, 7, 6, 7, 3, 7}}},
+    {0x4e, 4, {{0, 2, 0, 1, 4, 6}, {0, 1, 3, 7, 4, 6}, {0, 1, 1, 5, 3, 7}, {4, 6, 3, 7, 6, 7}}},
+    {0x6d, 5, {{0, 1, 4, 6, 0, 4}, {0, 1, 6, 7, 4, 6}, {0, 1, 1, 3, 6, 7}, {1, 3, 3, 7, 6, 7}, {5, 7, 1, 5, 4, 5}}},
+    {0x7c, 5, {{5, 7, 1, 5, 0, 4}, {0, 4, 6, 7, 5, 7}, {0, 2, 6, 7, 0, 4}, {0, 2, 3, 7, 6, 7}, {0, 2, 1, 3, 3, 7}}},
+    {0xf1, 3, {{1, 5, 0, 1, 0, 2}, {0, 2, 2, 6, 1, 5}, {1, 5, 2, 6, 3, 7}}},
+    {0x7e, 2, {{0, 2, 0, 1, 0, 4}, {3, 7, 6, 7, 5, 7}}},
+    {0xde, 4, {{0, 2, 4, 5, 0, 4}, {0, 2, 5, 7, 4, 5}, {0, 2, 1, 5, 5, 7}, {0, 1, 1, 5, 0, 2}}},
+    {0xfc, 2, {{1, 5, 0, 4, 0, 2}, {1, 3, 1, 5, 0, 2}}},
+    {0xfe, 1, {{0, 2, 0, 1, 0, 4}}},
+    {0xff, 0, {}},
+};
+}  // namespace
+
+int build_case_table(uint8_t counts[256], uint8_t tris[256][5][6]) {
+    // The 24 rotations (allMcRotations, mc.go:312-353): closure of the
+    // identity under the two generators, sorted lexicographically.
+    const uint8_t gz[8] = {2, 0, 3, 1, 6, 4, 7, 5};
+    const uint8_t gx[8] = {2, 3, 6, 7, 0, 1, 4, 5};
+    std::vector<std::array<uint8_t, 8>> rots = {{0, 1, 2, 3, 4, 5, 6, 7}};
+    for (size_t i = 0; i < rots.size(); i++)
+        for (const uint8_t* g : {gz, gx}) {
+            std::array<uint8_t, 8> r;
+            for (int k = 0; k < 8; k++) r[k] = g[rots[i][k]];
+            if (std::find(rots.begin(), rots.end(), r) == rots.end()) rots.push_back(r);
+        }
+    std::sort(rots.begin(), rots.end());
+    std::memset(counts, 0, 256);
+    std::memset(tris, 0, 256 * 5 * 6);
+    bool seen[256] = {false};
+    int owner[256];
+    int conflicts = 0;
+    for (int b = 0; b < 23; b++) {
+        for (const auto& r : rots) {
+            int ni = 0;
+            for (int c = 0; c < 8; c++)
+                if (kBase[b].inside & (1 << c)) ni |= 1 << r[c];
+            if (seen[ni]) {
+                conflicts += owner[ni] != b;
+                continue;
+            }
+            seen[ni] = true;
+            owner[ni] = b;
+            counts[ni] = (uint8_t)kBase[b].ntri;
+            for (int t = 0; t < kBase[b].ntri; t++)
+                for (int k = 0; k < 6; k++) tris[ni][t][k] = r[kBase[b].t[t][k]];
+        }
+    }
+    int covered = 0;
+    for (int i = 0; i < 256; i++) covered += seen[i];
+    return (covered == 256 && conflicts == 0 && rots.size() == 24) ? 0 : -1;
+}
+
+}  // namespace mcgpu

@@ -1,0 +1,50 @@
+// mc_lower.h — host-side lowering of the mc_node serialisation into the
+// device program layout of mc_internal.h.
+#pragma once
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mcgpu.h"
+#include "mc_internal.h"
+
+namespace mcgpu {
+
+struct LowerError : std::runtime_error {
+    mc_status status;
+    LowerError(mc_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+// Host copy of a lowered solid; uploaded once by mc_solid_create.
+struct HostProgram {
+    std::vector<uint32_t> ops, ops_allfalse;
+    int n_ops_allfalse = FOLD_FALSE;
+    std::vector<int32_t> leaf_kind;
+    std::vector<double> leaf_d;
+    std::vector<float> leaf_f;
+    std::vector<double> cull;
+    std::vector<XBoxD> xbox;
+    std::vector<XStepD> xstep;
+    std::vector<TreeD> trees;
+    std::vector<BvhNodeD> nodes;
+    std::vector<BvhNodeF> nodes_f;
+    std::vector<int32_t> child;
+    std::vector<TriD> tris;
+    std::vector<TriF> tris_f;
+    double root_min[3] = {0, 0, 0}, root_max[3] = {0, 0, 0};
+    int max_stack = 0, max_xdepth = 0;
+    bool has_collider = false;
+};
+
+// Throws LowerError.
+void lower_scene(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets, size_t n_sets,
+                 HostProgram* out);
+
+// newSquareSpacer for one axis; MC_OK or MC_ERR_GRID.
+int spacer_axis(double lo, double hi, double delta, std::vector<double>* out, int64_t limit);
+
+// mcLookupTable; 0 when all 256 cases are covered without conflicts.
+int build_case_table(uint8_t counts[256], uint8_t tris[256][5][6]);
+
+}  // namespace mcgpu

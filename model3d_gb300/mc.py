@@ -1,0 +1,222 @@
+"""MarchingCubesSearch on the GPU behind model3d's API.
+
+    mesh = MarchingCubesSearch(solid, delta, iters)
+
+mirrors model3d.MarchingCubesSearch (model3d/mc.go:45-49): the same grid
+(newSquareSpacer on the solid's bounds), the same lookup-table triangle
+order and the same bisection search, with the reference's panics raised as
+``MCError`` carrying the same message.  The mesh is returned indexed
+(vertices + triangles); ``Mesh.TriangleSoup()`` gives the reference's
+per-triangle coordinates.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from typing import Optional
+
+import numpy as np
+
+from . import _native as N
+from .solids import Solid, serialize
+
+
+class MCError(RuntimeError):
+    """A failed call.  ``str(err)`` is the reference's panic text where the
+    reference panics (e.g. "solid is true outside of bounds")."""
+
+    def __init__(self, status: int, detail: str = ""):
+        self.status = status
+        msg = N.status_string(status)
+        super().__init__(msg if not detail or detail == msg else f"{msg}: {detail}")
+
+
+def _check(status: int, ctx_ptr=None):
+    if status != N.MC_OK:
+        detail = N.lib().mc_last_error(ctx_ptr).decode() if ctx_ptr else ""
+        raise MCError(status, detail)
+
+
+class Context:
+    """One CUDA stream and its buffers on one device (mc_ctx)."""
+
+    def __init__(self, device: int = 0):
+        L = N.lib()
+        p = ctypes.c_void_p()
+        _check(L.mc_create(ctypes.byref(p), int(device)))
+        self._p = p
+        self.device = device
+
+    @property
+    def ptr(self):
+        return self._p
+
+    def close(self):
+        if getattr(self, "_p", None) and self._p.value:
+            N.lib().mc_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_tls = threading.local()
+
+
+def default_context(device: int = 0) -> Context:
+    ctxs = getattr(_tls, "ctxs", None)
+    if ctxs is None:
+        ctxs = _tls.ctxs = {}
+    if device not in ctxs:
+        ctxs[device] = Context(device)
+    return ctxs[device]
+
+
+class DeviceSolid:
+    """A Solid lowered to the device (mc_solid): CSG bytecode and collider
+    trees resident in HBM.  Reuse it across calls to avoid re-lowering."""
+
+    def __init__(self, solid: Solid, ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        nodes, sets = serialize(solid)
+        self.nodes = nodes
+        self._sets = sets
+        arr = (N.MCTriSet * max(1, len(sets)))()
+        keep = []
+        for i, s in enumerate(sets):
+            t = np.ascontiguousarray(s.tris, dtype=np.float64)
+            keep.append(t)
+            arr[i].tris = t.ctypes.data
+            arr[i].n = len(t)
+            arr[i].grouped = int(s.grouped)
+        p = ctypes.c_void_p()
+        _check(N.lib().mc_solid_create(self.ctx.ptr, nodes.ctypes.data, len(nodes),
+                                       ctypes.addressof(arr), len(sets), ctypes.byref(p)),
+               self.ctx.ptr)
+        self._p = p
+
+    @property
+    def ptr(self):
+        return self._p
+
+    def bounds(self):
+        mn, mx = np.zeros(3), np.zeros(3)
+        _check(N.lib().mc_solid_bounds(self._p, mn.ctypes.data, mx.ctypes.data))
+        return mn, mx
+
+    def close(self):
+        if getattr(self, "_p", None) and self._p.value:
+            N.lib().mc_solid_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Mesh:
+    """Indexed triangle mesh: vertices (V,3) float64, triangles (T,3) int32
+    (vertex order of the reference's lookup table)."""
+
+    def __init__(self, vertices: np.ndarray, triangles: np.ndarray, stats: Optional[dict] = None):
+        self.vertices = vertices
+        self.triangles = triangles
+        self.stats = stats or {}
+
+    def NumTriangles(self) -> int:
+        return len(self.triangles)
+
+    def TriangleSoup(self) -> np.ndarray:
+        """(T, 9) float64: each triangle's three vertices."""
+        if len(self.triangles) == 0:
+            return np.zeros((0, 9))
+        return self.vertices[self.triangles].reshape(-1, 9)
+
+    def Volume(self) -> float:
+        """Mesh.Volume (model3d/measurements.go:18-31) up to summation order."""
+        t = self.TriangleSoup().reshape(-1, 3, 3)
+        return float(abs(np.linalg.det(t).sum() / 6.0)) if len(t) else 0.0
+
+
+def _opts(precision="fp32", cull=True, tile_y=0, tile_z=0):
+    o = N.MCOpts()
+    o.precision = N.MC_PREC_FP64 if precision in ("fp64", N.MC_PREC_FP64) else N.MC_PREC_FP32_FILTERED
+    o.cull = 1 if cull else 0
+    o.tile_y = int(tile_y)
+    o.tile_z = int(tile_z)
+    return o
+
+
+def _as_device_solid(solid, ctx):
+    if isinstance(solid, DeviceSolid):
+        return solid
+    return DeviceSolid(solid, ctx)
+
+
+def MarchingCubesSearch(solid, delta: float, iters: int, *, precision: str = "fp32",
+                        cull: bool = True, ctx: Optional[Context] = None, tile_y: int = 0,
+                        tile_z: int = 0) -> Mesh:
+    """model3d.MarchingCubesSearch (model3d/mc.go:45-49) on the GPU."""
+    ctx = ctx or (solid.ctx if isinstance(solid, DeviceSolid) else default_context())
+    ds = _as_device_solid(solid, ctx)
+    out = N.MCMesh()
+    o = _opts(precision, cull, tile_y, tile_z)
+    _check(N.lib().mc_search(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
+                             ctypes.byref(out)), ctx.ptr)
+    try:
+        V, T = out.n_vertices, out.n_triangles
+        verts = np.ctypeslib.as_array(out.vertices, shape=(max(V, 1) * 3,))[:V * 3].reshape(V, 3).copy()
+        tris = np.ctypeslib.as_array(out.triangles, shape=(max(T, 1) * 3,))[:T * 3].reshape(T, 3).copy()
+        stats = out.stats.as_dict()
+    finally:
+        N.lib().mc_mesh_free(ctypes.byref(out))
+    return Mesh(verts, tris, stats)
+
+
+def MarchingCubes(solid, delta: float, **kw) -> Mesh:
+    """model3d.MarchingCubes (model3d/mc.go:14-37): the search with iters=0."""
+    return MarchingCubesSearch(solid, delta, 0, **kw)
+
+
+def Contains(solid, points, *, precision: str = "fp32", ctx: Optional[Context] = None) -> np.ndarray:
+    """Solid.Contains at each of the (n, 3) points, evaluated on the GPU."""
+    ctx = ctx or (solid.ctx if isinstance(solid, DeviceSolid) else default_context())
+    ds = _as_device_solid(solid, ctx)
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros(len(pts), dtype=np.uint8)
+    o = _opts(precision)
+    _check(N.lib().mc_contains(ctx.ptr, ds.ptr, pts.ctypes.data, len(pts), ctypes.byref(o),
+                               out.ctypes.data), ctx.ptr)
+    return out.astype(bool)
+
+
+def case_table():
+    """The library's 256-case lookup table (counts, tris[256][5][6])."""
+    counts = np.zeros(256, dtype=np.uint8)
+    tris = np.zeros((256, 5, 6), dtype=np.uint8)
+    _check(N.lib().mc_case_table(counts.ctypes.data, tris.ctypes.data))
+    return counts, tris
+
+
+def spacer_axis(lo: float, hi: float, delta: float) -> np.ndarray:
+    n = ctypes.c_int64()
+    N.lib().mc_spacer_axis(lo, hi, delta, None, 0, ctypes.byref(n))
+    out = np.zeros(n.value)
+    _check(N.lib().mc_spacer_axis(lo, hi, delta, out.ctypes.data, n.value, ctypes.byref(n)))
+    return out
+
+
+def canonical(soup: np.ndarray) -> np.ndarray:
+    """Triangles as 9 float64 bit patterns each, rows sorted: two meshes are
+    bit-identical iff their canonical arrays are equal (vertex order inside a
+    triangle is kept, only the triangle list is sorted)."""
+    bits = np.ascontiguousarray(soup, dtype=np.float64).reshape(-1, 9).view(np.uint64)
+    if len(bits) == 0:
+        return bits
+    order = np.lexsort(bits.T[::-1])
+    return bits[order]

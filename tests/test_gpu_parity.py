@@ -1,0 +1,228 @@
+"""Parity of the CUDA path with the oracle, through the C ABI.
+
+Bit-exact: every mesh is compared as the sorted list of its triangles' nine
+float64 bit patterns (triangle vertex order kept), for both precision modes
+(FP64 and FP32-filtered) and with tile culling on and off.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from model3d_gb300 import (CacheSolidBounds, Capsule, Contains, Cylinder, DeviceSolid,
+                           GroupedTrianglesToCollider, IntersectedSolid, JoinedSolid,
+                           JoinedTransform, MarchingCubesSearch, MCError, MeshToCollider,
+                           NewColliderSolid, NotLowerable, Rect, Rotation, Scale, Sphere,
+                           SubtractedSolid, Torus, TransformSolid, Translate, VecScale, XYZ,
+                           canonical, serialize)
+from model3d_gb300 import _native as N
+from model3d_gb300.workloads import (SplitMix64, box_triangles, csg_tree, displaced_icosphere,
+                                     random_primitive)
+
+pytestmark = pytest.mark.gpu
+
+MODES = [("fp64", True), ("fp32", True), ("fp32", False)]
+
+
+def _same(mesh, ref):
+    a = canonical(mesh.TriangleSoup())
+    b = canonical(ref["tris"])
+    assert a.shape == b.shape, f"triangle count {len(a)} != oracle {len(b)}"
+    diff = np.nonzero((a != b).any(1))[0]
+    assert len(diff) == 0, f"{len(diff)} triangles differ, first at {diff[:3]}"
+
+
+def _check(oracle, solid, delta, iters, modes=MODES):
+    nodes, sets = serialize(solid)
+    ref = oracle.mc_search(nodes, sets, delta, iters)
+    ds = DeviceSolid(solid)
+    for prec, cull in modes:
+        m = MarchingCubesSearch(ds, delta, iters, precision=prec, cull=cull)
+        _same(m, ref)
+        assert m.stats["vertices"] == ref["n_vertices"]
+        assert (m.stats["nx"], m.stats["ny"], m.stats["nz"]) == (ref["nx"], ref["ny"], ref["nz"])
+    return m
+
+
+def test_sphere_full_size(oracle):
+    """Plain sphere at delta 0.01 (202^3 corners), iters 8."""
+    m = _check(oracle, Sphere(XYZ(0, 0, 0), 1.0), 0.01, 8)
+    assert m.stats["corners"] == 202 ** 3
+
+
+@pytest.mark.parametrize("iters", [0, 1, 2, 8])
+def test_sphere_iters(oracle, iters):
+    _check(oracle, Sphere(XYZ(0.1, 0.3, -0.2), 0.7), 0.05, iters)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_single_primitives(oracle, seed):
+    rng = SplitMix64(1000 + seed)
+    for _ in range(4):
+        _check(oracle, random_primitive(rng), 0.02, 8)
+
+
+def test_reference_benchmark_cylinder(oracle):
+    """BenchmarkMarchingCubes' cylinder (mc_test.go:98-106) at delta 0.025."""
+    _check(oracle, Cylinder(XYZ(1, 2, 3), XYZ(3, 1, 4), 0.5), 0.025, 8)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_csg_trees(oracle, seed):
+    _check(oracle, csg_tree(seed, 24, 8), 0.015, 8)
+
+
+def test_csg_config_shape_reduced_delta(oracle):
+    """The 48-minus-16 CSG tree of the headline workload at delta 0.01."""
+    _check(oracle, csg_tree(1, 48, 16), 0.01, 8)
+
+
+def test_torus(oracle):
+    _check(oracle, Torus(XYZ(0.1, -0.2, 0.3), XYZ(0.3, 1, -0.2), 0.6, 0.2), 0.02, 8)
+    _check(oracle, Torus(XYZ(0, 0, 0), XYZ(0, 0, 1), 0.5, 0.25), 0.02, 8)
+
+
+def test_transforms_and_combinators(oracle):
+    base = SubtractedSolid(Cylinder(XYZ(0, 0, -0.5), XYZ(0.2, 0.1, 0.5), 0.4),
+                           Sphere(XYZ(0.1, 0, 0.3), 0.25))
+    solids = [
+        TransformSolid(Translate(XYZ(0.3, -0.2, 0.1)), base),
+        TransformSolid(Scale(1.7), base),
+        TransformSolid(VecScale(XYZ(1.3, -0.7, 0.9)), base),
+        TransformSolid(Rotation(XYZ(0, 0.6, 0.8), 0.7), base),
+        TransformSolid(JoinedTransform([Scale(1.2), Rotation(XYZ(1, 0, 0), 0.3),
+                                        Translate(XYZ(0.1, 0.2, 0.3))]), base),
+        IntersectedSolid([Sphere(XYZ(0, 0, 0), 1), Rect(XYZ(-0.5, -2, -2), XYZ(2, 0.4, 2))]),
+        JoinedSolid([random_primitive(SplitMix64(i)) for i in range(10)]).Optimize(),
+        CacheSolidBounds(TransformSolid(Translate(XYZ(1, 0, 0)),
+                                        TransformSolid(Scale(0.5), base))),
+    ]
+    for s in solids:
+        _check(oracle, s, 0.02, 8)
+
+
+def test_collider_icosphere(oracle):
+    s = NewColliderSolid(MeshToCollider(displaced_icosphere(8)))
+    _check(oracle, s, 0.03, 8)
+
+
+def test_collider_boxes(oracle):
+    """The two-box collider of mc_test.go:51-60 / BenchmarkMarchingCubes."""
+    tris = np.concatenate([box_triangles((-1, -1, -1), (0, 0, 0)), box_triangles((0.1, 0, 0), (1, 1, 1))])
+    _check(oracle, NewColliderSolid(MeshToCollider(tris)), 0.1, 8)
+    _check(oracle, NewColliderSolid(GroupedTrianglesToCollider(tris)), 0.05, 8)
+
+
+def test_collider_single_triangle_and_csg_mix(oracle):
+    tris = displaced_icosphere(3)
+    col = NewColliderSolid(MeshToCollider(tris))
+    s = SubtractedSolid(col, Sphere(XYZ(0.5, 0.5, 0.5), 0.5))
+    _check(oracle, s, 0.04, 8)
+
+
+def test_empty_and_degenerate(oracle):
+    # smaller than one grid cell: no corner inside, empty mesh
+    m = _check(oracle, Sphere(XYZ(0.0123, 0.0456, 0.0789), 0.001), 0.1, 8)
+    assert m.NumTriangles() == 0
+    # flat box (zero extent in z) and a zero-length capsule
+    _check(oracle, Rect(XYZ(-0.3, -0.2, 0.1), XYZ(0.4, 0.5, 0.1)), 0.05, 8)
+    _check(oracle, Capsule(XYZ(0.1, 0.1, 0.1), XYZ(0.1, 0.1, 0.1), 0.3), 0.05, 8)
+
+
+def test_border_inside_raises(oracle):
+    nodes, sets = serialize(Sphere(XYZ(0, 0, 0), 1.0))
+    s = Sphere(XYZ(0, 0, 0), 1.0)
+
+    class Lying(Sphere):
+        def Min(self):
+            return XYZ(-0.5, -0.5, -0.5)
+
+        def Max(self):
+            return XYZ(0.5, 0.5, 0.5)
+
+    with pytest.raises(MCError) as e:
+        MarchingCubesSearch(Lying(XYZ(0, 0, 0), 1.0), 0.1, 8)
+    assert e.value.status == N.MC_ERR_BOUNDS_INSIDE
+    assert "solid is true outside of bounds" in str(e.value)
+    with pytest.raises(Exception):
+        oracle.mc_search(*serialize(Lying(XYZ(0, 0, 0), 1.0)), 0.1, 8)
+
+
+def test_invalid_bounds_raise():
+    class Inverted(Sphere):
+        def Max(self):
+            return XYZ(-2, 0, 0)
+
+    with pytest.raises(MCError) as e:
+        MarchingCubesSearch(Inverted(XYZ(0, 0, 0), 1.0), 0.1, 8)
+    assert e.value.status == N.MC_ERR_INVALID_BOUNDS
+
+
+def test_unlowerable_solid_raises():
+    class Custom:
+        def Min(self):
+            return XYZ(0, 0, 0)
+
+        def Max(self):
+            return XYZ(1, 1, 1)
+
+    with pytest.raises(NotLowerable):
+        MarchingCubesSearch(Custom(), 0.1, 8)
+
+
+def _near_surface_points(solid, n, rng):
+    mn, mx = np.array(solid.Min().Array()), np.array(solid.Max().Array())
+    pad = 0.1 * (mx - mn + 1e-3)
+    p = mn - pad + (mx - mn + 2 * pad) * rng.random((n, 3))
+    return p
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_contains_parity(oracle, prec):
+    """Solid.Contains at random points, incl. points on grid values of the
+    reference spacer and points nudged by one ulp off a surface."""
+    rng = np.random.default_rng(7)
+    solids = [random_primitive(SplitMix64(50 + i)) for i in range(16)]
+    solids += [Torus(XYZ(0.1, -0.2, 0.3), XYZ(0.3, 1, -0.2), 0.6, 0.2), csg_tree(3, 12, 4)]
+    for s in solids:
+        nodes, sets = serialize(s)
+        pts = _near_surface_points(s, 20000, rng)
+        ref, _ = oracle.contains(nodes, sets, pts)
+        got = Contains(s, pts, precision=prec)
+        assert (got == ref).all()
+    # points exactly on a sphere surface and one ulp either side
+    s = Sphere(XYZ(0.25, -0.5, 0.125), 0.75)
+    d = rng.normal(size=(5000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    p = np.array(s.Center.Array()) + 0.75 * d
+    pts = np.concatenate([p, np.nextafter(p, np.inf), np.nextafter(p, -np.inf)])
+    ref, _ = oracle.contains(*serialize(s), pts)
+    assert (Contains(s, pts, precision=prec) == ref).all()
+
+
+def test_filter_escalation_rate_is_small():
+    m = MarchingCubesSearch(csg_tree(1, 48, 16), 0.01, 8, precision="fp32")
+    st = m.stats
+    assert st["leaf_evals"] > 0
+    assert st["escalations"] <= 0.01 * st["leaf_evals"]
+
+
+def _closed_oriented(tris):
+    e = tris[:, [0, 1, 1, 2, 2, 0]].reshape(-1, 2).astype(np.int64)
+    V = int(e.max()) + 1 if len(e) else 1
+    k = e[:, 0] * V + e[:, 1]
+    r = e[:, 1] * V + e[:, 0]
+    assert len(np.unique(k)) == len(k)
+    assert np.array_equal(np.sort(k), np.sort(r))
+
+
+def test_headline_csg_full_size_properties():
+    """The headline workload at full size (delta 0.004): the FP32-filtered and
+    FP64 meshes are bit-identical, closed and consistently oriented."""
+    s = csg_tree(1, 48, 16)
+    ds = DeviceSolid(s)
+    a = MarchingCubesSearch(ds, 0.004, 8, precision="fp32")
+    b = MarchingCubesSearch(ds, 0.004, 8, precision="fp64")
+    assert a.stats["corners"] > 1.0e8
+    assert np.array_equal(canonical(a.TriangleSoup()), canonical(b.TriangleSoup()))
+    _closed_oriented(a.triangles)
