@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Benchmark: MarchingCubesSearch of the 48-minus-16 CSG tree (delta 0.004,
+iters 8) on one GB300 — corners/s of the FP32-filtered kernel, next to the
+plain FP64 kernel (bit-identical meshes) and the CPU restatement of the
+reference path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one MarchingCubesSearch of the solid resident on the device
+(corner classification, cube classification + prefix sums, emission, edge
+bisection).  L2 is flushed (a 256 MiB write) before every timed step; step
+time is the library's CUDA-event time on its own stream.  Under torchrun
+each rank runs an independent replica (the path does not shard: replicas
+only) and ``value`` sums all ranks' corners over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "corners/sec & meshes/sec: FP32-filtered vs FP64 GPU, bit-identical mesh"
+WORKLOAD = "csg_tree(seed=1, 48 joined primitives minus 16), delta=0.004, iters=8"
+SEED, N_POS, N_NEG, DELTA, ITERS = 1, 48, 16, 0.004, 8
+CPU_SLABS = 200  # bounded CPU sample: the central 200 z-slabs of the same grid
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_sample(nodes, sets, nz, threads):
+    """The oracle on the central CPU_SLABS z-slabs of the same grid."""
+    from oracle import oracle as O
+    z0 = max(0, nz // 2 - CPU_SLABS // 2)
+    z1 = min(nz, z0 + CPU_SLABS)
+    t = time.perf_counter()
+    m = O.mc_search(nodes, sets, DELTA, ITERS, threads=threads, z_range=(z0, z1))
+    dt = time.perf_counter() - t
+    corners = (z1 - z0) * m["nx"] * m["ny"]
+    return corners / dt, dict(slabs=(z0, z1), corners=corners, seconds=dt,
+                              triangles=len(m["tris"]))
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from model3d_gb300 import serialize
+    from model3d_gb300.workloads import csg_tree
+    solid = csg_tree(SEED, N_POS, N_NEG)
+    nodes, sets = serialize(solid)
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    ny = len(O.spacer_axis(solid.Min().Y, solid.Max().Y, DELTA))
+    nz = len(O.spacer_axis(solid.Min().Z, solid.Max().Z, DELTA))
+    for _ in range(args.warmup):
+        cpu_sample(nodes, sets, nz, threads)
+    vals, secs, info = [], 0.0, None
+    for _ in range(args.steps):
+        v, info = cpu_sample(nodes, sets, nz, threads)
+        vals.append(v)
+        secs += info["seconds"]
+    value = float(np.mean(vals))
+    sample = (f"oracle port (C++ restatement of model3d MarchingCubesSearch; no Go toolchain), "
+              f"{threads} threads, z-slabs {info['slabs'][0]}..{info['slabs'][1]} of the grid "
+              f"({info['corners']} corners incl. cube pass and bisection search)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "corners/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded splitmix64)",
+        "config": {"workload": WORKLOAD, "precision": "fp64 (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "corners/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "corners/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from model3d_gb300 import (Context, DeviceSolid, MarchingCubesSearch, serialize)
+    from model3d_gb300 import _native as N
+    from model3d_gb300.workloads import csg_tree
+    import ctypes
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    ctx = Context(local)
+    solid = csg_tree(SEED, N_POS, N_NEG)
+    ds = DeviceSolid(solid, ctx)
+    L = N.lib()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def step(prec):
+        o = N.MCOpts()
+        o.precision = prec
+        o.cull = 1
+        V, T = ctypes.c_int64(), ctypes.c_int64()
+        st = N.MCStats()
+        s = L.mc_search_device(ctx.ptr, ds.ptr, DELTA, ITERS, ctypes.byref(o), ctypes.byref(V),
+                               ctypes.byref(T), ctypes.byref(st))
+        if s != 0:
+            raise RuntimeError(L.mc_last_error(ctx.ptr).decode())
+        return st.as_dict()
+
+    def timed(prec, K):
+        sts = []
+        for _ in range(K):
+            flush.zero_()
+            torch.cuda.synchronize()
+            sts.append(step(prec))
+        return sts
+
+    for _ in range(args.warmup):
+        step(N.MC_PREC_FP32_FILTERED)
+        step(N.MC_PREC_FP64)
+
+    # Bit-identity of the two precisions on this workload (same vertex and
+    # triangle layout by construction, so array equality is mesh equality).
+    def fetch():
+        V, T = ctypes.c_int64(), ctypes.c_int64()
+        st = step_stats[-1]
+        v = np.zeros((st["vertices"], 3))
+        t = np.zeros((st["triangles"], 3), dtype=np.int32)
+        L.mc_result_copy(ctx.ptr, v.ctypes.data, t.ctypes.data)
+        return v, t
+
+    step_stats = [step(N.MC_PREC_FP32_FILTERED)]
+    v32, t32 = fetch()
+    step_stats.append(step(N.MC_PREC_FP64))
+    v64, t64 = fetch()
+    identical = bool(np.array_equal(v32.view(np.uint64), v64.view(np.uint64)) and
+                     np.array_equal(t32, t64))
+
+    barrier()
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        sts = timed(N.MC_PREC_FP32_FILTERED, args.steps)
+    barrier()
+    wall = time.perf_counter() - t0
+    sts64 = timed(N.MC_PREC_FP64, args.steps)
+
+    ms = [s["ms_total"] for s in sts]
+    ms_step = float(np.mean(ms))
+    if ws > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    corners = sts[0]["corners"]
+    value = ws * corners / (ms_step / 1000.0)
+    ms64 = float(np.mean([s["ms_total"] for s in sts64]))
+    value64 = ws * corners / (ms64 / 1000.0)
+
+    # End to end through the public call: serialise, lower + upload the solid,
+    # search, copy the indexed mesh to host arrays.
+    e2e_t, h2d, d2h = [], 0, 0
+    for i in range(max(args.steps, 1)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        m = MarchingCubesSearch(solid, DELTA, ITERS, ctx=ctx)
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t)
+        h2d = m.stats["h2d_bytes"] + int(ds.nodes.nbytes)
+        d2h = m.stats["d2h_bytes"]
+    e2e_s = float(np.median(e2e_t))
+
+    # Roofline of the dominant kernel.
+    phases = {k: float(np.mean([s[k] for s in sts]))
+              for k in ("ms_classify", "ms_count", "ms_emit", "ms_search")}
+    dom = max(phases, key=phases.get)
+    peaks, kind = measured_peaks()
+    roof = roofline(dom, phases[dom], sts[0], peaks, kind)
+
+    if rank == 0:
+        cpu = None
+        if ws == 1 and not args.no_cpu:
+            threads = os.cpu_count() or 1
+            nodes, sets = serialize(solid)
+            cv, info = cpu_sample(nodes, sets, sts[0]["nz"], threads)
+            cpu = {"value": cv, "unit": "corners/s", "cores": threads, "kind": "port",
+                   "sample": (f"oracle port, {threads} threads, z-slabs {info['slabs'][0]}.."
+                              f"{info['slabs'][1]} ({info['corners']} corners, "
+                              f"{info['seconds']:.1f} s)")}
+        s0 = sts[0]
+        out = {
+            "metric": METRIC, "value": value, "unit": "corners/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32-filtered/f64", "data": "synthetic (seeded splitmix64)",
+            "config": {"workload": WORKLOAD, "grid": [s0["nx"], s0["ny"], s0["nz"]],
+                       "corners": corners, "precision": "fp32-filtered, fp64 escalation",
+                       "parallelism": "replicas" if ws > 1 else "1 GPU",
+                       "l2": "flushed (256 MiB write) before every timed step"},
+            "meshes_per_s": ws / (ms_step / 1000.0),
+            "triangles_per_s": ws * s0["triangles"] / (ms_step / 1000.0),
+            "fp64": {"value": value64, "unit": "corners/s", "ms_per_step": ms64},
+            "fp32_over_fp64": value / value64,
+            "bit_identical_fp32_fp64": identical,
+            "escalation_rate": s0["escalations"] / max(1, s0["leaf_evals"]),
+            "mesh": {"vertices": s0["vertices"], "triangles": s0["triangles"]},
+            "phases_ms": phases,
+            "gpu_launches": 6 * args.steps,
+            "roofline": roof,
+            "clocks": clk.summary(),
+            "wall_s_timed_region": wall,
+            "e2e": {"value": corners / e2e_s, "unit": "corners/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "ms_per_step": 1000 * e2e_s},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def roofline(kernel, ms, st, peaks, kind):
+    """Algorithmic bytes of one launch of the dominant kernel over its CUDA-
+    event time, against the measured HBM copy bandwidth."""
+    nx, ny, nz = st["nx"], st["ny"], st["nz"]
+    W = (nx + 31) // 32 + 1
+    bits = nz * ny * W * 4
+    chunks = ((nx - 1 + 31) // 32) * (ny - 1) * (nz - 1)
+    V, T = st["vertices"], st["triangles"]
+    if kernel == "ms_classify":
+        alg = bits                                  # one bit per corner written
+    elif kernel == "ms_count":
+        alg = bits + chunks * 4 * 3                 # bits read; counts + 2 prefixes written
+    elif kernel == "ms_emit":
+        alg = bits + chunks * 12 + V * 8 + T * 12   # bits + offsets read; keys, triangles written
+    else:
+        alg = V * 8 + V * 24                        # keys read, vertices written
+    achieved = alg / (ms / 1000.0) / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    return {"kernel": kernel.replace("ms_", "k_"), "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "algorithmic_bytes": int(alg), "ms": ms, "peak_kind": kind}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -147,10 +147,13 @@ typedef struct mc_stats {
     int64_t tiles_const;     /* tiles decided without evaluating any leaf */
     int64_t bvh_nodes;       /* collider: BVH nodes whose box was tested */
     int64_t bvh_tris;        /* collider: ray-triangle tests */
-    double ms_classify;      /* device time per phase (CUDA events) */
-    double ms_cubes;
-    double ms_search;
-    double ms_total;
+    double ms_classify;      /* device time per phase (CUDA events on the context's stream) */
+    double ms_count;         /* cube classification + prefix sums */
+    double ms_emit;          /* vertex / triangle emission */
+    double ms_search;        /* edge bisection */
+    double ms_total;         /* first upload to last kernel, including the totals read-back */
+    int64_t h2d_bytes;       /* host-to-device bytes of the call */
+    int64_t d2h_bytes;       /* device-to-host bytes of the call (incl. the mesh for mc_search) */
 } mc_stats;
 
 /* Indexed mesh: vertices n_vertices x 3 float64, triangles n_triangles x 3

@@ -42,7 +42,9 @@ class MCStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int64) for n in (
         "nx", "ny", "nz", "corners", "vertices", "triangles", "leaf_evals", "escalations",
         "tiles", "tiles_const", "bvh_nodes", "bvh_tris")] + [
-        (n, ctypes.c_double) for n in ("ms_classify", "ms_cubes", "ms_search", "ms_total")]
+        (n, ctypes.c_double) for n in ("ms_classify", "ms_count", "ms_emit", "ms_search",
+                                       "ms_total")] + [
+        (n, ctypes.c_int64) for n in ("h2d_bytes", "d2h_bytes")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

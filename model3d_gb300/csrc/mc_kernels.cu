@@ -778,7 +778,7 @@ void build_table_host() {
 struct mc_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[8] = {};
     std::string err;
     DevBuf xs, ys, zs, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
     DevBuf pts, pout;
@@ -1029,6 +1029,7 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     g.nz = nz;
     g.W = (nx + 31) / 32 + 1;
     g.CX = nx >= 2 ? (nx - 1 + 31) / 32 : 0;
+    CK(cudaEventRecord(ctx->ev[0], sm));
     CK(ctx->xs.ensure(nx * 8));
     CK(ctx->ys.ensure(ny * 8));
     CK(ctx->zs.ensure(nz * 8));
@@ -1049,7 +1050,7 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     CK(cudaMemsetAsync(ctx->bits.p, 0, nbits * 4, sm));
 
     const ProgView& P = solid->view;
-    CK(cudaEventRecord(ctx->ev[0], sm));
+    CK(cudaEventRecord(ctx->ev[5], sm));
     // ---- classify
     ClassifyArgs ca{};
     ca.bits = ctx->bits.as<uint32_t>();
@@ -1089,6 +1090,7 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
                                             nchunks, ctx->prefv.as<uint32_t>(), ctx->preft.as<uint32_t>());
         CK(cudaGetLastError());
     }
+    CK(cudaEventRecord(ctx->ev[6], sm));
     unsigned long long* hp = ctx->h_pin;
     CK(cudaMemcpyAsync(hp, ctx->totals.p, 16, cudaMemcpyDeviceToHost, sm));
     CK(cudaMemcpyAsync(hp + 2, ctx->errs.p, ER_N * 4, cudaMemcpyDeviceToHost, sm));
@@ -1143,17 +1145,18 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     st.bvh_tris = (int64_t)hp[8 + ST_TRIS];
     st.tiles_const = (int64_t)hp[8 + ST_TILES_CONST];
     float ms;
-    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[1]);
     st.ms_classify = ms;
-    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
-    st.ms_cubes = ms;
-    float ms_emit;
-    cudaEventElapsedTime(&ms_emit, ctx->ev[2], ctx->ev[3]);
-    st.ms_cubes += ms_emit;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[6]);
+    st.ms_count = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+    st.ms_emit = ms;
     cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
     st.ms_search = ms;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[4]);
     st.ms_total = ms;
+    st.h2d_bytes = (int64_t)(nx + ny + nz) * 8;
+    st.d2h_bytes = 16 + 2 * ER_N * 4 + ST_N * 8;
     ctx->last_V = V;
     ctx->last_T = T;
     if (n_vertices) *n_vertices = V;
@@ -1200,6 +1203,7 @@ mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t it
     }
     out->n_vertices = V;
     out->n_triangles = T;
+    out->stats.d2h_bytes += V * 24 + T * 12;
     return MC_OK;
 }
 
