@@ -239,6 +239,39 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
  * corner pairs tris[c][t][0..5]. */
 mc_status mc_case_table(uint8_t counts[256], uint8_t tris[256][5][6]);
 
+/*
+ * Allocation-free MarchingCubesSearch, for callers that cannot allocate
+ * device memory when they mesh: a process whose device memory belongs to
+ * another allocator that hands the caller only its own buffers, or a
+ * real-time loop that forbids cudaMalloc / cudaFree after start-up because
+ * those calls can synchronise the whole device.  No counterpart in the
+ * reference (it is a GPU-memory concern the Go code does not have).
+ *
+ * Same result as mc_search for CSG solids (no MC_NODE_COLLIDER nodes; those
+ * return MC_ERR_BAD_PROGRAM).  Every intermediate array lives in one
+ * file-scope device array of MC_NOALLOC_SCRATCH_BYTES, which every GPU that
+ * loads the library holds until the process exits; the call makes no
+ * cudaMalloc / cudaFree.  Inputs: the node array (host memory), delta,
+ * iters, opts (may be NULL), the stream to run on (NULL: the legacy default
+ * stream) on the current device.  Outputs: device buffers vertices
+ * (vertex_cap x 3 float64) and triangles (triangle_cap x 3 int32), written in
+ * the same layout as mc_search_device; *n_vertices / *n_triangles receive the
+ * mesh size, also when the status is MC_ERR_LIMIT because a buffer is too
+ * small (the caller can retry with larger buffers).  A grid or program that
+ * does not fit the scratch array returns MC_ERR_LIMIT.
+ *
+ * The first call on a device looks up the scratch array's device address
+ * (cudaGetSymbolAddress) and uploads the case table; make that first call
+ * before any stream capture.  All calls share the scratch array, which
+ * keeps the last call's contents (each call clears what must start at
+ * zero): calls whose GPU work overlaps, from other threads or streams, race.
+ */
+#define MC_NOALLOC_SCRATCH_BYTES (64u << 20)
+mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, double delta, int32_t iters,
+                            const mc_opts* opts, void* stream, double* vertices,
+                            int64_t vertex_cap, int32_t* triangles, int64_t triangle_cap,
+                            int64_t* n_vertices, int64_t* n_triangles);
+
 /* Library version string. */
 const char* mc_version(void);
 

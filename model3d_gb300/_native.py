@@ -34,7 +34,7 @@ EXPORTS = [
     "mc_status_string", "mc_last_error", "mc_create", "mc_destroy", "mc_solid_create",
     "mc_solid_destroy", "mc_solid_bounds", "mc_spacer_axis", "mc_search", "mc_mesh_free",
     "mc_search_device", "mc_result_device", "mc_result_copy", "mc_contains", "mc_search_batch",
-    "mc_case_table", "mc_version",
+    "mc_case_table", "mc_version", "mc_search_noalloc",
 ]
 
 
@@ -115,6 +115,8 @@ def lib():
         L.mc_search_batch.argtypes = [vp, ctypes.POINTER(MCJob), ctypes.c_size_t,
                                       ctypes.POINTER(MCOpts), ctypes.POINTER(MCMesh), vp]
         L.mc_case_table.argtypes = [vp, vp]
+        L.mc_search_noalloc.argtypes = [vp, ctypes.c_size_t, dbl, i32, ctypes.POINTER(MCOpts), vp,
+                                        vp, i64, vp, i64, ctypes.POINTER(i64), ctypes.POINTER(i64)]
         for name in EXPORTS:
             getattr(L, name)  # every declared entry point must be exported
         _lib = L

@@ -1254,3 +1254,222 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
 }
 
 }  // extern "C"
+
+// ======================================================================
+// Allocation-free MarchingCubesSearch (mc_search_noalloc).
+//
+// For callers that cannot call cudaMalloc at the time they mesh: a process
+// whose device memory is owned by another allocator that only hands out the
+// caller's own input/output buffers, or a real-time loop that forbids
+// cudaMalloc/cudaFree after start-up because those calls can synchronise the
+// whole device.  The same kernels run with every intermediate array (the
+// lowered program, the spacer, corner bits, chunk counts and offsets, vertex
+// keys, error and statistics words) carved out of one file-scope device
+// array of MC_NOALLOC_SCRATCH_BYTES bytes.  Every GPU that loads this library
+// holds that array until the process exits.  All calls share it, so calls
+// whose work overlaps on the GPU (other host threads, other streams) race.
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MC_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 256;
+std::mutex g_noalloc_mu;
+void* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// Once per device, with that device current: the device address of the
+// scratch array (the host-side symbol is only a stand-in) and the case table.
+mc_status noalloc_setup(int dev, unsigned char** base) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return MC_ERR_ARG;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_base[dev]) {
+        std::call_once(g_table_once, build_table_host);
+        if (g_table_status != 0) return MC_ERR_LIMIT;
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return MC_ERR_CUDA;
+        if (cudaMemcpyToSymbol(c_table, &g_table_host, sizeof(CaseTable)) != cudaSuccess) return MC_ERR_CUDA;
+        g_noalloc_base[dev] = p;
+    }
+    *base = (unsigned char*)g_noalloc_base[dev];
+    return MC_OK;
+}
+
+struct Carver {
+    unsigned char* base;
+    size_t used = 0;
+    bool ok = true;
+    unsigned char* take(size_t bytes) {
+        size_t off = (used + 255) & ~(size_t)255;
+        if (off + bytes > MC_NOALLOC_SCRATCH_BYTES) {
+            ok = false;
+            return base;
+        }
+        used = off + bytes;
+        return base + off;
+    }
+};
+
+}  // namespace
+
+extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, double delta, int32_t iters,
+                                       const mc_opts* opts_in, void* stream, double* vertices,
+                                       int64_t vertex_cap, int32_t* triangles, int64_t triangle_cap,
+                                       int64_t* n_vertices, int64_t* n_triangles) {
+    if (!nodes || n_nodes == 0 || iters < 0 || vertex_cap < 0 || triangle_cap < 0) return MC_ERR_ARG;
+    if (n_vertices) *n_vertices = 0;
+    if (n_triangles) *n_triangles = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MC_ERR_CUDA;
+    unsigned char* base = nullptr;
+    mc_status s0 = noalloc_setup(dev, &base);
+    if (s0 != MC_OK) return s0;
+    mc_opts opts = default_opts(opts_in);
+    cudaStream_t sm = (cudaStream_t)stream;
+
+    HostProgram H;
+    try {
+        lower_scene(nodes, n_nodes, nullptr, 0, &H);  // CSG solids only: no triangle sets
+    } catch (const LowerError& e) {
+        return e.status;
+    } catch (const std::exception&) {
+        return MC_ERR_BAD_PROGRAM;
+    }
+    if (!bounds_valid(H.root_min, H.root_max)) return MC_ERR_INVALID_BOUNDS;
+    std::vector<double> X, Y, Z;
+    if (spacer_axis(H.root_min[0], H.root_max[0], delta, &X, kMaxAxis + 1) ||
+        spacer_axis(H.root_min[1], H.root_max[1], delta, &Y, kMaxAxis + 1) ||
+        spacer_axis(H.root_min[2], H.root_max[2], delta, &Z, kMaxAxis + 1))
+        return MC_ERR_GRID;
+    const int nx = (int)X.size(), ny = (int)Y.size(), nz = (int)Z.size();
+
+    // Carve the scratch array; refuse anything that does not fit.
+    Carver cv{base};
+    struct Piece {
+        const void* src;
+        size_t bytes;
+        unsigned char* dst;
+    };
+    std::vector<Piece> up = {
+        {H.ops.data(), H.ops.size() * 4, nullptr},         {H.ops_allfalse.data(), H.ops_allfalse.size() * 4, nullptr},
+        {H.leaf_kind.data(), H.leaf_kind.size() * 4, nullptr}, {H.leaf_d.data(), H.leaf_d.size() * 8, nullptr},
+        {H.leaf_f.data(), H.leaf_f.size() * 4, nullptr},   {H.cull.data(), H.cull.size() * 8, nullptr},
+        {H.xbox.data(), H.xbox.size() * sizeof(XBoxD), nullptr}, {H.xstep.data(), H.xstep.size() * sizeof(XStepD), nullptr},
+        {X.data(), X.size() * 8, nullptr},                 {Y.data(), Y.size() * 8, nullptr},
+        {Z.data(), Z.size() * 8, nullptr},
+    };
+    for (auto& p : up) p.dst = cv.take(p.bytes);
+    int* errs = (int*)cv.take(ER_N * 4);
+    unsigned long long* stats = (unsigned long long*)cv.take(ST_N * 8);
+    unsigned long long* totals = (unsigned long long*)cv.take(16);
+    GridView g{};
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.W = (nx + 31) / 32 + 1;
+    g.CX = nx >= 2 ? (nx - 1 + 31) / 32 : 0;
+    const size_t nbits = (size_t)nz * ny * g.W;
+    uint32_t* bits = (uint32_t*)cv.take(nbits * 4);
+    long long nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)g.CX * (ny - 1) * (nz - 1) : 0;
+    int nblk = (int)((nchunks + 255) / 256);
+    uint32_t* packed = (uint32_t*)cv.take(nchunks * 4);
+    uint32_t* blocksum = (uint32_t*)cv.take((size_t)nblk * 8);
+    unsigned long long* blockoff = (unsigned long long*)cv.take((size_t)nblk * 16);
+    uint32_t* prefv = (uint32_t*)cv.take(nchunks * 4);
+    uint32_t* preft = (uint32_t*)cv.take(nchunks * 4);
+    if (!cv.ok) return MC_ERR_LIMIT;  // grid or program larger than the scratch array
+    unsigned char* keys_base = cv.take(0);
+    const long long keys_cap = (long long)((MC_NOALLOC_SCRATCH_BYTES - (keys_base - base)) / 8);
+
+    // The program, spacer and zeroed words / corner bits.
+    std::vector<unsigned char> staging;
+    {
+        size_t lo = (size_t)(up.front().dst - base), hi = (size_t)(up.back().dst - base) + up.back().bytes;
+        staging.assign(hi - lo, 0);
+        for (auto& p : up)
+            if (p.bytes) std::memcpy(staging.data() + (p.dst - base - lo), p.src, p.bytes);
+        if (cudaMemcpyAsync(base + lo, staging.data(), hi - lo, cudaMemcpyHostToDevice, sm) != cudaSuccess)
+            return MC_ERR_CUDA;
+    }
+    if (cudaMemsetAsync(errs, 0, ER_N * 4, sm) != cudaSuccess || cudaMemsetAsync(stats, 0, ST_N * 8, sm) != cudaSuccess ||
+        cudaMemsetAsync(totals, 0, 16, sm) != cudaSuccess || cudaMemsetAsync(bits, 0, nbits * 4, sm) != cudaSuccess)
+        return MC_ERR_CUDA;
+    g.xs = (const double*)up[8].dst;
+    g.ys = (const double*)up[9].dst;
+    g.zs = (const double*)up[10].dst;
+    ProgView P{};
+    P.ops = (const uint32_t*)up[0].dst;
+    P.ops_allfalse = (const uint32_t*)up[1].dst;
+    P.leaf_kind = (const int32_t*)up[2].dst;
+    P.leaf_d = (const double*)up[3].dst;
+    P.leaf_f = (const float*)up[4].dst;
+    P.cull = (const double*)up[5].dst;
+    P.xbox = (const XBoxD*)up[6].dst;
+    P.xstep = (const XStepD*)up[7].dst;
+    P.n_ops = (int32_t)H.ops.size();
+    P.n_ops_allfalse = H.n_ops_allfalse;
+    P.n_leaves = (int32_t)H.leaf_kind.size();
+    P.n_xbox = (int32_t)H.xbox.size();
+
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ClassifyArgs ca{};
+    ca.bits = bits;
+    ca.err = errs;
+    ca.stats = stats;
+    ca.prec = opts.precision;
+    ca.cull = opts.cull;
+    ca.ty = opts.tile_y > 0 ? opts.tile_y : 8;
+    ca.tz = opts.tile_z > 0 ? opts.tile_z : 8;
+    ca.ntx = (nx + 31) / 32;
+    ca.nty = (ny + ca.ty - 1) / ca.ty;
+    ca.ntz = (nz + ca.tz - 1) / ca.tz;
+    long long ntiles = (long long)ca.ntx * ca.nty * ca.ntz;
+    size_t smem_c = 4 * (size_t)P.n_ops + (size_t)P.n_leaves + 16;
+    if (smem_c > 48 * 1024) return MC_ERR_LIMIT;
+    k_classify<<<(int)std::min<long long>(ntiles, (long long)sms * 8), 256, smem_c, sm>>>(g, P, ca);
+    if (nchunks > 0) {
+        k_count<<<nblk, 256, 0, sm>>>(g, CountArgs{bits, packed, blocksum, nchunks});
+        k_scan_blocks<<<1, 1024, 0, sm>>>(blocksum, blockoff, nblk, totals);
+        k_scan_chunks<<<nblk, 256, 0, sm>>>(packed, blockoff, nchunks, prefv, preft);
+    }
+    if (cudaGetLastError() != cudaSuccess) return MC_ERR_CUDA;
+    unsigned long long h[2 + (ER_N + 1) / 2] = {0};
+    if (cudaMemcpyAsync(h, totals, 16, cudaMemcpyDeviceToHost, sm) != cudaSuccess ||
+        cudaMemcpyAsync(h + 2, errs, ER_N * 4, cudaMemcpyDeviceToHost, sm) != cudaSuccess ||
+        cudaStreamSynchronize(sm) != cudaSuccess)
+        return MC_ERR_CUDA;
+    const int* herr = (const int*)(h + 2);
+    if (herr[ER_BORDER]) return MC_ERR_BOUNDS_INSIDE;
+    const long long V = (long long)h[0], T = (long long)h[1];
+    if (n_vertices) *n_vertices = V;
+    if (n_triangles) *n_triangles = T;
+    if (V > keys_cap) return MC_ERR_LIMIT;  // vertex keys do not fit the scratch array
+    if (V > vertex_cap || T > triangle_cap || (V > 0 && !vertices) || (T > 0 && !triangles))
+        return MC_ERR_LIMIT;  // caller's buffers too small; *n_vertices / *n_triangles say how large
+    if (nchunks > 0 && (V > 0 || T > 0)) {
+        EmitArgs ea{bits, packed, prefv, preft, (unsigned long long*)keys_base, triangles, nchunks};
+        k_emit<<<nblk, 256, 0, sm>>>(g, ea);
+    }
+    if (V > 0) {
+        SearchArgs sa{};
+        sa.keys = (const unsigned long long*)keys_base;
+        sa.verts = vertices;
+        sa.nverts = V;
+        sa.iters = iters;
+        sa.prec = opts.precision;
+        sa.cull = opts.cull;
+        sa.err = errs;
+        sa.stats = stats;
+        size_t per_warp = 4 * (size_t)P.n_ops + (((size_t)P.n_leaves + 15) & ~(size_t)15);
+        if (4 * per_warp > 48 * 1024) return MC_ERR_LIMIT;
+        k_search<<<(int)std::min<long long>((V + 127) / 128, (long long)sms * 16), 128, 4 * per_warp, sm>>>(g, P, sa);
+    }
+    if (cudaGetLastError() != cudaSuccess) return MC_ERR_CUDA;
+    if (cudaMemcpyAsync(h + 2, errs, ER_N * 4, cudaMemcpyDeviceToHost, sm) != cudaSuccess ||
+        cudaStreamSynchronize(sm) != cudaSuccess)
+        return MC_ERR_CUDA;
+    if (herr[ER_NOT_ON_EDGE]) return MC_ERR_NOT_ON_EDGE;
+    if (herr[ER_EDGE_INDEX]) return MC_ERR_EDGE_INDEX;
+    if (herr[ER_LIMIT]) return MC_ERR_LIMIT;
+    return MC_OK;
+}
