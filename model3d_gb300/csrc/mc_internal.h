@@ -33,7 +33,12 @@ enum Op : uint32_t {
     OP_BOXAND = 9,  // top &= inbox(arg, point)  (CheckedFuncSolid)
     OP_TRUE = 10,
     OP_FALSE = 11,
+    OP_JLEAVES = 12,  // push OR of leaves [a, a + n)   (arg = a << 14 | n; n-ary JoinedSolid)
+    OP_ALEAVES = 13,  // push AND of leaves [a, a + n)  (n-ary IntersectedSolid)
+    OP_JLIST = 14,    // push OR of the arg leaves whose ids follow as raw words (only produced by folding)
 };
+__host__ __device__ inline uint32_t range_first(uint32_t arg) { return arg >> 14; }
+__host__ __device__ inline uint32_t range_count(uint32_t arg) { return arg & 0x3fffu; }
 __host__ __device__ inline uint32_t make_op(uint32_t code, uint32_t arg) { return (code << 28) | arg; }
 __host__ __device__ inline uint32_t op_code(uint32_t op) { return op >> 28; }
 __host__ __device__ inline uint32_t op_arg(uint32_t op) { return op & 0x0fffffffu; }
@@ -128,6 +133,7 @@ struct ProgView {
     const double* leaf_d;   // n_leaves * LEAF_D
     const float* leaf_f;    // n_leaves * LEAF_F
     const double* cull;     // n_leaves * 6: lo.xyz, hi.xyz (world space, widened); NaN = never cull
+    const float* cull_f;    // the same boxes rounded outward to float
     const XBoxD* xbox;
     const XStepD* xstep;
     const TreeD* trees;
@@ -140,6 +146,8 @@ struct ProgView {
     int32_t n_ops_allfalse;  // -1: const false, -2: const true, else length
     int32_t n_leaves;
     int32_t n_xbox;
+    int32_t rows_ok;  // no TRANSFORM node: tiles may be evaluated row-vectorised
+    int32_t fold_cap; // longest folded program (words)
 };
 
 // Constant folding of a postfix program given which leaves are active
@@ -152,8 +160,36 @@ constexpr int FOLD_FALSE = -1;
 constexpr int FOLD_TRUE = -2;
 constexpr int FOLD_STACK = MAX_STACK + MAX_XDEPTH + 2;
 
-template <class Active>
-__host__ __device__ inline int fold_program(const uint32_t* ops, int n, Active active, uint32_t* q) {
+__host__ __device__ inline int ctz32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    return __ffs((int)x) - 1;
+#else
+    return __builtin_ctz(x);
+#endif
+}
+
+__host__ __device__ inline int popcount32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
+}
+
+// Bits of word w that fall in [a, e).
+__host__ __device__ inline uint32_t range_mask(uint32_t w, uint32_t a, uint32_t e) {
+    uint32_t m = ~0u;
+    if ((w << 5) < a) m &= ~0u << (a & 31);
+    if (((w + 1) << 5) > e) m &= (e & 31) ? ((1u << (e & 31)) - 1u) : ~0u;
+    return m;
+}
+
+// act: one bit per leaf (32 per word); nullptr means every leaf is inactive.
+__host__ __device__ inline bool leaf_active(const uint32_t* act, uint32_t l) {
+    return act && ((act[l >> 5] >> (l & 31)) & 1u);
+}
+
+__host__ __device__ inline int fold_program(const uint32_t* ops, int n, const uint32_t* act, uint32_t* q) {
     // Entries: >= 0 fragment start; -1 const false; -2 const true; <= -3 marker (-3 - start).
     int stk[FOLD_STACK];
     int sp = 0, qn = 0;
@@ -162,13 +198,39 @@ __host__ __device__ inline int fold_program(const uint32_t* ops, int n, Active a
         uint32_t code = op_code(op), arg = op_arg(op);
         switch (code) {
             case OP_LEAF:
-                if (active(arg)) {
+                if (leaf_active(act, arg)) {
                     stk[sp++] = qn;
                     q[qn++] = op;
                 } else {
                     stk[sp++] = FOLD_FALSE;
                 }
                 break;
+            case OP_JLEAVES:
+            case OP_ALEAVES: {
+                // Count the active leaves of the range word by word.
+                const uint32_t a = range_first(arg), cnt = range_count(arg), e = a + cnt;
+                uint32_t k = 0;
+                if (act)
+                    for (uint32_t w = a >> 5; w <= ((e - 1) >> 5); w++) k += popcount32(act[w] & range_mask(w, a, e));
+                if (k == 0 || (code == OP_ALEAVES && k < cnt)) {
+                    stk[sp++] = FOLD_FALSE;  // an inactive leaf is false everywhere here
+                } else if (k == cnt) {
+                    stk[sp++] = qn;
+                    q[qn++] = op;
+                } else {
+                    stk[sp++] = qn;
+                    if (k > 1) q[qn++] = make_op(OP_JLIST, k);
+                    for (uint32_t w = a >> 5; w <= ((e - 1) >> 5); w++) {
+                        uint32_t bits = act[w] & range_mask(w, a, e);
+                        while (bits) {
+                            uint32_t l = (w << 5) + (uint32_t)ctz32(bits);
+                            bits &= bits - 1;
+                            q[qn++] = k > 1 ? l : make_op(OP_LEAF, l);
+                        }
+                    }
+                }
+                break;
+            }
             case OP_TRUE: stk[sp++] = FOLD_TRUE; break;
             case OP_FALSE: stk[sp++] = FOLD_FALSE; break;
             case OP_OR:

@@ -41,7 +41,7 @@ struct Counts {
     unsigned long long leaf = 0, esc = 0, nodes = 0, tris = 0;
 };
 
-enum StatSlot { ST_LEAF = 0, ST_ESC, ST_NODES, ST_TRIS, ST_TILES_CONST, ST_N };
+enum StatSlot { ST_LEAF = 0, ST_ESC, ST_NODES, ST_TRIS, ST_TILES_CONST, ST_WORK, ST_N };
 enum ErrSlot { ER_BORDER = 0, ER_NOT_ON_EDGE, ER_EDGE_INDEX, ER_LIMIT, ER_N };
 
 __device__ __forceinline__ void flush_counts(const Counts& c, unsigned long long* stats) {
@@ -131,24 +131,12 @@ __device__ P3 apply_inverse(const ProgView& P, const XBoxD& b, P3 p) {
     return p;
 }
 
-__device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf, int prec, Counts& cnt,
-                                          int* err) {
-    int kind = P.leaf_kind[id];
+// Float64 predicate of one leaf at one point (reference operation order).
+// Out of line: it is the rare path (escalations, tori, colliders) of the
+// filtered kernels, and keeping it out keeps their hot loops small.
+__device__ __noinline__ bool leaf64_point(const ProgView& P, int id, P3 p, Counts& cnt, int* err) {
     const double* d = P.leaf_d + (size_t)id * LEAF_D;
-    cnt.leaf++;
-    if (prec == MC_PREC_FP32_FILTERED && kind <= LK_CAPSULE) {
-        const float* f = P.leaf_f + (size_t)id * LEAF_F;
-        int r;
-        switch (kind) {
-            case LK_SPHERE: r = sphere_32(f, pf); break;
-            case LK_RECT: r = rect_32(f, pf); break;
-            case LK_CYLINDER: r = cylinder_32(f, pf); break;
-            default: r = capsule_32(f, pf); break;
-        }
-        if (r != 2) return r;
-        cnt.esc++;
-    }
-    switch (kind) {
+    switch (P.leaf_kind[id]) {
         case LK_SPHERE: return sphere_64(d, p);
         case LK_RECT: return rect_64(d, p);
         case LK_CYLINDER: return cylinder_64(d, p);
@@ -158,18 +146,59 @@ __device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf
     }
 }
 
+template <int PREC>
+__device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf, Counts& cnt, int* err) {
+    cnt.leaf++;
+    if (PREC == MC_PREC_FP32_FILTERED) {
+        const int kind = P.leaf_kind[id];
+        if (kind <= LK_CAPSULE) {
+            const float* f = P.leaf_f + (size_t)id * LEAF_F;
+            int r;
+            switch (kind) {
+                case LK_SPHERE: r = sphere_32(f, pf); break;
+                case LK_RECT: r = rect_32(f, pf); break;
+                case LK_CYLINDER: r = cylinder_32(f, pf); break;
+                default: r = capsule_32(f, pf); break;
+            }
+            if (r != 2) return r;
+            cnt.esc++;
+        }
+    }
+    return leaf64_point(P, id, p, cnt, err);
+}
+
 // Evaluate a (possibly folded) postfix program at p.  Bit stack: top = bit 0.
-__device__ bool eval_program(const ProgView& P, const uint32_t* q, int nq, P3 p, int prec, Counts& cnt,
-                             int* err) {
+template <int PREC>
+__device__ bool eval_program(const ProgView& P, const uint32_t* q, int nq, P3 p, F3 pf, Counts& cnt, int* err) {
     uint32_t st = 0;
     P3 saved[MAX_XDEPTH];
     int sp = 0;
-    F3 pf = to_f3(p);
     for (int i = 0; i < nq; i++) {
         uint32_t op = q[i];
         uint32_t arg = op_arg(op);
         switch (op_code(op)) {
-            case OP_LEAF: st = (st << 1) | (eval_leaf(P, arg, p, pf, prec, cnt, err) ? 1u : 0u); break;
+            case OP_LEAF: st = (st << 1) | (eval_leaf<PREC>(P, arg, p, pf, cnt, err) ? 1u : 0u); break;
+            case OP_JLEAVES:
+            case OP_ALEAVES: {  // short-circuit OR / AND over a leaf range
+                const uint32_t a0 = range_first(arg), e = a0 + range_count(arg);
+                const bool isor = op_code(op) == OP_JLEAVES;
+                bool v = !isor;
+                for (uint32_t l = a0; l < e; l++)
+                    if (eval_leaf<PREC>(P, l, p, pf, cnt, err) == isor) {
+                        v = isor;
+                        break;
+                    }
+                st = (st << 1) | (v ? 1u : 0u);
+                break;
+            }
+            case OP_JLIST: {
+                bool v = false;
+                for (uint32_t k = 0; k < arg; k++)
+                    if (!v) v = eval_leaf<PREC>(P, q[i + 1 + k], p, pf, cnt, err);
+                i += arg;
+                st = (st << 1) | (v ? 1u : 0u);
+                break;
+            }
             case OP_OR: {
                 uint32_t b = st & 1u;
                 st = (st >> 1) | b;
@@ -209,6 +238,294 @@ __device__ bool eval_program(const ProgView& P, const uint32_t* q, int nq, P3 p,
     return st & 1u;
 }
 
+
+// ------------------------------------------------------------ row-vectorised tiles
+//
+// A tile is 32 corners in x (one per lane) by up to 32 rows (y, z).  For a
+// program without transforms every leaf is evaluated for all rows of the
+// lane's x at once: the x-dependent part of the predicate once per lane, the
+// (y, z)-dependent part once per row by lane r and broadcast with shuffles.
+// The float64 path keeps the reference's operation order (the shared pieces
+// are exactly the reference's subexpressions, e.g. dx*dx of Coord3D.Dist).
+// Results are row masks (bit r = row r) combined with bitwise operators.
+
+struct RowCtx {
+    double px;        // this lane's x
+    float pxf;
+    double ry, rz;    // lane r < nrows: coordinates of row r
+    float ryf, rzf;
+    int nrows;
+    uint32_t rowmask; // rows inside the grid
+    int y0, z0, ty;   // row r is (y0 + r % ty, z0 + r / ty)
+    const double* ys;
+    const double* zs;
+};
+
+__device__ __forceinline__ P3 row_point(const RowCtx& rc, int r) {
+    return P3{rc.px, rc.ys[rc.y0 + r % rc.ty], rc.zs[rc.z0 + r / rc.ty]};
+}
+
+__device__ __noinline__ bool sphere_64_ni(const double* c, P3 p) { return sphere_64(c, p); }
+__device__ __noinline__ bool cylinder_64_ni(const double* c, P3 p) { return cylinder_64(c, p); }
+__device__ __noinline__ bool capsule_64_ni(const double* c, P3 p) { return capsule_64(c, p); }
+
+__device__ __forceinline__ float shf(float v, int r) { return __shfl_sync(0xffffffffu, v, r); }
+__device__ __forceinline__ double shd(double v, int r) { return __shfl_sync(0xffffffffu, v, r); }
+
+// Rect: compares only, separable and exact in either precision.
+__device__ __forceinline__ uint32_t rect_rows(const double* c, const RowCtx& rc) {
+    bool xin = rc.px >= c[0] && rc.px <= c[3];
+    bool yzin = rc.ry >= c[1] && rc.ry <= c[4] && rc.rz >= c[2] && rc.rz <= c[5];
+    uint32_t m = __ballot_sync(0xffffffffu, yzin);
+    return xin ? m : 0u;
+}
+
+__device__ uint32_t sphere_rows64(const double* c, const RowCtx& rc) {
+    double dx = D_SUB(rc.px, c[0]);
+    double dx2 = D_MUL(dx, dx);
+    double dy = D_SUB(rc.ry, c[1]), dz = D_SUB(rc.rz, c[2]);
+    double dy2 = D_MUL(dy, dy), dz2 = D_MUL(dz, dz);
+    uint32_t m = 0;
+    for (int r = 0; r < rc.nrows; r++) {
+        double S = D_ADD(D_ADD(dx2, shd(dy2, r)), shd(dz2, r));
+        m |= (S <= c[3] ? 1u : 0u) << r;
+    }
+    return m;
+}
+
+__device__ uint32_t sphere_rows32(const float* f, const double* d, const RowCtx& rc, Counts& cnt) {
+    const float dx = rc.pxf - f[0];
+    const float ex = 2.001f * U32 * (fabsf(rc.pxf) + fabsf(f[0]));
+    const float tx = ex * (2.f * fabsf(dx) + ex), dx2 = dx * dx;
+    const float dy = rc.ryf - f[1], dz = rc.rzf - f[2];
+    const float ey = 2.001f * U32 * (fabsf(rc.ryf) + fabsf(f[1]));
+    const float ez = 2.001f * U32 * (fabsf(rc.rzf) + fabsf(f[2]));
+    const float dyz = __fmaf_rn(dy, dy, dz * dz);
+    const float tyz = ey * (2.f * fabsf(dy) + ey) + ez * (2.f * fabsf(dz) + ez);
+    uint32_t m = 0;
+    for (int r = 0; r < rc.nrows; r++) {
+        float S = dx2 + shf(dyz, r);
+        float E = 1.001f * (tx + shf(tyz, r) + 3.01f * U32 * S) + 1e-30f;
+        int v = decide_le(S, E, f[4], f[5]);
+        if (v == 2) {
+            cnt.esc++;
+            v = sphere_64_ni(d, row_point(rc, r));
+        }
+        m |= (uint32_t)v << r;
+    }
+    return m;
+}
+
+__device__ uint32_t cylinder_rows64(const double* c, const RowCtx& rc) {
+    const double qx = D_SUB(rc.px, c[0]);
+    const double tx = D_MUL(qx, c[3]);
+    const double ty = D_MUL(D_SUB(rc.ry, c[1]), c[4]), tz = D_MUL(D_SUB(rc.rz, c[2]), c[5]);
+    uint32_t m = 0;
+    for (int r = 0; r < rc.nrows; r++) {
+        const double frac = D_ADD(D_ADD(tx, shd(ty, r)), shd(tz, r));
+        const double yr = shd(rc.ry, r), zr = shd(rc.rz, r);
+        if (frac < 0 || frac > c[6]) continue;
+        double d1 = D_SUB(D_ADD(c[0], D_MUL(c[3], frac)), rc.px);
+        double d2 = D_SUB(D_ADD(c[1], D_MUL(c[4], frac)), yr);
+        double d3 = D_SUB(D_ADD(c[2], D_MUL(c[5], frac)), zr);
+        double S = D_ADD(D_ADD(D_MUL(d1, d1), D_MUL(d2, d2)), D_MUL(d3, d3));
+        m |= (S <= c[7] ? 1u : 0u) << r;
+    }
+    return m;
+}
+
+__device__ uint32_t cylinder_rows32(const float* f, const double* d, const RowCtx& rc, Counts& cnt) {
+    const float ax = fabsf(f[3]), ay = fabsf(f[4]), az = fabsf(f[5]);
+    const float qx = rc.pxf - f[0];
+    const float eqx = 2.001f * U32 * (fabsf(rc.pxf) + fabsf(f[0]));
+    const float efx = ax * (eqx + 4.03f * U32 * fabsf(qx));
+    const float qy = rc.ryf - f[1], qz = rc.rzf - f[2];
+    const float eqy = 2.001f * U32 * (fabsf(rc.ryf) + fabsf(f[1]));
+    const float eqz = 2.001f * U32 * (fabsf(rc.rzf) + fabsf(f[2]));
+    const float fyz = __fmaf_rn(qy, f[4], qz * f[5]);
+    const float efyz = ay * (eqy + 4.03f * U32 * fabsf(qy)) + az * (eqz + 4.03f * U32 * fabsf(qz));
+    uint32_t m = 0;
+    for (int r = 0; r < rc.nrows; r++) {
+        const float Qy = shf(qy, r), Qz = shf(qz, r), Ey = shf(eqy, r), Ez = shf(eqz, r);
+        const float frac = __fmaf_rn(qx, f[3], shf(fyz, r));
+        const float Ef = 1.001f * (efx + shf(efyz, r)) + 1e-30f;
+        const float flo = __fsub_rd(frac, Ef), fhi = __fadd_ru(frac, Ef);
+        int v;
+        if (fhi < 0.f || flo > f[7]) {
+            v = 0;
+        } else if (!(flo >= 0.f && fhi <= f[6])) {
+            v = 2;
+        } else {
+            const float d1 = __fmaf_rn(f[3], frac, -qx);
+            const float d2 = __fmaf_rn(f[4], frac, -Qy);
+            const float d3 = __fmaf_rn(f[5], frac, -Qz);
+            const float S = __fmaf_rn(d1, d1, __fmaf_rn(d2, d2, d3 * d3));
+            const float g = 1.0001f * Ef + 1.0001f * U32 * (fabsf(frac) + Ef);
+            const float e1 = ax * g + eqx + 1.0001f * U32 * fabsf(d1);
+            const float e2 = ay * g + Ey + 1.0001f * U32 * fabsf(d2);
+            const float e3 = az * g + Ez + 1.0001f * U32 * fabsf(d3);
+            float E = e1 * (2.f * fabsf(d1) + e1) + e2 * (2.f * fabsf(d2) + e2) + e3 * (2.f * fabsf(d3) + e3);
+            E = 1.001f * (E + 3.02f * U32 * S) + 1e-30f;
+            v = decide_le(S, E, f[8], f[9]);
+        }
+        if (v == 2) {
+            cnt.esc++;
+            v = cylinder_64_ni(d, row_point(rc, r));
+        }
+        m |= (uint32_t)v << r;
+    }
+    return m;
+}
+
+__device__ uint32_t capsule_rows64(const double* c, const RowCtx& rc) {
+    const double vx = D_SUB(rc.px, c[0]), t0 = D_MUL(c[6], vx);
+    const double vy = D_SUB(rc.ry, c[1]), vz = D_SUB(rc.rz, c[2]);
+    const double t1 = D_MUL(c[7], vy), t2 = D_MUL(c[8], vz);
+    uint32_t m = 0;
+    for (int r = 0; r < rc.nrows; r++) {
+        const double mag = D_ADD(D_ADD(t0, shd(t1, r)), shd(t2, r));
+        const double yr = shd(rc.ry, r), zr = shd(rc.rz, r);
+        double qx, qy, qz;
+        if (mag > c[9]) {
+            qx = c[3], qy = c[4], qz = c[5];
+        } else if (mag < 0) {
+            qx = c[0], qy = c[1], qz = c[2];
+        } else {
+            qx = D_ADD(D_MUL(c[6], mag), c[0]);
+            qy = D_ADD(D_MUL(c[7], mag), c[1]);
+            qz = D_ADD(D_MUL(c[8], mag), c[2]);
+        }
+        double d1 = D_SUB(rc.px, qx), d2 = D_SUB(yr, qy), d3 = D_SUB(zr, qz);
+        double S = D_ADD(D_ADD(D_MUL(d1, d1), D_MUL(d2, d2)), D_MUL(d3, d3));
+        m |= (S <= c[10] ? 1u : 0u) << r;
+    }
+    return m;
+}
+
+__device__ uint32_t capsule_rows32(const float* f, const double* d, const RowCtx& rc, Counts& cnt) {
+    const float ax = fabsf(f[6]), ay = fabsf(f[7]), az = fabsf(f[8]);
+    const float vx = rc.pxf - f[0];
+    const float ex = 2.001f * U32 * (fabsf(rc.pxf) + fabsf(f[0]));
+    const float emx = ax * (ex + 4.03f * U32 * fabsf(vx));
+    const float vy = rc.ryf - f[1], vz = rc.rzf - f[2];
+    const float ey = 2.001f * U32 * (fabsf(rc.ryf) + fabsf(f[1]));
+    const float ez = 2.001f * U32 * (fabsf(rc.rzf) + fabsf(f[2]));
+    const float myz = __fmaf_rn(f[7], vy, f[8] * vz);
+    const float emyz = ay * (ey + 4.03f * U32 * fabsf(vy)) + az * (ez + 4.03f * U32 * fabsf(vz));
+    uint32_t m = 0;
+    for (int r = 0; r < rc.nrows; r++) {
+        const float Vy = shf(vy, r), Vz = shf(vz, r), Ey = shf(ey, r), Ez = shf(ez, r);
+        const float Ry = shf(rc.ryf, r), Rz = shf(rc.rzf, r);
+        const float mag = __fmaf_rn(f[6], vx, shf(myz, r));
+        const float Em = 1.001f * (emx + shf(emyz, r)) + 1e-30f;
+        const float mlo = __fsub_rd(mag, Em), mhi = __fadd_ru(mag, Em);
+        float d1, d2, d3, e1, e2, e3;
+        int v = -1;
+        if (mlo > f[10]) {
+            d1 = rc.pxf - f[3], d2 = Ry - f[4], d3 = Rz - f[5];
+            e1 = 2.001f * U32 * (fabsf(rc.pxf) + fabsf(f[3]));
+            e2 = 2.001f * U32 * (fabsf(Ry) + fabsf(f[4]));
+            e3 = 2.001f * U32 * (fabsf(Rz) + fabsf(f[5]));
+        } else if (mhi < 0.f && mhi <= f[9]) {
+            d1 = vx, d2 = Vy, d3 = Vz;
+            e1 = ex, e2 = Ey, e3 = Ez;
+        } else if (mlo >= 0.f && mhi <= f[9]) {
+            d1 = __fmaf_rn(-f[6], mag, vx);
+            d2 = __fmaf_rn(-f[7], mag, Vy);
+            d3 = __fmaf_rn(-f[8], mag, Vz);
+            const float g = 1.0001f * Em + 1.0001f * U32 * (fabsf(mag) + Em);
+            e1 = ax * g + ex + 1.0001f * U32 * fabsf(d1);
+            e2 = ay * g + Ey + 1.0001f * U32 * fabsf(d2);
+            e3 = az * g + Ez + 1.0001f * U32 * fabsf(d3);
+        } else {
+            v = 2;
+        }
+        if (v < 0) {
+            const float S = __fmaf_rn(d1, d1, __fmaf_rn(d2, d2, d3 * d3));
+            float E = e1 * (2.f * fabsf(d1) + e1) + e2 * (2.f * fabsf(d2) + e2) + e3 * (2.f * fabsf(d3) + e3);
+            E = 1.001f * (E + 3.02f * U32 * S) + 1e-30f;
+            v = decide_le(S, E, f[11], f[12]);
+        }
+        if (v == 2) {
+            cnt.esc++;
+            v = capsule_64_ni(d, row_point(rc, r));
+        }
+        m |= (uint32_t)v << r;
+    }
+    return m;
+}
+
+template <int PREC>
+__device__ __forceinline__ uint32_t leaf_rows(const ProgView& P, int id, const RowCtx& rc, Counts& cnt, int* err) {
+    const int kind = P.leaf_kind[id];
+    const double* d = P.leaf_d + (size_t)id * LEAF_D;
+    const float* f = P.leaf_f + (size_t)id * LEAF_F;
+    cnt.leaf += rc.nrows;
+    constexpr bool f32 = PREC == MC_PREC_FP32_FILTERED;
+    switch (kind) {
+        case LK_RECT: return rect_rows(d, rc);
+        case LK_SPHERE: return f32 ? sphere_rows32(f, d, rc, cnt) : sphere_rows64(d, rc);
+        case LK_CYLINDER: return f32 ? cylinder_rows32(f, d, rc, cnt) : cylinder_rows64(d, rc);
+        case LK_CAPSULE: return f32 ? capsule_rows32(f, d, rc, cnt) : capsule_rows64(d, rc);
+        default: {  // torus, collider: point by point in float64
+            uint32_t m = 0;
+            for (int r = 0; r < rc.nrows; r++) m |= (leaf64_point(P, id, row_point(rc, r), cnt, err) ? 1u : 0u) << r;
+            return m;
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t box_rows(const XBoxD& b, const RowCtx& rc) {
+    bool xin = rc.px >= b.lo[0] && rc.px <= b.hi[0];
+    bool yzin = rc.ry >= b.lo[1] && rc.ry <= b.hi[1] && rc.rz >= b.lo[2] && rc.rz <= b.hi[2];
+    uint32_t m = __ballot_sync(0xffffffffu, yzin);
+    return xin ? m : 0u;
+}
+
+// Postfix program over row masks (no XPUSH/XPOP: rows_ok programs only).
+template <int PREC>
+__device__ uint32_t eval_program_rows(const ProgView& P, const uint32_t* q, int nq, const RowCtx& rc, Counts& cnt,
+                                      int* err) {
+    uint32_t stk[MAX_STACK + 1];
+    int sp = 0;
+    for (int i = 0; i < nq; i++) {
+        const uint32_t op = q[i], arg = op_arg(op);
+        switch (op_code(op)) {
+            case OP_LEAF: stk[sp++] = leaf_rows<PREC>(P, arg, rc, cnt, err); break;
+            case OP_JLEAVES: {
+                const uint32_t a0 = range_first(arg), e = a0 + range_count(arg);
+                uint32_t m = 0;
+                for (uint32_t l = a0; l < e; l++) m |= leaf_rows<PREC>(P, l, rc, cnt, err);
+                stk[sp++] = m;
+                break;
+            }
+            case OP_ALEAVES: {
+                const uint32_t a0 = range_first(arg), e = a0 + range_count(arg);
+                uint32_t m = 0xffffffffu;
+                for (uint32_t l = a0; l < e; l++) m &= leaf_rows<PREC>(P, l, rc, cnt, err);
+                stk[sp++] = m;
+                break;
+            }
+            case OP_JLIST: {
+                uint32_t m = 0;
+                for (uint32_t k = 0; k < arg; k++) m |= leaf_rows<PREC>(P, q[i + 1 + k], rc, cnt, err);
+                i += arg;
+                stk[sp++] = m;
+                break;
+            }
+            case OP_OR: sp--; stk[sp - 1] |= stk[sp]; break;
+            case OP_AND: sp--; stk[sp - 1] &= stk[sp]; break;
+            case OP_ANDNOT: sp--; stk[sp - 1] &= ~stk[sp]; break;
+            case OP_NOT: stk[sp - 1] = ~stk[sp - 1]; break;
+            case OP_BOX: stk[sp++] = box_rows(P.xbox[arg], rc); break;
+            case OP_BOXAND: stk[sp - 1] &= box_rows(P.xbox[arg], rc); break;
+            case OP_TRUE: stk[sp++] = 0xffffffffu; break;
+            default: stk[sp++] = 0u; break;
+        }
+    }
+    return stk[0] & rc.rowmask;
+}
+
 // ------------------------------------------------------------ grid
 
 struct GridView {
@@ -231,80 +548,166 @@ struct ClassifyArgs {
     uint32_t* bits;
     int* err;
     unsigned long long* stats;
+    unsigned int* work;  // zeroed work counter
+    const float* xf;     // spacer rounded to float (the FP32 filter's input)
+    const float* yf;
+    const float* zf;
     int prec;
     int cull;
-    int ty, tz;  // tile height / depth
+    int ty, tz;  // tile height / depth (rows per tile = ty * tz)
     int ntx, nty, ntz;
 };
 
-__global__ void __launch_bounds__(256) k_classify(GridView g, ProgView P, ClassifyArgs a) {
+__device__ __forceinline__ bool cull_overlap_f(const float* c, const float lo[3], const float hi[3]) {
+    return !(hi[0] < c[0] || lo[0] > c[3] || hi[1] < c[1] || lo[1] > c[4] || hi[2] < c[2] || lo[2] > c[5]);
+}
+
+// 32 x 32 bit-matrix transpose across a warp: on entry bit b of lane l is
+// A[l][b]; on exit bit b of lane l is A[b][l].  Five butterfly stages swap
+// the off-diagonal blocks of size 16, 8, 4, 2, 1.
+__device__ __forceinline__ uint32_t transpose32(uint32_t m, int lane) {
+    const uint32_t masks[5] = {0x0000ffffu, 0x00ff00ffu, 0x0f0f0f0fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int j = 16 >> k;
+        const uint32_t lo = masks[k];
+        const uint32_t other = __shfl_xor_sync(0xffffffffu, m, j);
+        m = (lane & j) ? ((m & ~lo) | ((other & ~lo) >> j)) : ((m & lo) | ((other & lo) << j));
+    }
+    return m;
+}
+
+// One warp per work item = a column of 32 x ty x tz corner tiles along x.
+// Per tile the warp ballots which leaves' culling boxes meet the tile (float
+// boxes rounded outward, tile box rounded outward) and re-folds the program
+// only when that set changed since the previous tile of the column.
+template <int PREC>
+__global__ void __launch_bounds__(256, 3) k_classify(GridView g, ProgView P, ClassifyArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t* q = (uint32_t*)smem;                          // n_ops words
-    unsigned char* active = smem + 4 * (size_t)P.n_ops;     // n_leaves bytes
-    __shared__ int s_len;
-    __shared__ const uint32_t* s_prog;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (P.n_leaves + 31) >> 5;
+    const size_t per_warp = 4 * ((size_t)P.fold_cap + 2 * (size_t)nw);
+    uint32_t* q = (uint32_t*)(smem + warp * per_warp);
+    uint32_t* cur = q + P.fold_cap;
+    uint32_t* prev = cur + nw;
     Counts cnt;
     unsigned long long nconst = 0;
-    const long long ntiles = (long long)a.ntx * a.nty * a.ntz;
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        int tx = (int)(tile % a.ntx);
-        long long r = tile / a.ntx;
-        int ty = (int)(r % a.nty), tz = (int)(r / a.nty);
-        int x0 = tx * 32, y0 = ty * a.ty, z0 = tz * a.tz;
-        int x1 = min(x0 + 31, g.nx - 1), y1 = min(y0 + a.ty - 1, g.ny - 1), z1 = min(z0 + a.tz - 1, g.nz - 1);
-        int any = 0;
-        if (a.cull) {
-            double lo[3] = {g.xs[x0], g.ys[y0], g.zs[z0]};
-            double hi[3] = {g.xs[x1], g.ys[y1], g.zs[z1]};
-            for (int l = threadIdx.x; l < P.n_leaves; l += blockDim.x) {
-                int on = cull_overlap(P.cull + 6 * (size_t)l, lo, hi);
-                active[l] = (unsigned char)on;
-                any |= on;
+    const int nitems = a.nty * a.ntz;
+    const int rows = a.ty * a.tz;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = (int)atomicAdd(a.work, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= nitems) break;
+        const int ty = item % a.nty, tz = item / a.nty;
+        const int y0 = ty * a.ty, z0 = tz * a.tz;
+        const int y1 = min(y0 + a.ty - 1, g.ny - 1), z1 = min(z0 + a.tz - 1, g.nz - 1);
+        const float ylo = __double2float_rd(g.ys[y0]), yhi = __double2float_ru(g.ys[y1]);
+        const float zlo = __double2float_rd(g.zs[z0]), zhi = __double2float_ru(g.zs[z1]);
+        bool have_prev = false;
+        int len = P.n_ops;
+        const uint32_t* prog = P.ops;
+        for (int tx = 0; tx < a.ntx; tx++) {
+            const int x0 = tx * 32, x1 = min(x0 + 31, g.nx - 1);
+            if (a.cull) {
+                const float lo[3] = {__double2float_rd(g.xs[x0]), ylo, zlo};
+                const float hi[3] = {__double2float_ru(g.xs[x1]), yhi, zhi};
+                uint32_t diff = 0, any = 0;
+                for (int k = 0; k < nw; k++) {
+                    int l = 32 * k + lane;
+                    bool on = l < P.n_leaves && cull_overlap_f(P.cull_f + 6 * (size_t)l, lo, hi);
+                    uint32_t w = __ballot_sync(0xffffffffu, on);
+                    any |= w;
+                    if (lane == 0) {
+                        diff |= (!have_prev || prev[k] != w) ? 1u : 0u;
+                        cur[k] = w;
+                        prev[k] = w;
+                    }
+                }
+                diff = __shfl_sync(0xffffffffu, diff, 0);
+                if (diff) {
+                    if (!any) {
+                        len = P.n_ops_allfalse;
+                        prog = P.ops_allfalse;
+                    } else {
+                        int L = 0;
+                        if (lane == 0)
+                            L = fold_program(P.ops, P.n_ops, cur, q);
+                        len = __shfl_sync(0xffffffffu, L, 0);
+                        prog = q;
+                    }
+                    have_prev = true;
+                }
+                __syncwarp();
+            }
+            if (len < 0) nconst++;
+            const int x = x0 + lane;
+            const bool xin = x < g.nx;
+            const double px = xin ? g.xs[x] : g.xs[g.nx - 1];
+            const float pxf = xin ? a.xf[x] : a.xf[g.nx - 1];
+            uint32_t edge_mask = 0;
+            if (x0 == 0) edge_mask |= 1u;
+            if (g.nx - 1 - x0 < 32) edge_mask |= 1u << (g.nx - 1 - x0);
+            if (len >= 0 && P.rows_ok && rows <= 32) {
+                RowCtx rc;
+                rc.px = px;
+                rc.pxf = pxf;
+                rc.nrows = rows;
+                rc.y0 = y0;
+                rc.z0 = z0;
+                rc.ty = a.ty;
+                rc.ys = g.ys;
+                rc.zs = g.zs;
+                const int ry = min(y0 + lane % a.ty, g.ny - 1), rz = min(z0 + lane / a.ty, g.nz - 1);
+                const bool rin = lane < rows && y0 + lane % a.ty < g.ny && z0 + lane / a.ty < g.nz;
+                rc.ry = g.ys[ry];
+                rc.rz = g.zs[rz];
+                rc.ryf = a.yf[ry];
+                rc.rzf = a.zf[rz];
+                rc.rowmask = __ballot_sync(0xffffffffu, rin);
+                uint32_t m = eval_program_rows<PREC>(P, prog, len, rc, cnt, a.err);
+                if (!xin) m = 0;
+                // Lane x holds bit r of row r; transpose the 32 x 32 bit block so
+                // that lane r holds row r's word (bit x), then store it.
+                m = transpose32(m, lane);
+                if (rin) {
+                    const int y = y0 + lane % a.ty, z = z0 + lane / a.ty;
+                    a.bits[((size_t)z * g.ny + y) * g.W + tx] = m;
+                    const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                    if (m && (edge_row || (m & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
+                }
+                continue;
+            }
+            if (len < 0 && rows <= 32) {
+                const uint32_t word = len == FOLD_TRUE ? __ballot_sync(0xffffffffu, xin) : 0u;
+                const int y = y0 + lane % a.ty, z = z0 + lane / a.ty;
+                if (lane < rows && y < g.ny && z < g.nz) {
+                    a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
+                    const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                    if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
+                }
+                continue;
+            }
+            for (int rr = 0; rr < rows; rr++) {
+                const int y = y0 + rr % a.ty, z = z0 + rr / a.ty;
+                if (y >= g.ny || z >= g.nz) continue;
+                bool b;
+                if (len == FOLD_FALSE) b = false;
+                else if (len == FOLD_TRUE) b = xin;
+                else b = xin && eval_program<PREC>(P, prog, len, P3{px, g.ys[y], g.zs[z]}, F3{pxf, a.yf[y], a.zf[z]},
+                                                   cnt, a.err);
+                const uint32_t word = __ballot_sync(0xffffffffu, b);
+                if (lane == 0) {
+                    a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
+                    // solid is true outside of bounds (mc.go:687-689)
+                    const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                    if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
+                }
             }
         }
-        any = __syncthreads_or(any);
-        if (threadIdx.x == 0) {
-            if (!a.cull) {
-                s_len = P.n_ops;
-                s_prog = P.ops;
-            } else if (!any) {
-                s_len = P.n_ops_allfalse;
-                s_prog = P.ops_allfalse;
-            } else {
-                s_len = fold_program(P.ops, P.n_ops, [&](uint32_t l) { return active[l] != 0; }, q);
-                s_prog = q;
-            }
-        }
-        __syncthreads();
-        const int len = s_len;
-        const uint32_t* prog = s_prog;
-        if (len < 0) nconst++;
-        const int x = x0 + lane;
-        const bool xin = x < g.nx;
-        const int rows = a.ty * a.tz;
-        for (int rr = warp; rr < rows; rr += nwarp) {
-            int y = y0 + rr % a.ty, z = z0 + rr / a.ty;
-            if (y >= g.ny || z >= g.nz) continue;
-            bool b;
-            if (len == FOLD_FALSE) b = false;
-            else if (len == FOLD_TRUE) b = xin;
-            else b = xin && eval_program(P, prog, len, P3{g.xs[x], g.ys[y], g.zs[z]}, a.prec, cnt, a.err);
-            uint32_t word = __ballot_sync(0xffffffffu, b);
-            if (lane == 0) {
-                a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
-                // solid is true outside of bounds (mc.go:687-689)
-                bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
-                uint32_t edge_mask = 0;
-                if (x0 == 0) edge_mask |= 1u;
-                if (g.nx - 1 - x0 < 32) edge_mask |= 1u << (g.nx - 1 - x0);
-                if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
-            }
-        }
-        __syncthreads();
     }
     flush_counts(cnt, a.stats);
-    if (threadIdx.x == 0 && nconst) atomicAdd(&a.stats[ST_TILES_CONST], nconst);
+    if (lane == 0 && nconst) atomicAdd(&a.stats[ST_TILES_CONST], nconst);
 }
 
 // ------------------------------------------------------------ case table
@@ -593,18 +996,29 @@ __device__ __forceinline__ double warp_max(double v) {
     return v;
 }
 
+template <int PREC>
 __global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const size_t per_warp = 4 * (size_t)P.n_ops + (((size_t)P.n_leaves + 15) & ~(size_t)15);
+    const int nw = (P.n_leaves + 31) >> 5;
+    const size_t per_warp = 4 * ((size_t)P.fold_cap + 2 * (size_t)nw);
     uint32_t* q = (uint32_t*)(smem + warp * per_warp);
-    unsigned char* active = smem + warp * per_warp + 4 * (size_t)P.n_ops;
+    uint32_t* cur = q + P.fold_cap;
+    uint32_t* prev = cur + nw;
     Counts cnt;
+    // Each warp takes a contiguous run of 32-vertex batches: neighbouring
+    // vertices share their culled program, so it is folded only on change.
     const long long nwarps_total = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long base = ((long long)blockIdx.x * (blockDim.x >> 5) + warp) * 32; base < a.nverts;
-         base += nwarps_total * 32) {
-        long long v = base + lane;
-        bool live = v < a.nverts;
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    const long long nbatch = (a.nverts + 31) / 32;
+    const long long per = (nbatch + nwarps_total - 1) / nwarps_total;
+    const long long b_begin = gw * per, b_end = min(nbatch, b_begin + per);
+    bool have_prev = false;
+    const uint32_t* prog = P.ops;
+    int len = P.n_ops;
+    for (long long bt = b_begin; bt < b_end; bt++) {
+        const long long v = bt * 32 + lane;
+        const bool live = v < a.nverts;
         int axis = 0;
         double lo = 0, hi = 0;
         P3 cpt{0, 0, 0};
@@ -649,28 +1063,45 @@ __global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchAr
         if (status == 1) atomicOr(&a.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&a.err[ER_EDGE_INDEX], 1);
         const bool work = live && a.iters != 0 && status == 0;
-        // Per-warp culling box: union of the segments this warp bisects.
-        const uint32_t* prog = P.ops;
-        int len = P.n_ops;
         if (a.cull && __any_sync(0xffffffffu, work)) {
-            double blo[3], bhi[3];
+            // Union of the segments this warp bisects, rounded outward to float.
+            float blo[3], bhi[3];
             for (int i = 0; i < 3; i++) {
                 double vlo = work ? comp(cpt, i) : CUDART_INF, vhi = work ? comp(cpt, i) : -CUDART_INF;
                 if (work && i == axis) {
                     vlo = fmin(lo, hi);
                     vhi = fmax(lo, hi);
                 }
-                blo[i] = warp_min(vlo);
-                bhi[i] = warp_max(vhi);
+                blo[i] = __double2float_rd(warp_min(vlo));
+                bhi[i] = __double2float_ru(warp_max(vhi));
             }
-            for (int l = lane; l < P.n_leaves; l += 32) active[l] = (unsigned char)cull_overlap(P.cull + 6 * (size_t)l, blo, bhi);
+            uint32_t diff = 0, any = 0;
+            for (int k = 0; k < nw; k++) {
+                int l = 32 * k + lane;
+                bool on = l < P.n_leaves && cull_overlap_f(P.cull_f + 6 * (size_t)l, blo, bhi);
+                uint32_t w = __ballot_sync(0xffffffffu, on);
+                any |= w;
+                if (lane == 0) {
+                    diff |= (!have_prev || prev[k] != w) ? 1u : 0u;
+                    cur[k] = w;
+                    prev[k] = w;
+                }
+            }
+            diff = __shfl_sync(0xffffffffu, diff, 0);
+            if (diff) {
+                if (!any) {
+                    len = P.n_ops_allfalse;
+                    prog = P.ops_allfalse;
+                } else {
+                    int L = 0;
+                    if (lane == 0)
+                        L = fold_program(P.ops, P.n_ops, cur, q);
+                    len = __shfl_sync(0xffffffffu, L, 0);
+                    prog = q;
+                }
+                have_prev = true;
+            }
             __syncwarp();
-            int L = 0;
-            if (lane == 0) L = fold_program(P.ops, P.n_ops, [&](uint32_t l) { return active[l] != 0; }, q);
-            L = __shfl_sync(0xffffffffu, L, 0);
-            __syncwarp();
-            prog = q;
-            len = L;
         }
         if (live && status == 0) {
             P3 out = cpt;
@@ -679,7 +1110,7 @@ __global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchAr
                 auto contains = [&](P3 pt) -> bool {
                     if (len == FOLD_FALSE) return false;
                     if (len == FOLD_TRUE) return true;
-                    return eval_program(P, prog, len, pt, a.prec, cnt, a.err);
+                    return eval_program<PREC>(P, prog, len, pt, to_f3(pt), cnt, a.err);
                 };
                 double fp = lo, tp = hi;
                 P3 t = cpt;
@@ -709,12 +1140,13 @@ __global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchAr
 
 // ------------------------------------------------------------ k_contains
 
-__global__ void k_contains(ProgView P, const double* pts, long long n, int prec, uint8_t* out, int* err,
+template <int PREC>
+__global__ void k_contains(ProgView P, const double* pts, long long n, uint8_t* out, int* err,
                            unsigned long long* stats) {
     Counts cnt;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         P3 p{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
-        out[i] = eval_program(P, P.ops, P.n_ops, p, prec, cnt, err) ? 1 : 0;
+        out[i] = eval_program<PREC>(P, P.ops, P.n_ops, p, to_f3(p), cnt, err) ? 1 : 0;
     }
     flush_counts(cnt, stats);
 }
@@ -780,7 +1212,7 @@ struct mc_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
     std::string err;
-    DevBuf xs, ys, zs, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
+    DevBuf xs, ys, zs, xf, yf, zf, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
     DevBuf pts, pout;
     unsigned long long* h_pin = nullptr;  // pinned: totals[2], stats[ST_N], errs (as ints) ...
     int64_t last_V = 0, last_T = 0;
@@ -824,6 +1256,18 @@ mc_opts default_opts(const mc_opts* o) {
         r.tile_z = o->tile_z;
     }
     return r;
+}
+
+constexpr int kTileY = 8, kTileZ = 4;  // default corner-tile rows (32 x 8 x 4 corners per warp tile)
+
+size_t search_smem(const ProgView& P) {
+    const size_t nw = ((size_t)P.n_leaves + 31) / 32;
+    return 4 * 4 * ((size_t)P.fold_cap + 2 * nw);
+}
+
+size_t classify_smem(const ProgView& P) {
+    const size_t nw = ((size_t)P.n_leaves + 31) / 32;
+    return 8 * 4 * ((size_t)P.fold_cap + 2 * nw);
 }
 
 bool bounds_valid(const double* mn, const double* mx) {  // BoundsValid, bounder.go:30-46
@@ -885,7 +1329,7 @@ void mc_destroy(mc_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf* b : {&ctx->xs, &ctx->ys, &ctx->zs, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
+    for (DevBuf* b : {&ctx->xs, &ctx->ys, &ctx->zs, &ctx->xf, &ctx->yf, &ctx->zf, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
                       &ctx->prefv, &ctx->preft, &ctx->keys, &ctx->verts, &ctx->tris, &ctx->stats, &ctx->errs,
                       &ctx->totals, &ctx->pts, &ctx->pout})
         b->release();
@@ -931,6 +1375,7 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
         {H.child.data(), H.child.size() * 4, 0},
         {H.tris.data(), H.tris.size() * sizeof(TriD), 0},
         {H.tris_f.data(), H.tris_f.size() * sizeof(TriF), 0},
+        {H.cull_f.data(), H.cull_f.size() * 4, 0},
     };
     size_t total = 0;
     for (auto& p : pcs) {
@@ -960,10 +1405,13 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
     v.child = (const int32_t*)(b + pcs[11].off);
     v.tris = (const TriD*)(b + pcs[12].off);
     v.tris_f = (const TriF*)(b + pcs[13].off);
+    v.cull_f = (const float*)(b + pcs[14].off);
     v.n_ops = (int32_t)H.ops.size();
     v.n_ops_allfalse = H.n_ops_allfalse;
     v.n_leaves = (int32_t)H.leaf_kind.size();
     v.n_xbox = (int32_t)H.xbox.size();
+    v.rows_ok = H.has_transform ? 0 : 1;
+    v.fold_cap = H.fold_cap;
     *out = s.release();
     return MC_OK;
 }
@@ -1039,6 +1487,13 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     CK(cudaMemcpyAsync(ctx->xs.p, X.data(), nx * 8, cudaMemcpyHostToDevice, sm));
     CK(cudaMemcpyAsync(ctx->ys.p, Y.data(), ny * 8, cudaMemcpyHostToDevice, sm));
     CK(cudaMemcpyAsync(ctx->zs.p, Z.data(), nz * 8, cudaMemcpyHostToDevice, sm));
+    std::vector<float> XF(X.begin(), X.end()), YF(Y.begin(), Y.end()), ZF(Z.begin(), Z.end());
+    CK(ctx->xf.ensure(nx * 4));
+    CK(ctx->yf.ensure(ny * 4));
+    CK(ctx->zf.ensure(nz * 4));
+    CK(cudaMemcpyAsync(ctx->xf.p, XF.data(), nx * 4, cudaMemcpyHostToDevice, sm));
+    CK(cudaMemcpyAsync(ctx->yf.p, YF.data(), ny * 4, cudaMemcpyHostToDevice, sm));
+    CK(cudaMemcpyAsync(ctx->zf.p, ZF.data(), nz * 4, cudaMemcpyHostToDevice, sm));
     CK(cudaMemsetAsync(ctx->stats.p, 0, ST_N * 8, sm));
     CK(cudaMemsetAsync(ctx->errs.p, 0, ER_N * 4, sm));
     CK(cudaMemsetAsync(ctx->totals.p, 0, 16, sm));
@@ -1058,17 +1513,25 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     ca.stats = ctx->stats.as<unsigned long long>();
     ca.prec = opts.precision;
     ca.cull = opts.cull;
-    ca.ty = opts.tile_y > 0 ? opts.tile_y : 8;
-    ca.tz = opts.tile_z > 0 ? opts.tile_z : 8;
+    ca.work = (unsigned int*)(ctx->stats.as<unsigned long long>() + ST_WORK);
+    ca.xf = ctx->xf.as<float>();
+    ca.yf = ctx->yf.as<float>();
+    ca.zf = ctx->zf.as<float>();
+    ca.ty = opts.tile_y > 0 ? opts.tile_y : kTileY;
+    ca.tz = opts.tile_z > 0 ? opts.tile_z : kTileZ;
     ca.ntx = (nx + 31) / 32;
     ca.nty = (ny + ca.ty - 1) / ca.ty;
     ca.ntz = (nz + ca.tz - 1) / ca.tz;
     long long ntiles = (long long)ca.ntx * ca.nty * ca.ntz;
     st.tiles = ntiles;
-    size_t smem_c = 4 * (size_t)P.n_ops + (size_t)P.n_leaves + 16;
-    if (smem_c > 48 * 1024) CK(cudaFuncSetAttribute(k_classify, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
-    int grid_c = (int)std::min<long long>(ntiles, (long long)ctx->sm_count * 8);
-    k_classify<<<grid_c, 256, smem_c, sm>>>(g, P, ca);
+    const size_t smem_c = classify_smem(P);
+    auto kc = opts.precision == MC_PREC_FP64 ? k_classify<MC_PREC_FP64> : k_classify<MC_PREC_FP32_FILTERED>;
+    if (smem_c > 48 * 1024) CK(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+    int occ = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kc, 256, smem_c));
+    long long items = (long long)ca.nty * ca.ntz;
+    int grid_c = (int)std::max<long long>(1, std::min<long long>((items + 7) / 8, (long long)ctx->sm_count * std::max(occ, 1)));
+    kc<<<grid_c, 256, smem_c, sm>>>(g, P, ca);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[1], sm));
 
@@ -1124,12 +1587,12 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
         sa.cull = opts.cull;
         sa.err = ctx->errs.as<int>();
         sa.stats = ctx->stats.as<unsigned long long>();
-        size_t per_warp = 4 * (size_t)P.n_ops + (((size_t)P.n_leaves + 15) & ~(size_t)15);
-        size_t smem_s = 4 * per_warp;
+        size_t smem_s = search_smem(P);
+        auto ks = opts.precision == MC_PREC_FP64 ? k_search<MC_PREC_FP64> : k_search<MC_PREC_FP32_FILTERED>;
         if (smem_s > 48 * 1024)
-            CK(cudaFuncSetAttribute(k_search, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s));
+            CK(cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s));
         int grid_s = (int)std::min<long long>((V + 127) / 128, (long long)ctx->sm_count * 16);
-        k_search<<<grid_s, 128, smem_s, sm>>>(g, P, sa);
+        ks<<<grid_s, 128, smem_s, sm>>>(g, P, sa);
         CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ctx->ev[4], sm));
@@ -1230,9 +1693,9 @@ mc_status mc_contains(mc_ctx* ctx, const mc_solid* solid, const double* points, 
     CK(cudaMemsetAsync(ctx->stats.p, 0, ST_N * 8, ctx->stream));
     CK(cudaMemcpyAsync(ctx->pts.p, points, n * 24, cudaMemcpyHostToDevice, ctx->stream));
     int grid = (int)std::min<long long>((n + 255) / 256, (long long)ctx->sm_count * 16);
-    k_contains<<<grid, 256, 0, ctx->stream>>>(solid->view, ctx->pts.as<double>(), n, opts.precision,
-                                              ctx->pout.as<uint8_t>(), ctx->errs.as<int>(),
-                                              ctx->stats.as<unsigned long long>());
+    auto kk = opts.precision == MC_PREC_FP64 ? k_contains<MC_PREC_FP64> : k_contains<MC_PREC_FP32_FILTERED>;
+    kk<<<grid, 256, 0, ctx->stream>>>(solid->view, ctx->pts.as<double>(), n, ctx->pout.as<uint8_t>(),
+                                      ctx->errs.as<int>(), ctx->stats.as<unsigned long long>());
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, ctx->pout.p, n, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_pin + 2, ctx->errs.p, ER_N * 4, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1341,6 +1804,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         spacer_axis(H.root_min[2], H.root_max[2], delta, &Z, kMaxAxis + 1))
         return MC_ERR_GRID;
     const int nx = (int)X.size(), ny = (int)Y.size(), nz = (int)Z.size();
+    std::vector<float> XF(X.begin(), X.end()), YF(Y.begin(), Y.end()), ZF(Z.begin(), Z.end());
 
     // Carve the scratch array; refuse anything that does not fit.
     Carver cv{base};
@@ -1355,7 +1819,9 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         {H.leaf_f.data(), H.leaf_f.size() * 4, nullptr},   {H.cull.data(), H.cull.size() * 8, nullptr},
         {H.xbox.data(), H.xbox.size() * sizeof(XBoxD), nullptr}, {H.xstep.data(), H.xstep.size() * sizeof(XStepD), nullptr},
         {X.data(), X.size() * 8, nullptr},                 {Y.data(), Y.size() * 8, nullptr},
-        {Z.data(), Z.size() * 8, nullptr},
+        {Z.data(), Z.size() * 8, nullptr},                 {H.cull_f.data(), H.cull_f.size() * 4, nullptr},
+        {XF.data(), XF.size() * 4, nullptr},               {YF.data(), YF.size() * 4, nullptr},
+        {ZF.data(), ZF.size() * 4, nullptr},
     };
     for (auto& p : up) p.dst = cv.take(p.bytes);
     int* errs = (int*)cv.take(ER_N * 4);
@@ -1405,10 +1871,13 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     P.cull = (const double*)up[5].dst;
     P.xbox = (const XBoxD*)up[6].dst;
     P.xstep = (const XStepD*)up[7].dst;
+    P.cull_f = (const float*)up[11].dst;
     P.n_ops = (int32_t)H.ops.size();
     P.n_ops_allfalse = H.n_ops_allfalse;
     P.n_leaves = (int32_t)H.leaf_kind.size();
     P.n_xbox = (int32_t)H.xbox.size();
+    P.rows_ok = H.has_transform ? 0 : 1;
+    P.fold_cap = H.fold_cap;
 
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1418,15 +1887,21 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     ca.stats = stats;
     ca.prec = opts.precision;
     ca.cull = opts.cull;
-    ca.ty = opts.tile_y > 0 ? opts.tile_y : 8;
-    ca.tz = opts.tile_z > 0 ? opts.tile_z : 8;
+    ca.work = (unsigned int*)(stats + ST_WORK);
+    ca.xf = (const float*)up[12].dst;
+    ca.yf = (const float*)up[13].dst;
+    ca.zf = (const float*)up[14].dst;
+    ca.ty = opts.tile_y > 0 ? opts.tile_y : kTileY;
+    ca.tz = opts.tile_z > 0 ? opts.tile_z : kTileZ;
     ca.ntx = (nx + 31) / 32;
     ca.nty = (ny + ca.ty - 1) / ca.ty;
     ca.ntz = (nz + ca.tz - 1) / ca.tz;
-    long long ntiles = (long long)ca.ntx * ca.nty * ca.ntz;
-    size_t smem_c = 4 * (size_t)P.n_ops + (size_t)P.n_leaves + 16;
+    const size_t smem_c = classify_smem(P);
     if (smem_c > 48 * 1024) return MC_ERR_LIMIT;
-    k_classify<<<(int)std::min<long long>(ntiles, (long long)sms * 8), 256, smem_c, sm>>>(g, P, ca);
+    long long items = (long long)ca.nty * ca.ntz;
+    auto kc = opts.precision == MC_PREC_FP64 ? k_classify<MC_PREC_FP64> : k_classify<MC_PREC_FP32_FILTERED>;
+    kc<<<(int)std::max<long long>(1, std::min<long long>((items + 7) / 8, (long long)sms * 4)), 256, smem_c, sm>>>(
+        g, P, ca);
     if (nchunks > 0) {
         k_count<<<nblk, 256, 0, sm>>>(g, CountArgs{bits, packed, blocksum, nchunks});
         k_scan_blocks<<<1, 1024, 0, sm>>>(blocksum, blockoff, nblk, totals);
@@ -1460,9 +1935,9 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         sa.cull = opts.cull;
         sa.err = errs;
         sa.stats = stats;
-        size_t per_warp = 4 * (size_t)P.n_ops + (((size_t)P.n_leaves + 15) & ~(size_t)15);
-        if (4 * per_warp > 48 * 1024) return MC_ERR_LIMIT;
-        k_search<<<(int)std::min<long long>((V + 127) / 128, (long long)sms * 16), 128, 4 * per_warp, sm>>>(g, P, sa);
+        if (search_smem(P) > 48 * 1024) return MC_ERR_LIMIT;
+        auto ks = opts.precision == MC_PREC_FP64 ? k_search<MC_PREC_FP64> : k_search<MC_PREC_FP32_FILTERED>;
+        ks<<<(int)std::min<long long>((V + 127) / 128, (long long)sms * 16), 128, search_smem(P), sm>>>(g, P, sa);
     }
     if (cudaGetLastError() != cudaSuccess) return MC_ERR_CUDA;
     if (cudaMemcpyAsync(h + 2, errs, ER_N * 4, cudaMemcpyDeviceToHost, sm) != cudaSuccess ||

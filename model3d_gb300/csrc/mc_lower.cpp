@@ -268,6 +268,13 @@ struct Lowerer {
         if ((int)P->ops.size() >= MAX_OPS) throw LowerError(MC_ERR_LIMIT, "program too long");
         P->ops.push_back(op);
     }
+    void leaf_out(int id) {
+        last_leaf = id;
+        if (emit_leaves) {
+            emit(make_op(OP_LEAF, id));
+            push_bool();
+        }
+    }
     void push_bool() {
         depth++;
         P->max_stack = std::max(P->max_stack, depth);
@@ -282,7 +289,10 @@ struct Lowerer {
         P->leaf_f.resize(bf + LEAF_F, 0.0f);
         for (int i = 0; i < nd; i++) P->leaf_d[bd + i] = d[i];
         for (int i = 0; i < nf; i++) P->leaf_f[bf + i] = f[i];
-        for (int i = 0; i < 6; i++) P->cull.push_back(cull[i]);
+        for (int i = 0; i < 6; i++) {
+            P->cull.push_back(cull[i]);
+            P->cull_f.push_back(i < 3 ? f_down(cull[i]) : f_up(cull[i]));
+        }
         return id;
     }
 
@@ -386,6 +396,21 @@ struct Lowerer {
 
     // Lower one node (and its subtree); outer = index of the outermost
     // enclosing TRANSFORM box (-1 if none) for culling.
+    // End (exclusive) of the serialised subtree starting at record p.
+    size_t subtree_end(size_t p) {
+        if (p >= n) fail("truncated node array");
+        const mc_node& nd = nodes[p];
+        size_t q = p + 1 + (nd.kind == MC_NODE_TRANSFORM ? (size_t)std::max(0, nd.n_steps) : 0);
+        int nc = (nd.kind >= MC_NODE_JOIN && nd.kind <= MC_NODE_CHECKED) ? nd.n_children : 0;
+        if (nc < 0) fail("negative child count");
+        for (int i = 0; i < nc; i++) q = subtree_end(q);
+        return q;
+    }
+    static bool is_leaf_kind(int k) { return k >= MC_NODE_SPHERE && k <= MC_NODE_COLLIDER; }
+
+    int last_leaf = -1;
+    bool emit_leaves = true;
+
     void lower(int outer) {
         if (pos >= n) fail("truncated node array");
         const mc_node& nd = nodes[pos++];
@@ -414,8 +439,7 @@ struct Lowerer {
                 set_cull(vsub(c, d3(R, R, R)), vadd(c, d3(R, R, R)));
                 if (!(R >= 0)) for (double& x : cull) x = 0;  // contains nothing: any box
                 int id = add_leaf(LK_SPHERE, d, 4, f, 6, cull);
-                emit(make_op(OP_LEAF, id));
-                push_bool();
+                leaf_out(id);
                 return;
             }
             case MC_NODE_RECT: {  // shapes.go:171-173
@@ -425,8 +449,7 @@ struct Lowerer {
                 for (int i = 0; i < 6; i++) f[i] = (float)d[i];
                 set_cull(lo, hi);
                 int id = add_leaf(LK_RECT, d, 6, f, 6, cull);
-                emit(make_op(OP_LEAF, id));
-                push_bool();
+                leaf_out(id);
                 return;
             }
             case MC_NODE_CYLINDER: {  // shapes.go:588-598
@@ -442,8 +465,7 @@ struct Lowerer {
                                f_down(TR), f_up(TR), 0, 0};
                 set_cull(vsub(vmin3(p1, p2), d3(R, R, R)), vadd(vmax3(p1, p2), d3(R, R, R)));
                 int id = add_leaf(LK_CYLINDER, d, 8, f, 12, cull);
-                emit(make_op(OP_LEAF, id));
-                push_bool();
+                leaf_out(id);
                 return;
             }
             case MC_NODE_CAPSULE: {  // shapes.go:365-368, primitives.go:547-594
@@ -467,8 +489,7 @@ struct Lowerer {
                 f[13] = f[14] = 0;
                 set_cull(vsub(vmin3(p1, p2), d3(R, R, R)), vadd(vmax3(p1, p2), d3(R, R, R)));
                 int id = add_leaf(LK_CAPSULE, d, 11, f, 15, cull);
-                emit(make_op(OP_LEAF, id));
-                push_bool();
+                leaf_out(id);
                 return;
             }
             case MC_NODE_TORUS: {  // shapes.go:1363-1365, :1451-1487
@@ -484,8 +505,7 @@ struct Lowerer {
                 double ext = std::fabs(outer_r) + std::fabs(inner);
                 set_cull(vsub(c, d3(ext, ext, ext)), vadd(c, d3(ext, ext, ext)));
                 int id = add_leaf(LK_TORUS, d, 11, f, 11, cull);
-                emit(make_op(OP_LEAF, id));
-                push_bool();
+                leaf_out(id);
                 return;
             }
             case MC_NODE_COLLIDER: {  // solid.go:292-305
@@ -496,20 +516,52 @@ struct Lowerer {
                 set_cull(d3(nd.min[0], nd.min[1], nd.min[2]), d3(nd.max[0], nd.max[1], nd.max[2]));
                 int id = add_leaf(LK_COLLIDER, d, 7, f, 1, cull);
                 P->has_collider = true;
-                emit(make_op(OP_LEAF, id));
-                push_bool();
+                leaf_out(id);
                 return;
             }
             case MC_NODE_JOIN:
             case MC_NODE_INTERSECT: {  // solid.go:89-98, :165-172
                 if (nd.n_children < 1) fail("JoinedSolid/IntersectedSolid without children");
-                uint32_t op = nd.kind == MC_NODE_JOIN ? OP_OR : OP_AND;
-                lower(outer);
-                for (int i = 1; i < nd.n_children; i++) {
-                    lower(outer);
-                    emit(make_op(op, 0));
-                    depth--;
+                // OR / AND are commutative: the leaf children get consecutive
+                // ids and one range op, then the other children follow.
+                const uint32_t op = nd.kind == MC_NODE_JOIN ? OP_OR : OP_AND;
+                const uint32_t rop = nd.kind == MC_NODE_JOIN ? OP_JLEAVES : OP_ALEAVES;
+                std::vector<size_t> starts;
+                size_t q = pos;
+                for (int i = 0; i < nd.n_children; i++) {
+                    starts.push_back(q);
+                    q = subtree_end(q);
                 }
+                const size_t end = q;
+                int first = -1, count = 0, have = 0;
+                for (size_t st : starts) {
+                    if (!is_leaf_kind(nodes[st].kind)) continue;
+                    pos = st;
+                    bool saved = emit_leaves;
+                    emit_leaves = false;
+                    lower(outer);
+                    emit_leaves = saved;
+                    if (first < 0) first = last_leaf;
+                    count++;
+                }
+                if (count > 0) {
+                    if (first >= (1 << 14) || count >= (1 << 14))
+                        throw LowerError(MC_ERR_LIMIT, "more than 16383 leaves");
+                    emit(make_op(rop, ((uint32_t)first << 14) | (uint32_t)count));
+                    push_bool();
+                    have = 1;
+                }
+                for (size_t st : starts) {
+                    if (is_leaf_kind(nodes[st].kind)) continue;
+                    pos = st;
+                    lower(outer);
+                    if (have) {
+                        emit(make_op(op, 0));
+                        depth--;
+                    }
+                    have = 1;
+                }
+                pos = end;
                 return;
             }
             case MC_NODE_SUBTRACT: {  // solid.go:138-141
@@ -552,6 +604,7 @@ struct Lowerer {
                 for (int i = (int)fwd.size() - 1; i >= 0; i--) P->xstep.push_back(fwd[i]);
                 int id = (int)P->xbox.size();
                 P->xbox.push_back(xb);
+                P->has_transform = true;
                 emit(make_op(OP_XPUSH, id));
                 if (++xdepth > MAX_XDEPTH) throw LowerError(MC_ERR_LIMIT, "transforms nested too deeply");
                 P->max_xdepth = std::max(P->max_xdepth, xdepth);
@@ -594,8 +647,12 @@ void lower_scene(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets, s
         P->root_max[i] = nodes[0].max[i];
     }
     P->ops_allfalse.resize(P->ops.size() + 1);
-    P->n_ops_allfalse = fold_program(P->ops.data(), (int)P->ops.size(), [](uint32_t) { return false; },
-                                     P->ops_allfalse.data());
+    P->n_ops_allfalse = fold_program(P->ops.data(), (int)P->ops.size(), nullptr, P->ops_allfalse.data());
+    P->fold_cap = 0;
+    for (uint32_t op : P->ops) {
+        uint32_t c = op_code(op);
+        P->fold_cap += (c == OP_JLEAVES || c == OP_ALEAVES) ? 1 + (int)range_count(op_arg(op)) : 1;
+    }
 }
 
 // ---------------------------------------------------------------- spacer

@@ -20,10 +20,12 @@ struct LowerError : std::runtime_error {
 struct HostProgram {
     std::vector<uint32_t> ops, ops_allfalse;
     int n_ops_allfalse = FOLD_FALSE;
+    int fold_cap = 0;
     std::vector<int32_t> leaf_kind;
     std::vector<double> leaf_d;
     std::vector<float> leaf_f;
     std::vector<double> cull;
+    std::vector<float> cull_f;
     std::vector<XBoxD> xbox;
     std::vector<XStepD> xstep;
     std::vector<TreeD> trees;
@@ -35,6 +37,7 @@ struct HostProgram {
     double root_min[3] = {0, 0, 0}, root_max[3] = {0, 0, 0};
     int max_stack = 0, max_xdepth = 0;
     bool has_collider = false;
+    bool has_transform = false;
 };
 
 // Throws LowerError.
