@@ -714,7 +714,7 @@ __global__ void __launch_bounds__(256, 3) k_classify(GridView g, ProgView P, Cla
 
 struct CaseTable {
     uint8_t count[256];
-    uint8_t edge[256][15];  // per triangle vertex: axis << 3 | min-corner index
+    uint8_t edge[256][15];  // per triangle vertex: cube edge 0..11 (x: dy+2dz, y: 4+dx+2dz, z: 8+dx+2dy)
 };
 __constant__ CaseTable c_table;
 
@@ -927,10 +927,35 @@ __global__ void __launch_bounds__(256) k_emit(GridView g, EmitArgs a) {
     }
     uint32_t nt = pk >> 18;
     if (nt == 0) return;
-    // Edge masks of the neighbouring rows (same word c) for rank queries.
-    // x-edges of rows k=(dy,dz): cp[2k] ^ cp[2k+1]; y-edges of rows (y, z+dz):
-    // r(y,z+dz) ^ r(y+1,z+dz); z-edges of rows (y+dy, z): r(y+dy,z) ^ r(y+dy,z+1).
+    // Vertex id bases (x, y, z edges) of the chunks this chunk's cubes touch:
+    // rows (y+dy, z+dz) at word c, and rows (y, z+dz) / (y+dy, z) at word c+1.
+    // A crossed edge never has its base corner on the last grid plane, so
+    // only the chunks inside the cube index space are read.
     const long long rowC = (long long)(g.ny - 1);
+    auto base = [&](int dy, int dz, int w, uint32_t* bx, uint32_t* by, uint32_t* bz) {
+        *bx = *by = *bz = 0;
+        if (y + dy > g.ny - 2 || z + dz > g.nz - 2 || c + w >= g.CX) return;
+        const long long ci = ((long long)(z + dz) * rowC + (y + dy)) * g.CX + c + w;
+        const uint32_t pv = a.prefv[ci], pn = a.packed[ci];
+        *bx = pv;
+        *by = pv + (pn & 63u);
+        *bz = *by + ((pn >> 6) & 63u);
+    };
+    uint32_t bx[4], byc[2], byn[2], bzc[2], bzn[2], t0, t1;
+    base(0, 0, 0, &bx[0], &byc[0], &bzc[0]);
+    base(1, 0, 0, &bx[1], &t0, &bzc[1]);
+    base(0, 1, 0, &bx[2], &byc[1], &t1);
+    base(1, 1, 0, &bx[3], &t0, &t1);
+    base(0, 0, 1, &t0, &byn[0], &bzn[0]);
+    base(0, 1, 1, &t0, &byn[1], &t1);
+    base(1, 0, 1, &t0, &t1, &bzn[1]);
+    uint32_t xm[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) xm[k] = (cp[2 * k] ^ cp[2 * k + 1]) & vm;
+    const uint32_t ym[2] = {R.r[0] ^ R.r[1], R.r[2] ^ R.r[3]};  // rows (y, z), (y, z+1)
+    const uint32_t zm[2] = {R.r[0] ^ R.r[2], R.r[1] ^ R.r[3]};  // rows (y, z), (y+1, z)
+    __shared__ uint32_t s_eid[256][13];
+    uint32_t* eid = s_eid[threadIdx.x];
     uint32_t t_out = a.preft[i];
     uint32_t all = cp[0], anyb = cp[0];
 #pragma unroll
@@ -940,43 +965,34 @@ __global__ void __launch_bounds__(256) k_emit(GridView g, EmitArgs a) {
     }
     uint32_t act = anyb & ~all & vm;
     while (act) {
-        int b = __ffs(act) - 1;
+        const int b = __ffs(act) - 1;
         act &= act - 1;
-        int kc = cube_case(cp, b);
-        int ntri = c_table.count[kc];
-        for (int e = 0; e < 3 * ntri; e++) {
-            int code = c_table.edge[kc][e];
-            int ax = code >> 3, corner = code & 7;
-            int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
-            int bb = b + dx, cc = c;
-            if (bb == 32) {
-                bb = 0;
-                cc = c + 1;
-            }
-            long long ci = ((long long)(z + dz) * rowC + (y + dy)) * g.CX + cc;
-            uint32_t mask;
-            if (ax == 0) {
-                int k = dy + 2 * dz;
-                mask = (cp[2 * k] ^ cp[2 * k + 1]) & vm;
-            } else if (ax == 1) {
-                mask = dz ? (R.r[2] ^ R.r[3]) : (R.r[0] ^ R.r[1]);
-            } else {
-                mask = dy ? (R.r[1] ^ R.r[3]) : (R.r[0] ^ R.r[2]);
-            }
-            uint32_t rank = bb ? __popc(mask & ((1u << bb) - 1u)) : 0u;
-            uint32_t pn = a.packed[ci];
-            uint32_t id = a.prefv[ci] + rank;
-            if (ax >= 1) id += pn & 63u;
-            if (ax == 2) id += (pn >> 6) & 63u;
-            a.tris[3 * (size_t)t_out + (e % 3)] = (int32_t)id;
-            if (e % 3 == 2) t_out++;
+        const uint32_t below = (1u << b) - 1u;            // bits < b
+        const uint32_t below1 = b < 31 ? (2u << b) - 1u : ~0u;  // bits < b + 1
+#pragma unroll
+        for (int k = 0; k < 4; k++) eid[k] = bx[k] + __popc(xm[k] & below);
+#pragma unroll
+        for (int dz = 0; dz < 2; dz++) {
+            eid[4 + 2 * dz] = byc[dz] + __popc(ym[dz] & below);
+            eid[5 + 2 * dz] = b < 31 ? byc[dz] + __popc(ym[dz] & below1) : byn[dz];
         }
+#pragma unroll
+        for (int dy = 0; dy < 2; dy++) {
+            eid[8 + 2 * dy] = bzc[dy] + __popc(zm[dy] & below);
+            eid[9 + 2 * dy] = b < 31 ? bzc[dy] + __popc(zm[dy] & below1) : bzn[dy];
+        }
+        const int kc = cube_case(cp, b);
+        const int n3 = 3 * c_table.count[kc];
+        int32_t* out = a.tris + 3 * (size_t)t_out;
+        for (int e = 0; e < n3; e++) out[e] = (int32_t)eid[c_table.edge[kc][e]];
+        t_out += n3 / 3;
     }
 }
 
 // ------------------------------------------------------------ k_search
 
 struct SearchArgs {
+    double inv_dl;  // 1 / (xs[1] - xs[0])
     const unsigned long long* keys;
     double* verts;  // V x 3
     long long nverts;
@@ -994,6 +1010,52 @@ __device__ __forceinline__ double warp_min(double v) {
 __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
+}
+
+// LookupEdgePoint (mc.go:647-660): the first axis i whose |fmod(c_i - o_i,
+// dl)| lies in (dl/4, 3dl/4), with idx = int((c_i - o_i) / dl).  Both the
+// band test and the truncation are decided from q = (c_i - o_i) * (1/dl)
+// when its fractional part is more than 1e-7 from the band edges: for
+// 0 <= q < 2^24 the error of q is below 3 * 2^-53 * 2^24 < 1e-8, and inside
+// the band the exact quotient is at least 1/4 from an integer, so the
+// correctly rounded quotient truncates to floor(q).  Otherwise the
+// reference's exact fmod and IEEE division decide.
+// Returns 0 (found), 1 ("vertex not on edge") or 2 (index out of range).
+__device__ __forceinline__ int lookup_edge(const GridView& g, const P3& c, double inv_dl, int* axis, double* lo,
+                                           double* hi) {
+    const double org[3] = {g.xs[0], g.ys[0], g.zs[0]};
+    const double* vals[3] = {g.xs, g.ys, g.zs};
+    const int nvals[3] = {g.nx, g.ny, g.nz};
+    const double dl = D_SUB(g.xs[1], g.xs[0]);
+    for (int i = 0; i < 3; i++) {
+        const double av = D_SUB(comp(c, i), org[i]);
+        const double q = D_MUL(av, inv_dl);
+        int band = -1;  // -1 undecided, 0 outside, 1 inside
+        long long idx = 0;
+        if (av >= 0 && q < 16777216.0) {
+            const double n = floor(q);
+            const double fr = D_SUB(q, n);
+            if (fr > 0.2500001 && fr < 0.7499999) {
+                band = 1;
+                idx = (long long)n;
+            } else if (fr < 0.2499999 || fr > 0.7500001) {
+                band = 0;
+            }
+        }
+        if (band < 0) {
+            const double m = fabs(fmod(av, dl));
+            band = (m > D_DIV(dl, 4.0) && m < D_DIV(D_MUL(3.0, dl), 4.0)) ? 1 : 0;
+            if (band) idx = __double2ll_rz(D_DIV(av, dl));
+        }
+        if (band) {
+            if (idx < 0 || idx + 1 >= nvals[i]) return 2;
+            *axis = i;
+            *lo = vals[i][idx];
+            *hi = vals[i][idx + 1];
+            return 0;
+        }
+    }
+    return 1;
 }
 
 template <int PREC>
@@ -1034,31 +1096,7 @@ __global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchAr
             else c1.z = g.zs[z + 1];
             // corners[a].Mid(corners[b]) (mc.go:401-407, coords.go:196-198)
             cpt = P3{D_MUL(D_ADD(c0.x, c1.x), 0.5), D_MUL(D_ADD(c0.y, c1.y), 0.5), D_MUL(D_ADD(c0.z, c1.z), 0.5)};
-            if (a.iters != 0) {
-                // LookupEdgePoint (mc.go:647-660)
-                const double org[3] = {g.xs[0], g.ys[0], g.zs[0]};
-                const double* vals[3] = {g.xs, g.ys, g.zs};
-                const int nvals[3] = {g.nx, g.ny, g.nz};
-                double dl = D_SUB(g.xs[1], g.xs[0]);
-                double q1 = D_DIV(dl, 4.0), q3 = D_DIV(D_MUL(3.0, dl), 4.0);
-                axis = -1;
-                for (int i = 0; i < 3; i++) {
-                    double ci = comp(cpt, i);
-                    double m = fabs(fmod(D_SUB(ci, org[i]), dl));
-                    if (m > q1 && m < q3) {
-                        long long idx = __double2ll_rz(D_DIV(D_SUB(ci, org[i]), dl));
-                        if (idx < 0 || idx + 1 >= nvals[i]) {
-                            status = 2;
-                        } else {
-                            axis = i;
-                            lo = vals[i][idx];
-                            hi = vals[i][idx + 1];
-                        }
-                        break;
-                    }
-                }
-                if (axis < 0 && status == 0) status = 1;
-            }
+            if (a.iters != 0) status = lookup_edge(g, cpt, a.inv_dl, &axis, &lo, &hi);
         }
         if (status == 1) atomicOr(&a.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&a.err[ER_EDGE_INDEX], 1);
@@ -1106,16 +1144,21 @@ __global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchAr
         if (live && status == 0) {
             P3 out = cpt;
             if (work) {
-                // mcSearchPoint (mc.go:223-258)
-                auto contains = [&](P3 pt) -> bool {
+                // mcSearchPoint (mc.go:223-258); only the axis coordinate moves.
+                F3 pf = to_f3(cpt);
+                auto contains = [&](P3 pt, double v) -> bool {
                     if (len == FOLD_FALSE) return false;
                     if (len == FOLD_TRUE) return true;
-                    return eval_program<PREC>(P, prog, len, pt, to_f3(pt), cnt, a.err);
+                    const float vf = (float)v;
+                    if (axis == 0) pf.x = vf;
+                    else if (axis == 1) pf.y = vf;
+                    else pf.z = vf;
+                    return eval_program<PREC>(P, prog, len, pt, pf, cnt, a.err);
                 };
                 double fp = lo, tp = hi;
                 P3 t = cpt;
                 set_comp(t, axis, tp);
-                if (!contains(t)) {
+                if (!contains(t, tp)) {
                     fp = hi;
                     tp = lo;
                 }
@@ -1123,7 +1166,7 @@ __global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchAr
                 for (int k = 0; k < a.iters; k++) {
                     double mid = D_DIV(D_ADD(fp, tp), 2.0);
                     set_comp(arr, axis, mid);
-                    if (contains(arr)) tp = mid;
+                    if (contains(arr, mid)) tp = mid;
                     else fp = mid;
                 }
                 set_comp(arr, axis, D_DIV(D_ADD(fp, tp), 2.0));
@@ -1198,9 +1241,10 @@ void build_table_host() {
             for (int k = 0; k < 3; k++) {
                 int a = tris[c][t][2 * k], b = tris[c][t][2 * k + 1];
                 int diff = a ^ b;
-                int axis = diff == 1 ? 0 : (diff == 2 ? 1 : 2);
                 int lo = a < b ? a : b;
-                g_table_host.edge[c][3 * t + k] = (uint8_t)((axis << 3) | lo);
+                int dx = lo & 1, dy = (lo >> 1) & 1, dz = lo >> 2;
+                int e = diff == 1 ? (dy + 2 * dz) : (diff == 2 ? 4 + dx + 2 * dz : 8 + dx + 2 * dy);
+                g_table_host.edge[c][3 * t + k] = (uint8_t)e;
             }
     }
 }
@@ -1579,6 +1623,7 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     CK(cudaEventRecord(ctx->ev[3], sm));
     if (V > 0) {
         SearchArgs sa{};
+        sa.inv_dl = nx >= 2 ? 1.0 / (X[1] - X[0]) : 0.0;
         sa.keys = ctx->keys.as<unsigned long long>();
         sa.verts = ctx->verts.as<double>();
         sa.nverts = V;
@@ -1927,6 +1972,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     }
     if (V > 0) {
         SearchArgs sa{};
+        sa.inv_dl = nx >= 2 ? 1.0 / (X[1] - X[0]) : 0.0;
         sa.keys = (const unsigned long long*)keys_base;
         sa.verts = vertices;
         sa.nverts = V;
