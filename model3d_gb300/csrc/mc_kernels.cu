@@ -1044,7 +1044,7 @@ __device__ __forceinline__ int lookup_edge(const GridView& g, const P3& c, doubl
         }
         if (band < 0) {
             const double m = fabs(fmod(av, dl));
-            band = (m > D_DIV(dl, 4.0) && m < D_DIV(D_MUL(3.0, dl), 4.0)) ? 1 : 0;
+            band = (m > D_MUL(dl, 0.25) && m < D_MUL(D_MUL(3.0, dl), 0.25)) ? 1 : 0;  // delta/4, 3*delta/4
             if (band) idx = __double2ll_rz(D_DIV(av, dl));
         }
         if (band) {
@@ -1059,7 +1059,7 @@ __device__ __forceinline__ int lookup_edge(const GridView& g, const P3& c, doubl
 }
 
 template <int PREC>
-__global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchArgs a) {
+__global__ void __launch_bounds__(128, 4) k_search(GridView g, ProgView P, SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (P.n_leaves + 31) >> 5;
@@ -1164,12 +1164,12 @@ __global__ void __launch_bounds__(128) k_search(GridView g, ProgView P, SearchAr
                 }
                 P3 arr = cpt;
                 for (int k = 0; k < a.iters; k++) {
-                    double mid = D_DIV(D_ADD(fp, tp), 2.0);
+                    double mid = D_MUL(D_ADD(fp, tp), 0.5);  // x / 2 and x * 0.5 round the same real
                     set_comp(arr, axis, mid);
                     if (contains(arr, mid)) tp = mid;
                     else fp = mid;
                 }
-                set_comp(arr, axis, D_DIV(D_ADD(fp, tp), 2.0));
+                set_comp(arr, axis, D_MUL(D_ADD(fp, tp), 0.5));
                 out = arr;
             }
             a.verts[3 * v] = out.x;
