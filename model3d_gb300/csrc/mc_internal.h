@@ -123,6 +123,8 @@ struct TriF {
 struct TreeD {
     int32_t kind;  // 0: no triangles (nullCollider); 1: root is a node; 2: root is one triangle
     int32_t root;  // node or triangle index (absolute)
+    float mbox[3]; // per axis, an upper bound of |coordinate| over every box of the tree
+    int32_t pad;
 };
 
 // Device view of one lowered solid (passed by value to kernels).

@@ -58,47 +58,60 @@ __device__ __forceinline__ void flush_counts(const Counts& c, unsigned long long
 // ------------------------------------------------------------ colliders
 
 // ColliderSolid.Contains (solid.go:292-305): InBounds, then ray parity over
-// the flattened JoinedCollider tree (collisions.go:119-134, :263-273).
-__device__ int collider_64(const ProgView& P, const double* d, P3 p, Counts& cnt, int* err) {
-    if (!(p.x >= d[0] && p.y >= d[1] && p.z >= d[2] && p.x <= d[3] && p.y <= d[4] && p.z <= d[5]))
-        return 0;
+// the flattened JoinedCollider tree (collisions.go:119-134, :263-273).  With
+// `filt` every box and triangle test runs in FP32 first (ray_box_32,
+// ray_tri_32) and falls back to the float64 test when undecided.
+__device__ __noinline__ bool collider_point(const ProgView& P, const double* d, P3 p, F3 pf, bool filt, Counts& cnt,
+                                            int* err) {
+    if (!(p.x >= d[0] && p.y >= d[1] && p.z >= d[2] && p.x <= d[3] && p.y <= d[4] && p.z <= d[5])) return false;
     const TreeD t = P.trees[(int)d[6]];
-    if (t.kind == 0) return 0;
-    if (t.kind == 2) {
+    if (t.kind == 0) return false;
+    auto tri_hit = [&](int i) -> int {
         cnt.tris++;
-        return ray_tri_64(P.tris[t.root], p) & 1;
-    }
+        if (filt) {
+            int v = ray_tri_32(P.tris_f[i], pf);
+            if (v != 2) return v;
+            cnt.esc++;
+        }
+        return ray_tri_64(P.tris[i], p);
+    };
+    if (t.kind == 2) return tri_hit(t.root) & 1;
+    RayF rf;
+    if (filt) rf = make_rayf(pf, t.mbox);
+    auto box_hit = [&](int c) -> bool {
+        cnt.nodes++;
+        if (filt) {
+            int v = ray_box_32(P.nodes_f[c], rf);
+            if (v != 2) return v == 1;
+            cnt.esc++;
+        }
+        return ray_box_64(P.nodes[c].lo, P.nodes[c].hi, p);
+    };
     // Depth-first over child ranges; the hit count is a sum, so order is free.
     int stk_i[MAX_BVH_DEPTH], stk_e[MAX_BVH_DEPTH];
     int sp = 0, hits = 0;
-    {
-        const BvhNodeD& n = P.nodes[t.root];
-        cnt.nodes++;
-        if (!ray_box_64(n.lo, n.hi, p)) return 0;
-        stk_i[0] = n.first;
-        stk_e[0] = n.first + n.count;
-        sp = 1;
-    }
+    if (!box_hit(t.root)) return false;
+    stk_i[0] = P.nodes[t.root].first;
+    stk_e[0] = stk_i[0] + P.nodes[t.root].count;
+    sp = 1;
     while (sp > 0) {
-        int i = stk_i[sp - 1];
+        const int i = stk_i[sp - 1];
         if (i >= stk_e[sp - 1]) {
             sp--;
             continue;
         }
         stk_i[sp - 1] = i + 1;
-        int c = P.child[i];
+        const int c = P.child[i];
         if (c < 0) {
-            cnt.tris++;
-            hits += ray_tri_64(P.tris[-c - 1], p);
+            hits += tri_hit(-c - 1);
             continue;
         }
-        const BvhNodeD& n = P.nodes[c];
-        cnt.nodes++;
-        if (!ray_box_64(n.lo, n.hi, p)) continue;
+        if (!box_hit(c)) continue;
         if (sp == MAX_BVH_DEPTH) {
             atomicOr(&err[ER_LIMIT], 1);
-            return 0;
+            return false;
         }
+        const BvhNodeF& n = P.nodes_f[c];
         stk_i[sp] = n.first;
         stk_e[sp] = n.first + n.count;
         sp++;
@@ -142,7 +155,7 @@ __device__ __noinline__ bool leaf64_point(const ProgView& P, int id, P3 p, Count
         case LK_CYLINDER: return cylinder_64(d, p);
         case LK_CAPSULE: return capsule_64(d, p);
         case LK_TORUS: return torus_64(d, p);
-        default: return collider_64(P, d, p, cnt, err);
+        default: return collider_point(P, d, p, to_f3(p), false, cnt, err);
     }
 }
 
@@ -162,6 +175,8 @@ __device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf
             }
             if (r != 2) return r;
             cnt.esc++;
+        } else if (kind == LK_COLLIDER) {
+            return collider_point(P, P.leaf_d + (size_t)id * LEAF_D, p, pf, true, cnt, err);
         }
     }
     return leaf64_point(P, id, p, cnt, err);
@@ -467,9 +482,15 @@ __device__ __forceinline__ uint32_t leaf_rows(const ProgView& P, int id, const R
         case LK_SPHERE: return f32 ? sphere_rows32(f, d, rc, cnt) : sphere_rows64(d, rc);
         case LK_CYLINDER: return f32 ? cylinder_rows32(f, d, rc, cnt) : cylinder_rows64(d, rc);
         case LK_CAPSULE: return f32 ? capsule_rows32(f, d, rc, cnt) : capsule_rows64(d, rc);
-        default: {  // torus, collider: point by point in float64
+        default: {  // torus, collider: point by point
             uint32_t m = 0;
-            for (int r = 0; r < rc.nrows; r++) m |= (leaf64_point(P, id, row_point(rc, r), cnt, err) ? 1u : 0u) << r;
+            for (int r = 0; r < rc.nrows; r++) {
+                const F3 pf{rc.pxf, shf(rc.ryf, r), shf(rc.rzf, r)};
+                const P3 p = row_point(rc, r);
+                bool v = (f32 && kind == LK_COLLIDER) ? collider_point(P, d, p, pf, true, cnt, err)
+                                                      : leaf64_point(P, id, p, cnt, err);
+                m |= (v ? 1u : 0u) << r;
+            }
             return m;
         }
     }

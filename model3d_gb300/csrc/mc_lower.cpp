@@ -315,7 +315,7 @@ struct Lowerer {
         } else {
             order = group_triangles(t);
         }
-        TreeD tree{0, 0};
+        TreeD tree{};
         int tri_base = (int)P->tris.size();
         // Triangle records in grouped order (traversal locality).
         std::vector<int> pos_of(ts.n);
@@ -351,7 +351,8 @@ struct Lowerer {
             P->tris_f.push_back(f);
         }
         if (ts.n == 1) {
-            tree = {2, tri_base};
+            tree.kind = 2;
+            tree.root = tri_base;
         } else if (ts.n > 1) {
             TreeBuilder tb{t, {}};
             int root = tb.build(order.data(), order.size());
@@ -386,7 +387,15 @@ struct Lowerer {
                 P->nodes[node_base + qi] = nd;
                 P->nodes_f[node_base + qi] = nf;
             }
-            tree = {1, node_base};
+            tree.kind = 1;
+            tree.root = node_base;
+        }
+        // Coordinate magnitude bound for the FP32 ray-box filter.
+        for (int a = 0; a < 3; a++) {
+            double m = 0;
+            for (const Tri& tr : t)
+                m = std::max(m, std::max(std::fabs(tr.mn.v[a]), std::fabs(tr.mx.v[a])));
+            tree.mbox[a] = f_up(m);
         }
         int id = (int)P->trees.size();
         P->trees.push_back(tree);

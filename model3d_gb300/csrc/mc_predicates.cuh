@@ -259,3 +259,106 @@ __device__ __forceinline__ int capsule_32(const float* f, F3 p) {
 }
 
 }  // namespace mcgpu
+
+namespace mcgpu {
+
+// ------------------------------------------------------------ FP32 collider
+
+// 1 / rate of the fixed ray direction, rounded to float at compile time.
+__device__ __forceinline__ float inv_rate(int a) {
+    return a == 0 ? (float)(1.0 / RAY_DX) : (a == 1 ? (float)(1.0 / RAY_DY) : (float)(1.0 / RAY_DZ));
+}
+__device__ __forceinline__ float rate_f(int a) {
+    return a == 0 ? (float)RAY_DX : (a == 1 ? (float)RAY_DY : (float)RAY_DZ);
+}
+
+// Per-ray constants of the FP32 slab test.  With t = fma(b, 1/r, -o/r) for a
+// box coordinate b (|b| <= M_a, the tree's magnitude bound) the error against
+// the float64 t = (b - o) / r is below 4.2u (M_a + |o_a|) / r_a: float
+// rounding of b (outward, <= 2u|b|), of 1/r (u), of o and o/r (3u|o|/r) and
+// of the fma (u|t|), plus the float64 rounding (2^-52 relative).
+struct RayF {
+    float oi[3];
+    float E[3];
+};
+__device__ __forceinline__ RayF make_rayf(F3 pf, const float* mbox) {
+    RayF r;
+    const float o[3] = {pf.x, pf.y, pf.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        r.oi[a] = o[a] * inv_rate(a);
+        r.E[a] = 4.21f * U32 * (mbox[a] + fabsf(o[a])) * inv_rate(a) + 1e-30f;
+    }
+    return r;
+}
+
+// rayCollisionWithBounds + rayCollidesWithBounds with every rate > 0 is
+// exactly: hit <=> min_a t2_a >= max(0, max_a t1_a).  1 hit, 0 miss,
+// 2 undecided (run ray_box_64).
+__device__ __forceinline__ int ray_box_32(const BvhNodeF& n, const RayF& r) {
+    float t2lo = CUDART_INF_F, t2hi = CUDART_INF_F, t1lo = 0.f, t1hi = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float t1 = __fmaf_rn(n.lo[a], inv_rate(a), -r.oi[a]);
+        const float t2 = __fmaf_rn(n.hi[a], inv_rate(a), -r.oi[a]);
+        t1lo = fmaxf(t1lo, __fsub_rd(t1, r.E[a]));
+        t1hi = fmaxf(t1hi, __fadd_ru(t1, r.E[a]));
+        t2lo = fminf(t2lo, __fsub_rd(t2, r.E[a]));
+        t2hi = fminf(t2hi, __fadd_ru(t2, r.E[a]));
+    }
+    if (t2lo >= t1hi) return 1;
+    if (t2hi < t1lo) return 0;
+    return 2;
+}
+
+// Moller-Trumbore of Triangle.rayCollision (primitives.go:207-249) in FP32
+// with running absolute error bounds on o = p - t0, s1 = o.c1, b1 = s1/det,
+// c2 = o x v1, s2 = D.c2, b2, b1 + b2, s3 = v2.c2, scale = s3/det; every
+// comparison the bounds cannot decide returns 2 (run ray_tri_64).
+__device__ __forceinline__ int ray_tri_32(const TriF& t, F3 p) {
+    if (!t.valid) return 0;
+    const float ox = p.x - t.t0[0], oy = p.y - t.t0[1], oz = p.z - t.t0[2];
+    const float eox = 2.001f * U32 * (fabsf(p.x) + fabsf(t.t0[0]));
+    const float eoy = 2.001f * U32 * (fabsf(p.y) + fabsf(t.t0[1]));
+    const float eoz = 2.001f * U32 * (fabsf(p.z) + fabsf(t.t0[2]));
+    const float ai = fabsf(t.inv_det);
+    const float s1 = __fmaf_rn(ox, t.c1[0], __fmaf_rn(oy, t.c1[1], oz * t.c1[2]));
+    const float Es1 = 1.001f * (fabsf(t.c1[0]) * (eox + 4.03f * U32 * fabsf(ox)) +
+                                fabsf(t.c1[1]) * (eoy + 4.03f * U32 * fabsf(oy)) +
+                                fabsf(t.c1[2]) * (eoz + 4.03f * U32 * fabsf(oz))) + 1e-30f;
+    const float b1 = t.inv_det * s1;
+    const float Eb1 = 1.001f * (ai * (Es1 + U32 * (fabsf(s1) + Es1)) + U32 * fabsf(b1)) + 1e-30f;
+    if (__fadd_ru(b1, Eb1) < 0.f || __fsub_rd(b1, Eb1) > 1.f) return 0;
+    if (!(__fsub_rd(b1, Eb1) >= 0.f && __fadd_ru(b1, Eb1) <= 1.f)) return 2;
+    const float c2x = __fmaf_rn(oy, t.v1[2], -(oz * t.v1[1]));
+    const float c2y = __fmaf_rn(oz, t.v1[0], -(ox * t.v1[2]));
+    const float c2z = __fmaf_rn(ox, t.v1[1], -(oy * t.v1[0]));
+    const float Ec2x = 1.001f * (fabsf(t.v1[2]) * (eoy + 3.01f * U32 * fabsf(oy)) +
+                                 fabsf(t.v1[1]) * (eoz + 3.01f * U32 * fabsf(oz))) + 1e-30f;
+    const float Ec2y = 1.001f * (fabsf(t.v1[0]) * (eoz + 3.01f * U32 * fabsf(oz)) +
+                                 fabsf(t.v1[2]) * (eox + 3.01f * U32 * fabsf(ox))) + 1e-30f;
+    const float Ec2z = 1.001f * (fabsf(t.v1[1]) * (eox + 3.01f * U32 * fabsf(ox)) +
+                                 fabsf(t.v1[0]) * (eoy + 3.01f * U32 * fabsf(oy))) + 1e-30f;
+    const float s2 = __fmaf_rn(rate_f(0), c2x, __fmaf_rn(rate_f(1), c2y, rate_f(2) * c2z));
+    const float Es2 = 1.001f * (rate_f(0) * (Ec2x + 4.03f * U32 * fabsf(c2x)) +
+                                rate_f(1) * (Ec2y + 4.03f * U32 * fabsf(c2y)) +
+                                rate_f(2) * (Ec2z + 4.03f * U32 * fabsf(c2z))) + 1e-30f;
+    const float b2 = t.inv_det * s2;
+    const float Eb2 = 1.001f * (ai * (Es2 + U32 * (fabsf(s2) + Es2)) + U32 * fabsf(b2)) + 1e-30f;
+    if (__fadd_ru(b2, Eb2) < 0.f) return 0;
+    const float bs = b1 + b2;
+    const float Ebs = 1.001f * (Eb1 + Eb2 + U32 * fabsf(bs)) + 1e-30f;
+    if (__fsub_rd(bs, Ebs) > 1.f) return 0;
+    if (!(__fsub_rd(b2, Eb2) >= 0.f && __fadd_ru(bs, Ebs) <= 1.f)) return 2;
+    const float s3 = __fmaf_rn(t.v2[0], c2x, __fmaf_rn(t.v2[1], c2y, t.v2[2] * c2z));
+    const float Es3 = 1.001f * (fabsf(t.v2[0]) * (Ec2x + 4.03f * U32 * fabsf(c2x)) +
+                                fabsf(t.v2[1]) * (Ec2y + 4.03f * U32 * fabsf(c2y)) +
+                                fabsf(t.v2[2]) * (Ec2z + 4.03f * U32 * fabsf(c2z))) + 1e-30f;
+    const float sc = t.inv_det * s3;
+    const float Esc = 1.001f * (ai * (Es3 + U32 * (fabsf(s3) + Es3)) + U32 * fabsf(sc)) + 1e-30f;
+    if (__fadd_ru(sc, Esc) < 0.f) return 0;
+    if (__fsub_rd(sc, Esc) >= 0.f) return 1;
+    return 2;
+}
+
+}  // namespace mcgpu

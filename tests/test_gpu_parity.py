@@ -226,3 +226,28 @@ def test_headline_csg_full_size_properties():
     assert a.stats["corners"] > 1.0e8
     assert np.array_equal(canonical(a.TriangleSoup()), canonical(b.TriangleSoup()))
     _closed_oriented(a.triangles)
+
+
+def test_collider_fp32_filter_larger_mesh(oracle):
+    """32k-triangle displaced icosphere: FP32-filtered box and triangle tests
+    with float64 escalation give the float64 mesh."""
+    s = NewColliderSolid(MeshToCollider(displaced_icosphere(40)))
+    m = _check(oracle, s, 0.02, 8)
+    assert m.stats["bvh_nodes"] > 0 and m.stats["bvh_tris"] > 0
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_collider_contains_parity(oracle, prec):
+    rng = np.random.default_rng(17)
+    tris = displaced_icosphere(12)
+    s = NewColliderSolid(MeshToCollider(tris))
+    nodes, sets = serialize(s)
+    # random points, and points on the mesh's vertices and edges (hardest cases)
+    pts = [rng.uniform(-1.3, 1.3, size=(20000, 3))]
+    t = tris.reshape(-1, 3, 3)
+    w = rng.dirichlet([1, 1, 1], size=len(t))
+    pts.append((t * w[:, :, None]).sum(1))
+    pts.append(t[:, 0] * 0.5 + t[:, 1] * 0.5)
+    pts = np.concatenate(pts)
+    ref, _ = oracle.contains(nodes, sets, pts)
+    assert (Contains(s, pts, precision=prec) == ref).all()
