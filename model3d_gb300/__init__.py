@@ -13,7 +13,8 @@ from .solids import (Capsule, CacheSolidBounds, ColliderSolid, Cylinder, ForceSo
                      NewRect, NotLowerable, Rect, RotateSolid, Rotation, Scale, ScaleSolid,
                      Solid, Sphere, Subtract, SubtractedSolid, Torus, TransformSolid, Translate,
                      TranslateSolid, VecScale, VecScaleSolid, serialize)
-from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesSearch, MCError,
+from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesSearch,
+                 MarchingCubesSearchBatch, MCError,
                  Mesh, canonical, case_table, default_context, spacer_axis)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

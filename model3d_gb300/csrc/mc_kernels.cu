@@ -602,6 +602,127 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t m, int lane) {
 // Per tile the warp ballots which leaves' culling boxes meet the tile (float
 // boxes rounded outward, tile box rounded outward) and re-folds the program
 // only when that set changed since the previous tile of the column.
+// One work item of the classification: the column of 32 x ty x tz corner
+// tiles at (ty, tz) = (item % nty, item / nty), walked along x.  Per tile the
+// warp ballots which leaves' culling boxes meet the tile (float boxes rounded
+// outward, tile box rounded outward) and re-folds the program only when that
+// set changed since the previous tile of the column.
+template <int PREC>
+__device__ __forceinline__ void classify_column(const GridView& g, const ProgView& P, const ClassifyArgs& a, int item,
+                                                uint32_t* q, uint32_t* cur, uint32_t* prev, Counts& cnt,
+                                                unsigned long long& nconst) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (P.n_leaves + 31) >> 5;
+    const int rows = a.ty * a.tz;
+    const int ty = item % a.nty, tz = item / a.nty;
+    const int y0 = ty * a.ty, z0 = tz * a.tz;
+    const int y1 = min(y0 + a.ty - 1, g.ny - 1), z1 = min(z0 + a.tz - 1, g.nz - 1);
+    const float ylo = __double2float_rd(g.ys[y0]), yhi = __double2float_ru(g.ys[y1]);
+    const float zlo = __double2float_rd(g.zs[z0]), zhi = __double2float_ru(g.zs[z1]);
+    bool have_prev = false;
+    int len = P.n_ops;
+    const uint32_t* prog = P.ops;
+    for (int tx = 0; tx < a.ntx; tx++) {
+        const int x0 = tx * 32, x1 = min(x0 + 31, g.nx - 1);
+        if (a.cull) {
+            const float lo[3] = {__double2float_rd(g.xs[x0]), ylo, zlo};
+            const float hi[3] = {__double2float_ru(g.xs[x1]), yhi, zhi};
+            uint32_t diff = 0, any = 0;
+            for (int k = 0; k < nw; k++) {
+                int l = 32 * k + lane;
+                bool on = l < P.n_leaves && cull_overlap_f(P.cull_f + 6 * (size_t)l, lo, hi);
+                uint32_t w = __ballot_sync(0xffffffffu, on);
+                any |= w;
+                if (lane == 0) {
+                    diff |= (!have_prev || prev[k] != w) ? 1u : 0u;
+                    cur[k] = w;
+                    prev[k] = w;
+                }
+            }
+            diff = __shfl_sync(0xffffffffu, diff, 0);
+            if (diff) {
+                if (!any) {
+                    len = P.n_ops_allfalse;
+                    prog = P.ops_allfalse;
+                } else {
+                    int L = 0;
+                    if (lane == 0)
+                        L = fold_program(P.ops, P.n_ops, cur, q);
+                    len = __shfl_sync(0xffffffffu, L, 0);
+                    prog = q;
+                }
+                have_prev = true;
+            }
+            __syncwarp();
+        }
+        if (len < 0) nconst++;
+        const int x = x0 + lane;
+        const bool xin = x < g.nx;
+        const double px = xin ? g.xs[x] : g.xs[g.nx - 1];
+        const float pxf = xin ? a.xf[x] : a.xf[g.nx - 1];
+        uint32_t edge_mask = 0;
+        if (x0 == 0) edge_mask |= 1u;
+        if (g.nx - 1 - x0 < 32) edge_mask |= 1u << (g.nx - 1 - x0);
+        if (len >= 0 && P.rows_ok && rows <= 32) {
+            RowCtx rc;
+            rc.px = px;
+            rc.pxf = pxf;
+            rc.nrows = rows;
+            rc.y0 = y0;
+            rc.z0 = z0;
+            rc.ty = a.ty;
+            rc.ys = g.ys;
+            rc.zs = g.zs;
+            const int ry = min(y0 + lane % a.ty, g.ny - 1), rz = min(z0 + lane / a.ty, g.nz - 1);
+            const bool rin = lane < rows && y0 + lane % a.ty < g.ny && z0 + lane / a.ty < g.nz;
+            rc.ry = g.ys[ry];
+            rc.rz = g.zs[rz];
+            rc.ryf = a.yf[ry];
+            rc.rzf = a.zf[rz];
+            rc.rowmask = __ballot_sync(0xffffffffu, rin);
+            uint32_t m = eval_program_rows<PREC>(P, prog, len, rc, cnt, a.err);
+            if (!xin) m = 0;
+            // Lane x holds bit r of row r; transpose the 32 x 32 bit block so
+            // that lane r holds row r's word (bit x), then store it.
+            m = transpose32(m, lane);
+            if (rin) {
+                const int y = y0 + lane % a.ty, z = z0 + lane / a.ty;
+                a.bits[((size_t)z * g.ny + y) * g.W + tx] = m;
+                const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                if (m && (edge_row || (m & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
+            }
+            continue;
+        }
+        if (len < 0 && rows <= 32) {
+            const uint32_t word = len == FOLD_TRUE ? __ballot_sync(0xffffffffu, xin) : 0u;
+            const int y = y0 + lane % a.ty, z = z0 + lane / a.ty;
+            if (lane < rows && y < g.ny && z < g.nz) {
+                a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
+                const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
+            }
+            continue;
+        }
+        for (int rr = 0; rr < rows; rr++) {
+            const int y = y0 + rr % a.ty, z = z0 + rr / a.ty;
+            if (y >= g.ny || z >= g.nz) continue;
+            bool b;
+            if (len == FOLD_FALSE) b = false;
+            else if (len == FOLD_TRUE) b = xin;
+            else b = xin && eval_program<PREC>(P, prog, len, P3{px, g.ys[y], g.zs[z]}, F3{pxf, a.yf[y], a.zf[z]},
+                                               cnt, a.err);
+            const uint32_t word = __ballot_sync(0xffffffffu, b);
+            if (lane == 0) {
+                a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
+                // solid is true outside of bounds (mc.go:687-689)
+                const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
+            }
+        }
+    }
+}
+
+// One warp per work item, items handed out by an atomic counter.
 template <int PREC>
 __global__ void __launch_bounds__(256, 3) k_classify(GridView g, ProgView P, ClassifyArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -614,118 +735,12 @@ __global__ void __launch_bounds__(256, 3) k_classify(GridView g, ProgView P, Cla
     Counts cnt;
     unsigned long long nconst = 0;
     const int nitems = a.nty * a.ntz;
-    const int rows = a.ty * a.tz;
     for (;;) {
         int item = 0;
         if (lane == 0) item = (int)atomicAdd(a.work, 1u);
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nitems) break;
-        const int ty = item % a.nty, tz = item / a.nty;
-        const int y0 = ty * a.ty, z0 = tz * a.tz;
-        const int y1 = min(y0 + a.ty - 1, g.ny - 1), z1 = min(z0 + a.tz - 1, g.nz - 1);
-        const float ylo = __double2float_rd(g.ys[y0]), yhi = __double2float_ru(g.ys[y1]);
-        const float zlo = __double2float_rd(g.zs[z0]), zhi = __double2float_ru(g.zs[z1]);
-        bool have_prev = false;
-        int len = P.n_ops;
-        const uint32_t* prog = P.ops;
-        for (int tx = 0; tx < a.ntx; tx++) {
-            const int x0 = tx * 32, x1 = min(x0 + 31, g.nx - 1);
-            if (a.cull) {
-                const float lo[3] = {__double2float_rd(g.xs[x0]), ylo, zlo};
-                const float hi[3] = {__double2float_ru(g.xs[x1]), yhi, zhi};
-                uint32_t diff = 0, any = 0;
-                for (int k = 0; k < nw; k++) {
-                    int l = 32 * k + lane;
-                    bool on = l < P.n_leaves && cull_overlap_f(P.cull_f + 6 * (size_t)l, lo, hi);
-                    uint32_t w = __ballot_sync(0xffffffffu, on);
-                    any |= w;
-                    if (lane == 0) {
-                        diff |= (!have_prev || prev[k] != w) ? 1u : 0u;
-                        cur[k] = w;
-                        prev[k] = w;
-                    }
-                }
-                diff = __shfl_sync(0xffffffffu, diff, 0);
-                if (diff) {
-                    if (!any) {
-                        len = P.n_ops_allfalse;
-                        prog = P.ops_allfalse;
-                    } else {
-                        int L = 0;
-                        if (lane == 0)
-                            L = fold_program(P.ops, P.n_ops, cur, q);
-                        len = __shfl_sync(0xffffffffu, L, 0);
-                        prog = q;
-                    }
-                    have_prev = true;
-                }
-                __syncwarp();
-            }
-            if (len < 0) nconst++;
-            const int x = x0 + lane;
-            const bool xin = x < g.nx;
-            const double px = xin ? g.xs[x] : g.xs[g.nx - 1];
-            const float pxf = xin ? a.xf[x] : a.xf[g.nx - 1];
-            uint32_t edge_mask = 0;
-            if (x0 == 0) edge_mask |= 1u;
-            if (g.nx - 1 - x0 < 32) edge_mask |= 1u << (g.nx - 1 - x0);
-            if (len >= 0 && P.rows_ok && rows <= 32) {
-                RowCtx rc;
-                rc.px = px;
-                rc.pxf = pxf;
-                rc.nrows = rows;
-                rc.y0 = y0;
-                rc.z0 = z0;
-                rc.ty = a.ty;
-                rc.ys = g.ys;
-                rc.zs = g.zs;
-                const int ry = min(y0 + lane % a.ty, g.ny - 1), rz = min(z0 + lane / a.ty, g.nz - 1);
-                const bool rin = lane < rows && y0 + lane % a.ty < g.ny && z0 + lane / a.ty < g.nz;
-                rc.ry = g.ys[ry];
-                rc.rz = g.zs[rz];
-                rc.ryf = a.yf[ry];
-                rc.rzf = a.zf[rz];
-                rc.rowmask = __ballot_sync(0xffffffffu, rin);
-                uint32_t m = eval_program_rows<PREC>(P, prog, len, rc, cnt, a.err);
-                if (!xin) m = 0;
-                // Lane x holds bit r of row r; transpose the 32 x 32 bit block so
-                // that lane r holds row r's word (bit x), then store it.
-                m = transpose32(m, lane);
-                if (rin) {
-                    const int y = y0 + lane % a.ty, z = z0 + lane / a.ty;
-                    a.bits[((size_t)z * g.ny + y) * g.W + tx] = m;
-                    const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
-                    if (m && (edge_row || (m & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
-                }
-                continue;
-            }
-            if (len < 0 && rows <= 32) {
-                const uint32_t word = len == FOLD_TRUE ? __ballot_sync(0xffffffffu, xin) : 0u;
-                const int y = y0 + lane % a.ty, z = z0 + lane / a.ty;
-                if (lane < rows && y < g.ny && z < g.nz) {
-                    a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
-                    const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
-                    if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
-                }
-                continue;
-            }
-            for (int rr = 0; rr < rows; rr++) {
-                const int y = y0 + rr % a.ty, z = z0 + rr / a.ty;
-                if (y >= g.ny || z >= g.nz) continue;
-                bool b;
-                if (len == FOLD_FALSE) b = false;
-                else if (len == FOLD_TRUE) b = xin;
-                else b = xin && eval_program<PREC>(P, prog, len, P3{px, g.ys[y], g.zs[z]}, F3{pxf, a.yf[y], a.zf[z]},
-                                                   cnt, a.err);
-                const uint32_t word = __ballot_sync(0xffffffffu, b);
-                if (lane == 0) {
-                    a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
-                    // solid is true outside of bounds (mc.go:687-689)
-                    const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
-                    if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
-                }
-            }
-        }
+        classify_column<PREC>(g, P, a, item, q, cur, prev, cnt, nconst);
     }
     flush_counts(cnt, a.stats);
     if (lane == 0 && nconst) atomicAdd(&a.stats[ST_TILES_CONST], nconst);
@@ -813,34 +828,41 @@ __device__ __forceinline__ void block_sum2(uint32_t& a, uint32_t& b) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_count(GridView g, CountArgs a) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t nv = 0, nt = 0;
-    if (i < a.nchunks) {
-        int c = (int)(i % g.CX);
-        long long r = i / g.CX;
-        int y = (int)(r % (g.ny - 1)), z = (int)(r / (g.ny - 1));
-        Rows R = load_rows(g, a.bits, c, y, z);
-        uint32_t vm = valid_mask(g, c);
-        uint32_t cp[8];
-        corner_planes(R, cp);
-        uint32_t xm = (cp[0] ^ cp[1]) & vm, ym = (R.r[0] ^ R.r[1]) & vm, zm = (R.r[0] ^ R.r[2]) & vm;
-        uint32_t all = cp[0], anyb = cp[0];
+// Counts of one 32-cube chunk (local index i of the grid's chunk space):
+// crossed x/y/z edges with base corner in the chunk and triangles of its
+// active cubes, packed as cx | cy << 6 | cz << 12 | ntri << 18.
+__device__ __forceinline__ uint32_t count_chunk(const GridView& g, const uint32_t* bits, long long i, uint32_t& nv,
+                                                uint32_t& nt) {
+    const int c = (int)(i % g.CX);
+    const long long r = i / g.CX;
+    const int y = (int)(r % (g.ny - 1)), z = (int)(r / (g.ny - 1));
+    Rows R = load_rows(g, bits, c, y, z);
+    const uint32_t vm = valid_mask(g, c);
+    uint32_t cp[8];
+    corner_planes(R, cp);
+    const uint32_t xm = (cp[0] ^ cp[1]) & vm, ym = (R.r[0] ^ R.r[1]) & vm, zm = (R.r[0] ^ R.r[2]) & vm;
+    uint32_t all = cp[0], anyb = cp[0];
 #pragma unroll
-        for (int k = 1; k < 8; k++) {
-            all &= cp[k];
-            anyb |= cp[k];
-        }
-        uint32_t act = anyb & ~all & vm;
-        while (act) {
-            int b = __ffs(act) - 1;
-            act &= act - 1;
-            nt += c_table.count[cube_case(cp, b)];
-        }
-        uint32_t cx = __popc(xm), cy = __popc(ym), cz = __popc(zm);
-        nv = cx + cy + cz;
-        a.packed[i] = cx | (cy << 6) | (cz << 12) | (nt << 18);
+    for (int k = 1; k < 8; k++) {
+        all &= cp[k];
+        anyb |= cp[k];
     }
+    uint32_t act = anyb & ~all & vm;
+    nt = 0;
+    while (act) {
+        const int b = __ffs(act) - 1;
+        act &= act - 1;
+        nt += c_table.count[cube_case(cp, b)];
+    }
+    const uint32_t cx = __popc(xm), cy = __popc(ym), cz = __popc(zm);
+    nv = cx + cy + cz;
+    return cx | (cy << 6) | (cz << 12) | (nt << 18);
+}
+
+__global__ void __launch_bounds__(256) k_count(GridView g, CountArgs a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t nv = 0, nt = 0;
+    if (i < a.nchunks) a.packed[i] = count_chunk(g, a.bits, i, nv, nt);
     block_sum2(nv, nt);
     if (threadIdx.x == 0) {
         a.blocksum[2 * blockIdx.x] = nv;
@@ -919,9 +941,11 @@ struct EmitArgs {
     long long nchunks;
 };
 
-__global__ void __launch_bounds__(256) k_emit(GridView g, EmitArgs a) {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.nchunks) return;
+// Emission for one chunk (local index i; a.packed / a.prefv / a.preft point
+// at the grid's own chunk arrays, whose vertex and triangle offsets may be
+// global).  Keys go to a.keys[prefv], triangles to a.tris[preft] with vertex
+// ids minus vsub (the grid's first global vertex).
+__device__ __forceinline__ void emit_chunk(const GridView& g, const EmitArgs& a, long long i, uint32_t vsub) {
     uint32_t pk = a.packed[i];
     if (pk == 0) return;
     const int c = (int)(i % g.CX);
@@ -1005,9 +1029,14 @@ __global__ void __launch_bounds__(256) k_emit(GridView g, EmitArgs a) {
         const int kc = cube_case(cp, b);
         const int n3 = 3 * c_table.count[kc];
         int32_t* out = a.tris + 3 * (size_t)t_out;
-        for (int e = 0; e < n3; e++) out[e] = (int32_t)eid[c_table.edge[kc][e]];
+        for (int e = 0; e < n3; e++) out[e] = (int32_t)(eid[c_table.edge[kc][e]] - vsub);
         t_out += n3 / 3;
     }
+}
+
+__global__ void __launch_bounds__(256) k_emit(GridView g, EmitArgs a) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.nchunks) emit_chunk(g, a, i, 0u);
 }
 
 // ------------------------------------------------------------ k_search
@@ -1079,6 +1108,102 @@ __device__ __forceinline__ int lookup_edge(const GridView& g, const P3& c, doubl
     return 1;
 }
 
+// Vertex setup: edge key -> midpoint (corners[a].Mid(corners[b]),
+// mc.go:401-407) and, when iters != 0, LookupEdgePoint.  Returns the status.
+__device__ __forceinline__ int vertex_setup(const GridView& g, unsigned long long key, int iters, double inv_dl,
+                                            P3* cpt, int* axis, double* lo, double* hi) {
+    const int ax = (int)(key >> 60);
+    const int z = (int)((key >> 40) & 0xfffff), y = (int)((key >> 20) & 0xfffff), x = (int)(key & 0xfffff);
+    const P3 c0{g.xs[x], g.ys[y], g.zs[z]};
+    P3 c1 = c0;
+    if (ax == 0) c1.x = g.xs[x + 1];
+    else if (ax == 1) c1.y = g.ys[y + 1];
+    else c1.z = g.zs[z + 1];
+    *cpt = P3{D_MUL(D_ADD(c0.x, c1.x), 0.5), D_MUL(D_ADD(c0.y, c1.y), 0.5), D_MUL(D_ADD(c0.z, c1.z), 0.5)};
+    *axis = 0;
+    if (iters == 0) return 0;
+    return lookup_edge(g, *cpt, inv_dl, axis, lo, hi);
+}
+
+// mcSearchPoint (mc.go:223-258) against a (folded) program; only the axis
+// coordinate moves, so the float point is updated in place.
+template <int PREC>
+__device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, int len, P3 cpt, int axis, double lo,
+                                     double hi, int iters, Counts& cnt, int* err) {
+    F3 pf = to_f3(cpt);
+    auto contains = [&](P3 pt, double v) -> bool {
+        if (len == FOLD_FALSE) return false;
+        if (len == FOLD_TRUE) return true;
+        const float vf = (float)v;
+        if (axis == 0) pf.x = vf;
+        else if (axis == 1) pf.y = vf;
+        else pf.z = vf;
+        return eval_program<PREC>(P, prog, len, pt, pf, cnt, err);
+    };
+    double fp = lo, tp = hi;
+    P3 t = cpt;
+    set_comp(t, axis, tp);
+    if (!contains(t, tp)) {
+        fp = hi;
+        tp = lo;
+    }
+    P3 arr = cpt;
+    for (int k = 0; k < iters; k++) {
+        const double mid = D_MUL(D_ADD(fp, tp), 0.5);  // x / 2 and x * 0.5 round the same real
+        set_comp(arr, axis, mid);
+        if (contains(arr, mid)) tp = mid;
+        else fp = mid;
+    }
+    set_comp(arr, axis, D_MUL(D_ADD(fp, tp), 0.5));
+    return arr;
+}
+
+// Per-warp culling for the search: the union of the segments the warp
+// bisects, rounded outward to float, selects the active leaves; the program
+// is re-folded only when that set changed.  All lanes must call it.
+__device__ __forceinline__ void search_cull(const ProgView& P, bool work, const P3& cpt, int axis, double lo,
+                                            double hi, uint32_t* q, uint32_t* cur, uint32_t* prev, bool& have_prev,
+                                            const uint32_t*& prog, int& len) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (P.n_leaves + 31) >> 5;
+    float blo[3], bhi[3];
+    for (int i = 0; i < 3; i++) {
+        double vlo = work ? comp(cpt, i) : CUDART_INF, vhi = work ? comp(cpt, i) : -CUDART_INF;
+        if (work && i == axis) {
+            vlo = fmin(lo, hi);
+            vhi = fmax(lo, hi);
+        }
+        blo[i] = __double2float_rd(warp_min(vlo));
+        bhi[i] = __double2float_ru(warp_max(vhi));
+    }
+    uint32_t diff = 0, any = 0;
+    for (int k = 0; k < nw; k++) {
+        const int l = 32 * k + lane;
+        const bool on = l < P.n_leaves && cull_overlap_f(P.cull_f + 6 * (size_t)l, blo, bhi);
+        const uint32_t w = __ballot_sync(0xffffffffu, on);
+        any |= w;
+        if (lane == 0) {
+            diff |= (!have_prev || prev[k] != w) ? 1u : 0u;
+            cur[k] = w;
+            prev[k] = w;
+        }
+    }
+    diff = __shfl_sync(0xffffffffu, diff, 0);
+    if (diff) {
+        if (!any) {
+            len = P.n_ops_allfalse;
+            prog = P.ops_allfalse;
+        } else {
+            int L = 0;
+            if (lane == 0) L = fold_program(P.ops, P.n_ops, cur, q);
+            len = __shfl_sync(0xffffffffu, L, 0);
+            prog = q;
+        }
+        have_prev = true;
+    }
+    __syncwarp();
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(128, 4) k_search(GridView g, ProgView P, SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1105,94 +1230,13 @@ __global__ void __launch_bounds__(128, 4) k_search(GridView g, ProgView P, Searc
         int axis = 0;
         double lo = 0, hi = 0;
         P3 cpt{0, 0, 0};
-        int status = 0;  // 0 ok, 1 not on edge, 2 index
-        if (live) {
-            unsigned long long key = a.keys[v];
-            int ax = (int)(key >> 60);
-            int z = (int)((key >> 40) & 0xfffff), y = (int)((key >> 20) & 0xfffff), x = (int)(key & 0xfffff);
-            P3 c0{g.xs[x], g.ys[y], g.zs[z]};
-            P3 c1 = c0;
-            if (ax == 0) c1.x = g.xs[x + 1];
-            else if (ax == 1) c1.y = g.ys[y + 1];
-            else c1.z = g.zs[z + 1];
-            // corners[a].Mid(corners[b]) (mc.go:401-407, coords.go:196-198)
-            cpt = P3{D_MUL(D_ADD(c0.x, c1.x), 0.5), D_MUL(D_ADD(c0.y, c1.y), 0.5), D_MUL(D_ADD(c0.z, c1.z), 0.5)};
-            if (a.iters != 0) status = lookup_edge(g, cpt, a.inv_dl, &axis, &lo, &hi);
-        }
+        int status = live ? vertex_setup(g, a.keys[v], a.iters, a.inv_dl, &cpt, &axis, &lo, &hi) : 0;
         if (status == 1) atomicOr(&a.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&a.err[ER_EDGE_INDEX], 1);
         const bool work = live && a.iters != 0 && status == 0;
-        if (a.cull && __any_sync(0xffffffffu, work)) {
-            // Union of the segments this warp bisects, rounded outward to float.
-            float blo[3], bhi[3];
-            for (int i = 0; i < 3; i++) {
-                double vlo = work ? comp(cpt, i) : CUDART_INF, vhi = work ? comp(cpt, i) : -CUDART_INF;
-                if (work && i == axis) {
-                    vlo = fmin(lo, hi);
-                    vhi = fmax(lo, hi);
-                }
-                blo[i] = __double2float_rd(warp_min(vlo));
-                bhi[i] = __double2float_ru(warp_max(vhi));
-            }
-            uint32_t diff = 0, any = 0;
-            for (int k = 0; k < nw; k++) {
-                int l = 32 * k + lane;
-                bool on = l < P.n_leaves && cull_overlap_f(P.cull_f + 6 * (size_t)l, blo, bhi);
-                uint32_t w = __ballot_sync(0xffffffffu, on);
-                any |= w;
-                if (lane == 0) {
-                    diff |= (!have_prev || prev[k] != w) ? 1u : 0u;
-                    cur[k] = w;
-                    prev[k] = w;
-                }
-            }
-            diff = __shfl_sync(0xffffffffu, diff, 0);
-            if (diff) {
-                if (!any) {
-                    len = P.n_ops_allfalse;
-                    prog = P.ops_allfalse;
-                } else {
-                    int L = 0;
-                    if (lane == 0)
-                        L = fold_program(P.ops, P.n_ops, cur, q);
-                    len = __shfl_sync(0xffffffffu, L, 0);
-                    prog = q;
-                }
-                have_prev = true;
-            }
-            __syncwarp();
-        }
+        if (a.cull && __any_sync(0xffffffffu, work)) search_cull(P, work, cpt, axis, lo, hi, q, cur, prev, have_prev, prog, len);
         if (live && status == 0) {
-            P3 out = cpt;
-            if (work) {
-                // mcSearchPoint (mc.go:223-258); only the axis coordinate moves.
-                F3 pf = to_f3(cpt);
-                auto contains = [&](P3 pt, double v) -> bool {
-                    if (len == FOLD_FALSE) return false;
-                    if (len == FOLD_TRUE) return true;
-                    const float vf = (float)v;
-                    if (axis == 0) pf.x = vf;
-                    else if (axis == 1) pf.y = vf;
-                    else pf.z = vf;
-                    return eval_program<PREC>(P, prog, len, pt, pf, cnt, a.err);
-                };
-                double fp = lo, tp = hi;
-                P3 t = cpt;
-                set_comp(t, axis, tp);
-                if (!contains(t, tp)) {
-                    fp = hi;
-                    tp = lo;
-                }
-                P3 arr = cpt;
-                for (int k = 0; k < a.iters; k++) {
-                    double mid = D_MUL(D_ADD(fp, tp), 0.5);  // x / 2 and x * 0.5 round the same real
-                    set_comp(arr, axis, mid);
-                    if (contains(arr, mid)) tp = mid;
-                    else fp = mid;
-                }
-                set_comp(arr, axis, D_MUL(D_ADD(fp, tp), 0.5));
-                out = arr;
-            }
+            const P3 out = work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, a.iters, cnt, a.err) : cpt;
             a.verts[3 * v] = out.x;
             a.verts[3 * v + 1] = out.y;
             a.verts[3 * v + 2] = out.z;
@@ -1213,6 +1257,177 @@ __global__ void k_contains(ProgView P, const double* pts, long long n, uint8_t* 
         out[i] = eval_program<PREC>(P, P.ops, P.n_ops, p, to_f3(p), cnt, err) ? 1 : 0;
     }
     flush_counts(cnt, stats);
+}
+
+// ------------------------------------------------------------ batched launch
+//
+// Many solids meshed by one launch per phase: every job's tile columns,
+// 32-cube chunks and vertices are concatenated into global index spaces;
+// a thread or warp finds its job by binary search over the job offsets.
+// Sizes are read from device memory, so after one sizing run the whole
+// pipeline can be captured in a CUDA graph and replayed.
+
+struct JobD {
+    GridView g;
+    ProgView P;
+    ClassifyArgs ca;  // bits / err point at the job's own regions
+    long long chunk_off;
+    long long nchunks;
+    int iters;
+    int pad;
+    double inv_dl;
+};
+
+// Last index k in [0, n) with off[k] <= x (off ascending, off[0] <= x).
+__device__ __forceinline__ int find_slot(const long long* off, int n, long long x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+struct BatchArgs {
+    const JobD* jobs;
+    int njobs;
+    const long long* sched_off;  // classify items, jobs in largest-first order
+    const int* sched_job;
+    long long nitems;
+    const long long* chunk_offs;  // njobs + 1, natural job order
+    long long nchunks;
+    unsigned long long* vbase;    // njobs + 1 (filled by k_job_bases)
+    unsigned long long* tbase;
+    unsigned long long* totals;   // [0] vertices, [1] triangles
+    unsigned int* work;
+    unsigned long long* stats;
+    int fold_words;  // per-warp shared words: max over jobs of fold_cap + 2 * leaf words
+    int cull;
+};
+
+template <int PREC>
+__global__ void __launch_bounds__(256, 3) k_classify_batch(BatchArgs b) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* base = (uint32_t*)smem + (size_t)warp * b.fold_words;
+    Counts cnt;
+    unsigned long long nconst = 0;
+    for (;;) {
+        long long item = 0;
+        if (lane == 0) item = (long long)atomicAdd(b.work, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= b.nitems) break;
+        const int k = find_slot(b.sched_off, b.njobs, item);
+        const JobD& J = b.jobs[b.sched_job[k]];
+        const int nw = (J.P.n_leaves + 31) >> 5;
+        uint32_t* cur = base + J.P.fold_cap;
+        classify_column<PREC>(J.g, J.P, J.ca, (int)(item - b.sched_off[k]), base, cur, cur + nw, cnt, nconst);
+    }
+    flush_counts(cnt, b.stats);
+    if (lane == 0 && nconst) atomicAdd(&b.stats[ST_TILES_CONST], nconst);
+}
+
+__global__ void __launch_bounds__(256) k_count_batch(BatchArgs b, uint32_t* packed, uint32_t* blocksum) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t nv = 0, nt = 0;
+    if (i < b.nchunks) {
+        const int j = find_slot(b.chunk_offs, b.njobs, i);
+        const JobD& J = b.jobs[j];
+        packed[i] = count_chunk(J.g, J.ca.bits, i - b.chunk_offs[j], nv, nt);
+    }
+    block_sum2(nv, nt);
+    if (threadIdx.x == 0) {
+        blocksum[2 * blockIdx.x] = nv;
+        blocksum[2 * blockIdx.x + 1] = nt;
+    }
+}
+
+// First global vertex / triangle of every job (a job without chunks starts
+// where the next one does).
+__global__ void k_job_bases(BatchArgs b, const uint32_t* prefv, const uint32_t* preft) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j <= b.njobs; j += gridDim.x * blockDim.x) {
+        const long long c0 = b.chunk_offs[j];
+        const bool in = c0 < b.nchunks;
+        b.vbase[j] = in ? prefv[c0] : b.totals[0];
+        b.tbase[j] = in ? preft[c0] : b.totals[1];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_emit_batch(BatchArgs b, const uint32_t* packed, const uint32_t* prefv,
+                                                     const uint32_t* preft, unsigned long long* keys, int32_t* tris) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.nchunks) return;
+    const int j = find_slot(b.chunk_offs, b.njobs, i);
+    const JobD& J = b.jobs[j];
+    const long long c0 = b.chunk_offs[j];
+    EmitArgs ea{J.ca.bits, packed + c0, prefv + c0, preft + c0, keys, tris, J.nchunks};
+    emit_chunk(J.g, ea, i - c0, (uint32_t)b.vbase[j]);
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsigned long long* keys, double* verts) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* q = (uint32_t*)smem + (size_t)warp * b.fold_words;
+    Counts cnt;
+    const long long nverts = (long long)b.totals[0];
+    const long long nwarps_total = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    const long long nbatch = (nverts + 31) / 32;
+    const long long per = (nbatch + nwarps_total - 1) / nwarps_total;
+    const long long b_begin = gw * per, b_end = min(nbatch, b_begin + per);
+    bool have_prev = false;
+    int prev_job = -1;
+    const uint32_t* prog = nullptr;
+    int len = 0;
+    for (long long bt = b_begin; bt < b_end; bt++) {
+        const long long v = bt * 32 + lane;
+        const bool live = v < nverts;
+        const int j = live ? find_slot((const long long*)b.vbase, b.njobs, v) : -1;
+        const int j0 = __shfl_sync(0xffffffffu, j, 0);
+        const bool uniform = __all_sync(0xffffffffu, !live || j == j0);
+        const JobD* Jp = live ? &b.jobs[j] : &b.jobs[j0];
+        int axis = 0;
+        double lo = 0, hi = 0;
+        P3 cpt{0, 0, 0};
+        const int status = live ? vertex_setup(Jp->g, keys[v], Jp->iters, Jp->inv_dl, &cpt, &axis, &lo, &hi) : 0;
+        if (status == 1) atomicOr(&Jp->ca.err[ER_NOT_ON_EDGE], 1);
+        if (status == 2) atomicOr(&Jp->ca.err[ER_EDGE_INDEX], 1);
+        const bool work = live && Jp->iters != 0 && status == 0;
+        if (uniform) {
+            const ProgView& P = b.jobs[j0].P;
+            if (j0 != prev_job) {
+                have_prev = false;
+                prev_job = j0;
+                prog = P.ops;
+                len = P.n_ops;
+            }
+            const int nw = (P.n_leaves + 31) >> 5;
+            uint32_t* cur = q + P.fold_cap;
+            if (b.cull && __any_sync(0xffffffffu, work))
+                search_cull(P, work, cpt, axis, lo, hi, q, cur, cur + nw, have_prev, prog, len);
+            if (live && status == 0) {
+                const P3 out = work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, Jp->iters, cnt, Jp->ca.err) : cpt;
+                verts[3 * v] = out.x;
+                verts[3 * v + 1] = out.y;
+                verts[3 * v + 2] = out.z;
+            }
+        } else {
+            // The batch straddles jobs: every lane runs its own job's full program.
+            prev_job = -1;
+            if (live && status == 0) {
+                const P3 out = work ? bisect<PREC>(Jp->P, Jp->P.ops, Jp->P.n_ops, cpt, axis, lo, hi, Jp->iters, cnt,
+                                                   Jp->ca.err)
+                                    : cpt;
+                verts[3 * v] = out.x;
+                verts[3 * v + 1] = out.y;
+                verts[3 * v + 2] = out.z;
+            }
+        }
+        __syncwarp();
+    }
+    flush_counts(cnt, b.stats);
 }
 
 }  // namespace mcgpu
@@ -1272,7 +1487,37 @@ void build_table_host() {
 
 }  // namespace
 
+// A batch laid out on the device, kept for CUDA-graph replay of the same
+// (solids, deltas, iters, options).
+struct BatchPlan {
+    std::vector<uint64_t> solids;  // serials
+    std::vector<double> deltas;
+    std::vector<int> iters;
+    mc_opts opts{};
+    std::vector<int> dev_job;            // caller job -> device job (-1: not run)
+    std::vector<mc_status> pre_status;   // per caller job, errors found on the host
+    std::vector<mcgpu::JobD> hjobs;
+    std::vector<long long> hchunk_offs;
+    long long nitems = 0, nchunks = 0;
+    int nblk = 0, fold_words = 0, grid_c = 1, grid_s = 1, prec = 1;
+    size_t smem_c = 0, smem_s = 0;
+    long long cap_V = -1, cap_T = -1;
+    cudaGraphExec_t exec = nullptr;
+    DevBuf jobs, sched_off, sched_job, chunk_offs, vbase, tbase, grid, bits, errs, packed, blocksum, blockoff, prefv,
+        preft, keys, verts, tris, totals, stats;
+    unsigned long long* h_stage = nullptr;  // pinned staging for the outputs
+    size_t h_stage_bytes = 0;
+    ~BatchPlan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (DevBuf* b : {&jobs, &sched_off, &sched_job, &chunk_offs, &vbase, &tbase, &grid, &bits, &errs, &packed,
+                          &blocksum, &blockoff, &prefv, &preft, &keys, &verts, &tris, &totals, &stats})
+            b->release();
+        if (h_stage) cudaFreeHost(h_stage);
+    }
+};
+
 struct mc_ctx {
+    std::unique_ptr<BatchPlan> plan;
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
@@ -1285,6 +1530,7 @@ struct mc_ctx {
 };
 
 struct mc_solid {
+    uint64_t serial = 0;  // unique per created solid (batch plans key on it, never on the address)
     mc_ctx* ctx = nullptr;
     HostProgram host;
     DevBuf buf;
@@ -1394,6 +1640,7 @@ void mc_destroy(mc_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    ctx->plan.reset();
     for (DevBuf* b : {&ctx->xs, &ctx->ys, &ctx->zs, &ctx->xf, &ctx->yf, &ctx->zf, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
                       &ctx->prefv, &ctx->preft, &ctx->keys, &ctx->verts, &ctx->tris, &ctx->stats, &ctx->errs,
                       &ctx->totals, &ctx->pts, &ctx->pout})
@@ -1409,7 +1656,9 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
                           size_t n_sets, mc_solid** out) {
     if (!ctx || !out) return MC_ERR_ARG;
     *out = nullptr;
+    static std::atomic<uint64_t> g_serial{0};
     std::unique_ptr<mc_solid> s(new mc_solid());
+    s->serial = ++g_serial;
     s->ctx = ctx;
     try {
         lower_scene(nodes, n_nodes, sets, n_sets, &s->host);
@@ -1770,15 +2019,331 @@ mc_status mc_contains(mc_ctx* ctx, const mc_solid* solid, const double* points, 
     return MC_OK;
 }
 
-mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_opts* opts, mc_mesh* outs,
+mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_opts* opts_in, mc_mesh* outs,
                           mc_status* job_status) {
     if (!ctx || (n && (!jobs || !outs))) return fail(ctx, MC_ERR_ARG, "bad argument");
+    for (size_t i = 0; i < n; i++) {
+        std::memset(&outs[i], 0, sizeof(mc_mesh));
+        if (job_status) job_status[i] = MC_OK;
+        if (!jobs[i].solid) return fail(ctx, MC_ERR_ARG, "null solid in batch");
+    }
+    if (n == 0) return MC_OK;
+    CK(cudaSetDevice(ctx->device));
+    const mc_opts opts = default_opts(opts_in);
+    cudaStream_t sm = ctx->stream;
+
+    // Reuse the plan (and its CUDA graph) when the same batch comes back.
+    BatchPlan* pl = ctx->plan.get();
+    bool same = pl && pl->solids.size() == n && std::memcmp(&pl->opts, &opts, sizeof(opts)) == 0;
+    for (size_t i = 0; same && i < n; i++)
+        same = pl->solids[i] == jobs[i].solid->serial && std::memcmp(&pl->deltas[i], &jobs[i].delta, 8) == 0 &&
+               pl->iters[i] == jobs[i].iters;
+    if (!same) {
+        ctx->plan.reset(new BatchPlan());
+        pl = ctx->plan.get();
+        pl->opts = opts;
+        pl->prec = opts.precision == MC_PREC_FP64 ? MC_PREC_FP64 : MC_PREC_FP32_FILTERED;
+        pl->dev_job.assign(n, -1);
+        pl->pre_status.assign(n, MC_OK);
+        std::vector<double> gd;
+        std::vector<float> gf;
+        struct Lay {
+            size_t xd, yd, zd, xf, yf, zf, bits, nbits;
+            long long items, cost;
+        };
+        std::vector<Lay> lay;
+        size_t nbits_total = 0;
+        int fold_words = 4;
+        for (size_t i = 0; i < n; i++) {
+            pl->solids.push_back(jobs[i].solid->serial);
+            pl->deltas.push_back(jobs[i].delta);
+            pl->iters.push_back(jobs[i].iters);
+            const HostProgram& H = jobs[i].solid->host;
+            if (jobs[i].iters < 0) {
+                pl->pre_status[i] = MC_ERR_ARG;
+                continue;
+            }
+            if (!bounds_valid(H.root_min, H.root_max)) {
+                pl->pre_status[i] = MC_ERR_INVALID_BOUNDS;
+                continue;
+            }
+            std::vector<double> X, Y, Z;
+            if (spacer_axis(H.root_min[0], H.root_max[0], jobs[i].delta, &X, kMaxAxis + 1) ||
+                spacer_axis(H.root_min[1], H.root_max[1], jobs[i].delta, &Y, kMaxAxis + 1) ||
+                spacer_axis(H.root_min[2], H.root_max[2], jobs[i].delta, &Z, kMaxAxis + 1) ||
+                (int64_t)X.size() * Y.size() * Z.size() > kMaxCorners) {
+                pl->pre_status[i] = MC_ERR_GRID;
+                continue;
+            }
+            pl->dev_job[i] = (int)pl->hjobs.size();
+            JobD J{};
+            const int nx = (int)X.size(), ny = (int)Y.size(), nz = (int)Z.size();
+            J.g.nx = nx;
+            J.g.ny = ny;
+            J.g.nz = nz;
+            J.g.W = (nx + 31) / 32 + 1;
+            J.g.CX = nx >= 2 ? (nx - 1 + 31) / 32 : 0;
+            J.P = jobs[i].solid->view;
+            J.ca.prec = pl->prec;
+            J.ca.cull = opts.cull;
+            J.ca.ty = opts.tile_y > 0 ? opts.tile_y : kTileY;
+            J.ca.tz = opts.tile_z > 0 ? opts.tile_z : kTileZ;
+            J.ca.ntx = (nx + 31) / 32;
+            J.ca.nty = (ny + J.ca.ty - 1) / J.ca.ty;
+            J.ca.ntz = (nz + J.ca.tz - 1) / J.ca.tz;
+            J.nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)J.g.CX * (ny - 1) * (nz - 1) : 0;
+            J.iters = jobs[i].iters;
+            J.inv_dl = nx >= 2 ? 1.0 / (X[1] - X[0]) : 0.0;
+            Lay L{};
+            L.xd = gd.size();
+            gd.insert(gd.end(), X.begin(), X.end());
+            L.yd = gd.size();
+            gd.insert(gd.end(), Y.begin(), Y.end());
+            L.zd = gd.size();
+            gd.insert(gd.end(), Z.begin(), Z.end());
+            L.xf = gf.size();
+            gf.insert(gf.end(), X.begin(), X.end());
+            L.yf = gf.size();
+            gf.insert(gf.end(), Y.begin(), Y.end());
+            L.zf = gf.size();
+            gf.insert(gf.end(), Z.begin(), Z.end());
+            L.nbits = (size_t)nz * ny * J.g.W;
+            L.bits = nbits_total;
+            nbits_total += L.nbits;
+            L.items = (long long)J.ca.nty * J.ca.ntz;
+            L.cost = (long long)nx * ny * nz;
+            const int nw = (J.P.n_leaves + 31) / 32;
+            fold_words = std::max(fold_words, (J.P.fold_cap + 2 * nw + 3) & ~3);
+            lay.push_back(L);
+            pl->hjobs.push_back(J);
+        }
+        const int nd = (int)pl->hjobs.size();
+        pl->fold_words = fold_words;
+        // Device buffers.
+        const size_t gd_bytes = gd.size() * 8, gf_off = align256(gd_bytes);
+        CK(pl->grid.ensure(gf_off + gf.size() * 4 + 8));
+        CK(pl->bits.ensure(std::max<size_t>(nbits_total, 1) * 4));
+        CK(pl->errs.ensure(std::max(nd, 1) * ER_N * 4));
+        CK(pl->stats.ensure(ST_N * 8));
+        CK(pl->totals.ensure(16));
+        CK(pl->vbase.ensure((nd + 1) * 8));
+        CK(pl->tbase.ensure((nd + 1) * 8));
+        unsigned char* gbase = (unsigned char*)pl->grid.p;
+        for (int d = 0; d < nd; d++) {
+            JobD& J = pl->hjobs[d];
+            const Lay& L = lay[d];
+            J.g.xs = (const double*)(gbase) + L.xd;
+            J.g.ys = (const double*)(gbase) + L.yd;
+            J.g.zs = (const double*)(gbase) + L.zd;
+            J.ca.xf = (const float*)(gbase + gf_off) + L.xf;
+            J.ca.yf = (const float*)(gbase + gf_off) + L.yf;
+            J.ca.zf = (const float*)(gbase + gf_off) + L.zf;
+            J.ca.bits = pl->bits.as<uint32_t>() + L.bits;
+            J.ca.err = pl->errs.as<int>() + d * ER_N;
+            J.ca.stats = pl->stats.as<unsigned long long>();
+            J.ca.work = nullptr;
+        }
+        // Schedule: classify items of the largest jobs first.
+        std::vector<int> order(nd);
+        for (int d = 0; d < nd; d++) order[d] = d;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return lay[x].cost > lay[y].cost; });
+        std::vector<long long> sched_off(std::max(nd, 1), 0);
+        std::vector<int> sched_job(std::max(nd, 1), 0);
+        long long acc = 0;
+        for (int k = 0; k < nd; k++) {
+            sched_off[k] = acc;
+            sched_job[k] = order[k];
+            acc += lay[order[k]].items;
+        }
+        pl->nitems = acc;
+        pl->hchunk_offs.assign(nd + 1, 0);
+        for (int d = 0; d < nd; d++) {
+            pl->hjobs[d].chunk_off = pl->hchunk_offs[d];
+            pl->hchunk_offs[d + 1] = pl->hchunk_offs[d] + pl->hjobs[d].nchunks;
+        }
+        pl->nchunks = pl->hchunk_offs[nd];
+        pl->nblk = (int)((pl->nchunks + 255) / 256);
+        CK(pl->jobs.ensure(std::max(nd, 1) * sizeof(JobD)));
+        CK(pl->sched_off.ensure(sched_off.size() * 8));
+        CK(pl->sched_job.ensure(sched_job.size() * 4));
+        CK(pl->chunk_offs.ensure((nd + 1) * 8));
+        if (pl->nchunks > 0) {
+            CK(pl->packed.ensure(pl->nchunks * 4));
+            CK(pl->blocksum.ensure((size_t)pl->nblk * 8));
+            CK(pl->blockoff.ensure((size_t)pl->nblk * 16));
+            CK(pl->prefv.ensure(pl->nchunks * 4));
+            CK(pl->preft.ensure(pl->nchunks * 4));
+        }
+        CK(cudaMemcpyAsync(pl->grid.p, gd.data(), gd_bytes, cudaMemcpyHostToDevice, sm));
+        CK(cudaMemcpyAsync(gbase + gf_off, gf.data(), gf.size() * 4, cudaMemcpyHostToDevice, sm));
+        if (nd) CK(cudaMemcpyAsync(pl->jobs.p, pl->hjobs.data(), nd * sizeof(JobD), cudaMemcpyHostToDevice, sm));
+        CK(cudaMemcpyAsync(pl->sched_off.p, sched_off.data(), sched_off.size() * 8, cudaMemcpyHostToDevice, sm));
+        CK(cudaMemcpyAsync(pl->sched_job.p, sched_job.data(), sched_job.size() * 4, cudaMemcpyHostToDevice, sm));
+        CK(cudaMemcpyAsync(pl->chunk_offs.p, pl->hchunk_offs.data(), (nd + 1) * 8, cudaMemcpyHostToDevice, sm));
+        CK(cudaStreamSynchronize(sm));  // host vectors die at scope end
+        pl->smem_c = (size_t)8 * fold_words * 4;
+        pl->smem_s = (size_t)4 * fold_words * 4;
+        auto kcb = pl->prec == MC_PREC_FP64 ? k_classify_batch<MC_PREC_FP64> : k_classify_batch<MC_PREC_FP32_FILTERED>;
+        auto ksb = pl->prec == MC_PREC_FP64 ? k_search_batch<MC_PREC_FP64> : k_search_batch<MC_PREC_FP32_FILTERED>;
+        if (pl->smem_c > 48 * 1024) CK(cudaFuncSetAttribute(kcb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl->smem_c));
+        if (pl->smem_s > 48 * 1024) CK(cudaFuncSetAttribute(ksb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl->smem_s));
+        int occ = 1;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kcb, 256, pl->smem_c));
+        pl->grid_c = std::max(1, ctx->sm_count * std::max(occ, 1));
+        pl->grid_s = ctx->sm_count * 16;
+    }
+    const int nd = (int)pl->hjobs.size();
+    BatchArgs ba{};
+    ba.jobs = pl->jobs.as<JobD>();
+    ba.njobs = nd;
+    ba.sched_off = pl->sched_off.as<long long>();
+    ba.sched_job = pl->sched_job.as<int>();
+    ba.nitems = pl->nitems;
+    ba.chunk_offs = pl->chunk_offs.as<long long>();
+    ba.nchunks = pl->nchunks;
+    ba.vbase = pl->vbase.as<unsigned long long>();
+    ba.tbase = pl->tbase.as<unsigned long long>();
+    ba.totals = pl->totals.as<unsigned long long>();
+    ba.work = (unsigned int*)(pl->stats.as<unsigned long long>() + ST_WORK);
+    ba.stats = pl->stats.as<unsigned long long>();
+    ba.fold_words = pl->fold_words;
+    ba.cull = opts.cull;
+    auto kcb = pl->prec == MC_PREC_FP64 ? k_classify_batch<MC_PREC_FP64> : k_classify_batch<MC_PREC_FP32_FILTERED>;
+    auto ksb = pl->prec == MC_PREC_FP64 ? k_search_batch<MC_PREC_FP64> : k_search_batch<MC_PREC_FP32_FILTERED>;
+    auto front = [&]() -> cudaError_t {
+        cudaMemsetAsync(pl->stats.p, 0, ST_N * 8, sm);
+        cudaMemsetAsync(pl->errs.p, 0, std::max(nd, 1) * ER_N * 4, sm);
+        cudaMemsetAsync(pl->totals.p, 0, 16, sm);
+        cudaMemsetAsync(pl->bits.p, 0, pl->bits.cap, sm);
+        if (nd > 0) kcb<<<pl->grid_c, 256, pl->smem_c, sm>>>(ba);
+        if (pl->nchunks > 0) {
+            k_count_batch<<<pl->nblk, 256, 0, sm>>>(ba, pl->packed.as<uint32_t>(), pl->blocksum.as<uint32_t>());
+            k_scan_blocks<<<1, 1024, 0, sm>>>(pl->blocksum.as<uint32_t>(), pl->blockoff.as<unsigned long long>(),
+                                              pl->nblk, ba.totals);
+            k_scan_chunks<<<pl->nblk, 256, 0, sm>>>(pl->packed.as<uint32_t>(), pl->blockoff.as<unsigned long long>(),
+                                                    pl->nchunks, pl->prefv.as<uint32_t>(), pl->preft.as<uint32_t>());
+        }
+        k_job_bases<<<(nd + 256) / 256, 256, 0, sm>>>(ba, pl->prefv.as<uint32_t>(), pl->preft.as<uint32_t>());
+        return cudaGetLastError();
+    };
+    auto back = [&]() -> cudaError_t {
+        if (pl->nchunks > 0)
+            k_emit_batch<<<pl->nblk, 256, 0, sm>>>(ba, pl->packed.as<uint32_t>(), pl->prefv.as<uint32_t>(),
+                                                   pl->preft.as<uint32_t>(), pl->keys.as<unsigned long long>(),
+                                                   pl->tris.as<int32_t>());
+        if (nd > 0) ksb<<<pl->grid_s, 128, pl->smem_s, sm>>>(ba, pl->keys.as<unsigned long long>(), pl->verts.as<double>());
+        return cudaGetLastError();
+    };
+    std::vector<int> herr(std::max(nd, 1) * ER_N);
+    std::vector<unsigned long long> hvb(nd + 1), htb(nd + 1), htot(2), hstats(ST_N);
+    auto readback = [&]() -> cudaError_t {
+        cudaMemcpyAsync(htot.data(), pl->totals.p, 16, cudaMemcpyDeviceToHost, sm);
+        cudaMemcpyAsync(herr.data(), pl->errs.p, herr.size() * 4, cudaMemcpyDeviceToHost, sm);
+        cudaMemcpyAsync(hvb.data(), pl->vbase.p, (nd + 1) * 8, cudaMemcpyDeviceToHost, sm);
+        cudaMemcpyAsync(htb.data(), pl->tbase.p, (nd + 1) * 8, cudaMemcpyDeviceToHost, sm);
+        cudaMemcpyAsync(hstats.data(), pl->stats.p, ST_N * 8, cudaMemcpyDeviceToHost, sm);
+        return cudaStreamSynchronize(sm);
+    };
+    float ms_total = 0;
+    bool ran = false;
+    if (pl->exec) {
+        CK(cudaEventRecord(ctx->ev[0], sm));
+        CK(cudaGraphLaunch(pl->exec, sm));
+        CK(cudaEventRecord(ctx->ev[4], sm));
+        CK(readback());
+        cudaEventElapsedTime(&ms_total, ctx->ev[0], ctx->ev[4]);
+        ran = (long long)htot[0] <= pl->cap_V && (long long)htot[1] <= pl->cap_T;
+    }
+    if (!ran) {
+        // Sizing run: read the totals back, size the outputs, finish, then
+        // capture the whole pipeline in a graph for the next identical call.
+        CK(cudaEventRecord(ctx->ev[0], sm));
+        CK(front());
+        CK(readback());
+        const long long V = (long long)htot[0], T = (long long)htot[1];
+        if (V >= ((long long)1 << 31) || T >= ((long long)1 << 31))
+            return fail(ctx, MC_ERR_LIMIT, "batch exceeds 2^31 vertices or triangles");
+        CK(pl->keys.ensure(std::max<long long>(V, 1) * 8));
+        CK(pl->verts.ensure(std::max<long long>(V, 1) * 24));
+        CK(pl->tris.ensure(std::max<long long>(T, 1) * 12));
+        CK(back());
+        CK(cudaEventRecord(ctx->ev[4], sm));
+        CK(readback());
+        cudaEventElapsedTime(&ms_total, ctx->ev[0], ctx->ev[4]);
+        pl->cap_V = (long long)(pl->keys.cap / 8);
+        pl->cap_T = (long long)(pl->tris.cap / 12);
+        if (pl->exec) {
+            cudaGraphExecDestroy(pl->exec);
+            pl->exec = nullptr;
+        }
+        cudaGraph_t graph = nullptr;
+        if (cudaStreamBeginCapture(sm, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            cudaError_t e1 = front(), e2 = back();
+            cudaError_t e3 = cudaStreamEndCapture(sm, &graph);
+            if (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess && graph) {
+                if (cudaGraphInstantiate(&pl->exec, graph, 0) != cudaSuccess) pl->exec = nullptr;
+            }
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+        }
+    }
+    // Outputs: one copy of the concatenated mesh, then split per job.
+    const long long V = (long long)htot[0], T = (long long)htot[1];
+    const size_t bytes = (size_t)V * 24 + (size_t)T * 12 + 16;
+    if (pl->h_stage_bytes < bytes) {
+        if (pl->h_stage) cudaFreeHost(pl->h_stage);
+        pl->h_stage = nullptr;
+        pl->h_stage_bytes = 0;
+        CK(cudaHostAlloc((void**)&pl->h_stage, bytes + bytes / 4, cudaHostAllocDefault));
+        pl->h_stage_bytes = bytes + bytes / 4;
+    }
+    double* hv = (double*)pl->h_stage;
+    int32_t* ht = (int32_t*)(hv + 3 * V);
+    if (V) CK(cudaMemcpyAsync(hv, pl->verts.p, V * 24, cudaMemcpyDeviceToHost, sm));
+    if (T) CK(cudaMemcpyAsync(ht, pl->tris.p, T * 12, cudaMemcpyDeviceToHost, sm));
+    CK(cudaStreamSynchronize(sm));
     mc_status first = MC_OK;
     for (size_t i = 0; i < n; i++) {
-        mc_status s = mc_search(ctx, jobs[i].solid, jobs[i].delta, jobs[i].iters, opts, &outs[i]);
-        if (job_status) job_status[i] = s;
-        if (s != MC_OK && first == MC_OK) first = s;
+        mc_status st = pl->pre_status[i];
+        const int d = pl->dev_job[i];
+        if (st == MC_OK && d >= 0) {
+            const int* e = &herr[d * ER_N];
+            st = e[ER_BORDER] ? MC_ERR_BOUNDS_INSIDE
+                              : e[ER_NOT_ON_EDGE] ? MC_ERR_NOT_ON_EDGE
+                                                  : e[ER_EDGE_INDEX] ? MC_ERR_EDGE_INDEX : e[ER_LIMIT] ? MC_ERR_LIMIT : MC_OK;
+        }
+        if (job_status) job_status[i] = st;
+        if (st != MC_OK) {
+            if (first == MC_OK) first = st;
+            continue;
+        }
+        const JobD& J = pl->hjobs[d];
+        const long long v0 = (long long)hvb[d], nv = (long long)(hvb[d + 1] - hvb[d]);
+        const long long t0 = (long long)htb[d], nt = (long long)(htb[d + 1] - htb[d]);
+        mc_mesh& m = outs[i];
+        m.vertices = (double*)std::malloc(std::max<long long>(nv, 1) * 24);
+        m.triangles = (int32_t*)std::malloc(std::max<long long>(nt, 1) * 12);
+        if (!m.vertices || !m.triangles) {
+            mc_mesh_free(&m);
+            return fail(ctx, MC_ERR_OOM, "host allocation failed");
+        }
+        if (nv) std::memcpy(m.vertices, hv + 3 * v0, nv * 24);
+        if (nt) std::memcpy(m.triangles, ht + 3 * t0, nt * 12);
+        m.n_vertices = nv;
+        m.n_triangles = nt;
+        m.stats.nx = J.g.nx;
+        m.stats.ny = J.g.ny;
+        m.stats.nz = J.g.nz;
+        m.stats.corners = (int64_t)J.g.nx * J.g.ny * J.g.nz;
+        m.stats.vertices = nv;
+        m.stats.triangles = nt;
+        m.stats.leaf_evals = (int64_t)hstats[ST_LEAF];
+        m.stats.escalations = (int64_t)hstats[ST_ESC];
+        m.stats.tiles_const = (int64_t)hstats[ST_TILES_CONST];
+        m.stats.ms_total = ms_total;
+        m.stats.d2h_bytes = nv * 24 + nt * 12;
     }
+    if (first != MC_OK) fail(ctx, first, "a batch job failed");
     return first;
 }
 

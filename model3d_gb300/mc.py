@@ -178,6 +178,40 @@ def MarchingCubesSearch(solid, delta: float, iters: int, *, precision: str = "fp
     return Mesh(verts, tris, stats)
 
 
+def MarchingCubesSearchBatch(jobs, *, precision: str = "fp32", cull: bool = True,
+                             ctx: Optional[Context] = None, tile_y: int = 0, tile_z: int = 0):
+    """Many MarchingCubesSearch calls in one batched launch (mc_search_batch).
+
+    jobs: sequence of (solid or DeviceSolid, delta, iters).  Returns a list
+    with a Mesh per job, or the MCError of a job that failed.  Repeating the
+    same batch replays a captured CUDA graph."""
+    ctx = ctx or default_context()
+    dss = [_as_device_solid(s, ctx) for s, _, _ in jobs]
+    arr = (N.MCJob * max(1, len(jobs)))()
+    for i, (ds, (_, d, it)) in enumerate(zip(dss, jobs)):
+        arr[i].solid = ds.ptr.value
+        arr[i].delta = float(d)
+        arr[i].iters = int(it)
+    outs = (N.MCMesh * max(1, len(jobs)))()
+    status = (ctypes.c_int * max(1, len(jobs)))()
+    o = _opts(precision, cull, tile_y, tile_z)
+    st = N.lib().mc_search_batch(ctx.ptr, arr, len(jobs), ctypes.byref(o), outs, status)
+    res = []
+    for i in range(len(jobs)):
+        if status[i] != N.MC_OK:
+            res.append(MCError(status[i]))
+            continue
+        m = outs[i]
+        V, T = m.n_vertices, m.n_triangles
+        verts = np.ctypeslib.as_array(m.vertices, shape=(max(V, 1) * 3,))[:V * 3].reshape(V, 3).copy()
+        tris = np.ctypeslib.as_array(m.triangles, shape=(max(T, 1) * 3,))[:T * 3].reshape(T, 3).copy()
+        res.append(Mesh(verts, tris, m.stats.as_dict()))
+        N.lib().mc_mesh_free(ctypes.byref(m))
+    if st != N.MC_OK and all(not isinstance(r, MCError) for r in res):
+        raise MCError(st, N.lib().mc_last_error(ctx.ptr).decode())
+    return res
+
+
 def MarchingCubes(solid, delta: float, **kw) -> Mesh:
     """model3d.MarchingCubes (model3d/mc.go:14-37): the search with iters=0."""
     return MarchingCubesSearch(solid, delta, 0, **kw)
