@@ -199,6 +199,9 @@ def run_ours(args):
             sts.append(step(prec))
         return sts
 
+    # Tile shape chosen by the library's autotuner (outside the timed region).
+    from model3d_gb300 import autotune, measure_peaks
+    tuned = autotune(ds, DELTA, ITERS, ctx=ctx)
     for _ in range(args.warmup):
         step(N.MC_PREC_FP32_FILTERED)
         step(N.MC_PREC_FP64)
@@ -259,6 +262,9 @@ def run_ours(args):
     peaks, kind = measured_peaks()
     roof = roofline(dom, phases[dom], sts[0], peaks, kind)
 
+    others = {} if args.no_extra else other_configs(ctx, torch, flush, value)
+    pk = measure_peaks(ctx)
+
     if rank == 0:
         cpu = None
         if ws == 1 and not args.no_cpu:
@@ -289,6 +295,9 @@ def run_ours(args):
             "phases_ms": phases,
             "gpu_launches": 6 * args.steps,
             "roofline": roof,
+            "tiles": {"tile_y": tuned[0], "tile_z": tuned[1], "chosen_by": "mc_autotune"},
+            "measured_peaks_this_gpu": {"fp32_tflops": pk[0], "fp64_tflops": pk[1], "l2_read_gbs": pk[2]},
+            "other_configs": others,
             "clocks": clk.summary(),
             "wall_s_timed_region": wall,
             "e2e": {"value": corners / e2e_s, "unit": "corners/s",
@@ -299,6 +308,87 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _device_rate(L, N, ctx, ds, delta, iters, prec, flush, torch, reps=3):
+    import ctypes
+    o = N.MCOpts()
+    o.precision = prec
+    o.cull = 1
+    V, T = ctypes.c_int64(), ctypes.c_int64()
+    best = None
+    for _ in range(reps + 1):
+        flush.zero_()
+        torch.cuda.synchronize()
+        st = N.MCStats()
+        if L.mc_search_device(ctx.ptr, ds.ptr, delta, iters, ctypes.byref(o), ctypes.byref(V),
+                              ctypes.byref(T), ctypes.byref(st)) != 0:
+            raise RuntimeError(L.mc_last_error(ctx.ptr).decode())
+        d = st.as_dict()
+        if best is None or d["ms_total"] < best["ms_total"]:
+            best = d
+    return best
+
+
+def other_configs(ctx, torch, flush, single_rate):
+    """The other benchmark configurations, device time (CUDA events, best of 3
+    after a warm-up): unit sphere (delta 0.01), the 1,048,820-triangle
+    displaced icosphere collider on a ~256^3 grid, and 512 CSG solids in one
+    batched launch (graph replay) next to the same solids one call at a time."""
+    import ctypes
+    from model3d_gb300 import (DeviceSolid, MarchingCubesSearchBatch, MeshToCollider,
+                               NewColliderSolid, Sphere, XYZ)
+    from model3d_gb300 import _native as N
+    from model3d_gb300.workloads import csg_batch, displaced_icosphere
+    L = N.lib()
+    out = {}
+    sph = DeviceSolid(Sphere(XYZ(0, 0, 0), 1.0), ctx)
+    a = _device_rate(L, N, ctx, sph, 0.01, 8, N.MC_PREC_FP32_FILTERED, flush, torch)
+    b = _device_rate(L, N, ctx, sph, 0.01, 8, N.MC_PREC_FP64, flush, torch)
+    out["sphere_r1_delta0.01"] = {"corners": a["corners"], "triangles": a["triangles"],
+                                  "fp32_corners_per_s": a["corners"] / (a["ms_total"] / 1e3),
+                                  "fp64_corners_per_s": b["corners"] / (b["ms_total"] / 1e3),
+                                  "ms_fp32": a["ms_total"], "ms_fp64": b["ms_total"]}
+    tris = displaced_icosphere(229)
+    col = NewColliderSolid(MeshToCollider(tris))
+    mn, mx = col.Min(), col.Max()
+    d = max(mx.X - mn.X, mx.Y - mn.Y, mx.Z - mn.Z) / 255
+    t0 = time.perf_counter()
+    cds = DeviceSolid(col, ctx)
+    lower_s = time.perf_counter() - t0
+    a = _device_rate(L, N, ctx, cds, d, 8, N.MC_PREC_FP32_FILTERED, flush, torch, reps=2)
+    b = _device_rate(L, N, ctx, cds, d, 8, N.MC_PREC_FP64, flush, torch, reps=1)
+    tests = a["bvh_nodes"] + a["bvh_tris"]
+    out["collider_icosphere_1048820_tris_256cubed"] = {
+        "grid": [a["nx"], a["ny"], a["nz"]], "triangles_in": len(tris), "triangles_out": a["triangles"],
+        "fp32_corners_per_s": a["corners"] / (a["ms_total"] / 1e3),
+        "fp64_corners_per_s": b["corners"] / (b["ms_total"] / 1e3),
+        "ms_fp32": a["ms_total"], "ms_fp64": b["ms_total"],
+        "escalation_rate": a["escalations"] / max(1, tests), "bvh_box_tests": a["bvh_nodes"],
+        "triangle_tests": a["bvh_tris"], "host_lowering_s": lower_s}
+    items = csg_batch(2024, count=512)
+    jobs = [(DeviceSolid(s, ctx), dd, 8) for s, dd in items]
+    res = {}
+    for prec in ("fp32", "fp64"):
+        ms = []
+        for _ in range(4):
+            m = MarchingCubesSearchBatch(jobs, precision=prec, ctx=ctx)
+            ms.append(m[0].stats["ms_total"])
+        res[prec] = (min(ms[1:]), sum(x.stats["corners"] for x in m), sum(x.NumTriangles() for x in m))
+    seq = 0.0
+    for ds_, dd, it in jobs:
+        seq += _device_rate(L, N, ctx, ds_, dd, it, N.MC_PREC_FP32_FILTERED, flush, torch, reps=0)["ms_total"]
+    corners = res["fp32"][1]
+    out["batch_512_csg"] = {
+        "jobs": len(jobs), "corners": corners, "triangles": res["fp32"][2],
+        "fp32_corners_per_s": corners / (res["fp32"][0] / 1e3),
+        "fp32_meshes_per_s": len(jobs) / (res["fp32"][0] / 1e3),
+        "fp64_corners_per_s": corners / (res["fp64"][0] / 1e3),
+        "ms_fp32_graph_replay": res["fp32"][0], "ms_fp64_graph_replay": res["fp64"][0],
+        "sequential_single_calls_ms": seq,
+        "batched_over_sequential": seq / res["fp32"][0],
+        "fraction_of_single_large_solid_rate": (corners / (res["fp32"][0] / 1e3)) / single_rate}
+    return out
 
 
 def roofline(kernel, ms, st, peaks, kind):
@@ -331,6 +421,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -234,6 +234,22 @@ typedef struct mc_job {
 mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_opts* opts,
                           mc_mesh* outs, mc_status* job_status);
 
+/* Autotuner for the corner-tile shape of the classification kernel: times
+ * every candidate (tile_y, tile_z) on this solid and grid (CUDA events, best
+ * of three), keeps the fastest in the context — later calls on the context
+ * that leave tile_y / tile_z at 0 use it — and returns it in *best (may be
+ * NULL) with its classification time in *best_ms (may be NULL).  Tuning
+ * knob only: results are identical for every shape.  No counterpart in the
+ * reference (its z-slab ring has no tile shape). */
+mc_status mc_autotune(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters,
+                      const mc_opts* opts, mc_opts* best, double* best_ms);
+
+/* Roofline denominators for this path on the context's GPU, measured with
+ * micro-kernels: FP32 and FP64 FMA throughput (TFLOP/s, 2 flops per FMA)
+ * and the read bandwidth of a buffer resident in L2 (GB/s).  Any output may
+ * be NULL.  Measurement utility; no counterpart in the reference. */
+mc_status mc_measure_peaks(mc_ctx* ctx, double* fp32_tflops, double* fp64_tflops, double* l2_read_gbs);
+
 /* The 256-case lookup table the library uses (mcLookupTable,
  * model3d/mc.go:434-456): counts[c] triangles for case c, each as three
  * corner pairs tris[c][t][0..5]. */

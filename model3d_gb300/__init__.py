@@ -15,6 +15,7 @@ from .solids import (Capsule, CacheSolidBounds, ColliderSolid, Cylinder, ForceSo
                      TranslateSolid, VecScale, VecScaleSolid, serialize)
 from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesSearch,
                  MarchingCubesSearchBatch, MCError,
-                 Mesh, canonical, case_table, default_context, spacer_axis)
+                 Mesh, autotune, canonical, case_table, default_context, measure_peaks,
+                 spacer_axis)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -34,7 +34,8 @@ EXPORTS = [
     "mc_status_string", "mc_last_error", "mc_create", "mc_destroy", "mc_solid_create",
     "mc_solid_destroy", "mc_solid_bounds", "mc_spacer_axis", "mc_search", "mc_mesh_free",
     "mc_search_device", "mc_result_device", "mc_result_copy", "mc_contains", "mc_search_batch",
-    "mc_case_table", "mc_version", "mc_search_noalloc",
+    "mc_case_table", "mc_version", "mc_search_noalloc", "mc_autotune",
+    "mc_measure_peaks",
 ]
 
 
@@ -115,6 +116,9 @@ def lib():
         L.mc_search_batch.argtypes = [vp, ctypes.POINTER(MCJob), ctypes.c_size_t,
                                       ctypes.POINTER(MCOpts), ctypes.POINTER(MCMesh), vp]
         L.mc_case_table.argtypes = [vp, vp]
+        L.mc_measure_peaks.argtypes = [vp, ctypes.POINTER(dbl), ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
+        L.mc_autotune.argtypes = [vp, vp, dbl, i32, ctypes.POINTER(MCOpts), ctypes.POINTER(MCOpts),
+                                  ctypes.POINTER(dbl)]
         L.mc_search_noalloc.argtypes = [vp, ctypes.c_size_t, dbl, i32, ctypes.POINTER(MCOpts), vp,
                                         vp, i64, vp, i64, ctypes.POINTER(i64), ctypes.POINTER(i64)]
         for name in EXPORTS:

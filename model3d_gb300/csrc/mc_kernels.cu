@@ -1043,6 +1043,7 @@ __global__ void __launch_bounds__(256) k_emit(GridView g, EmitArgs a) {
 
 struct SearchArgs {
     double inv_dl;  // 1 / (xs[1] - xs[0])
+    const uint32_t* bits;  // the classification's corner bits
     const unsigned long long* keys;
     double* verts;  // V x 3
     long long nverts;
@@ -1053,6 +1054,14 @@ struct SearchArgs {
     unsigned long long* stats;
 };
 
+__device__ __forceinline__ float warp_minf(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_maxf(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
 __device__ __forceinline__ double warp_min(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
@@ -1072,16 +1081,45 @@ __device__ __forceinline__ double warp_max(double v) {
 // reference's exact fmod and IEEE division decide.
 // Returns 0 (found), 1 ("vertex not on edge") or 2 (index out of range).
 __device__ __forceinline__ int lookup_edge(const GridView& g, const P3& c, double inv_dl, int* axis, double* lo,
-                                           double* hi) {
+                                           double* hi, long long* idx_out) {
     const double org[3] = {g.xs[0], g.ys[0], g.zs[0]};
     const double* vals[3] = {g.xs, g.ys, g.zs};
     const int nvals[3] = {g.nx, g.ny, g.nz};
     const double dl = D_SUB(g.xs[1], g.xs[0]);
     for (int i = 0; i < 3; i++) {
-        const double av = D_SUB(comp(c, i), org[i]);
-        const double q = D_MUL(av, inv_dl);
+        const double ci = comp(c, i);
         int band = -1;  // -1 undecided, 0 outside, 1 inside
         long long idx = 0;
+        // FP32 stage: |qf - q_exact| <= u(|c| + |o|)/dl + 3u qf < 2e-3 when
+        // the coordinates are below 2^12 delta (checked), so a fractional
+        // part farther than 2e-3 from 1/4, 3/4 and the integers decides.
+        {
+            const float cf = (float)ci, of = (float)org[i], idl = (float)inv_dl;
+            const float qf = (cf - of) * idl;
+            const float bnd = (fabsf(cf) + fabsf(of)) * idl;
+            if (qf >= 0.f && qf < 4096.f && bnd < 4096.f) {
+                const float nf = floorf(qf), fr = qf - nf;
+                if (fr > 0.252f && fr < 0.748f) {
+                    band = 1;
+                    idx = (long long)nf;
+                } else if (fr < 0.248f || fr > 0.752f) {
+                    band = 0;
+                }
+            }
+        }
+        if (band >= 0) {
+            if (band) {
+                if (idx < 0 || idx + 1 >= nvals[i]) return 2;
+                *axis = i;
+                *lo = vals[i][idx];
+                *hi = vals[i][idx + 1];
+                *idx_out = idx;
+                return 0;
+            }
+            continue;
+        }
+        const double av = D_SUB(ci, org[i]);
+        const double q = D_MUL(av, inv_dl);
         if (av >= 0 && q < 16777216.0) {
             const double n = floor(q);
             const double fr = D_SUB(q, n);
@@ -1102,6 +1140,7 @@ __device__ __forceinline__ int lookup_edge(const GridView& g, const P3& c, doubl
             *axis = i;
             *lo = vals[i][idx];
             *hi = vals[i][idx + 1];
+            *idx_out = idx;
             return 0;
         }
     }
@@ -1110,8 +1149,8 @@ __device__ __forceinline__ int lookup_edge(const GridView& g, const P3& c, doubl
 
 // Vertex setup: edge key -> midpoint (corners[a].Mid(corners[b]),
 // mc.go:401-407) and, when iters != 0, LookupEdgePoint.  Returns the status.
-__device__ __forceinline__ int vertex_setup(const GridView& g, unsigned long long key, int iters, double inv_dl,
-                                            P3* cpt, int* axis, double* lo, double* hi) {
+__device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* bits, unsigned long long key, int iters,
+                                            double inv_dl, P3* cpt, int* axis, double* lo, double* hi, int* hi_bit) {
     const int ax = (int)(key >> 60);
     const int z = (int)((key >> 40) & 0xfffff), y = (int)((key >> 20) & 0xfffff), x = (int)(key & 0xfffff);
     const P3 c0{g.xs[x], g.ys[y], g.zs[z]};
@@ -1119,17 +1158,33 @@ __device__ __forceinline__ int vertex_setup(const GridView& g, unsigned long lon
     if (ax == 0) c1.x = g.xs[x + 1];
     else if (ax == 1) c1.y = g.ys[y + 1];
     else c1.z = g.zs[z + 1];
-    *cpt = P3{D_MUL(D_ADD(c0.x, c1.x), 0.5), D_MUL(D_ADD(c0.y, c1.y), 0.5), D_MUL(D_ADD(c0.z, c1.z), 0.5)};
+    // (v + v) * 0.5 == v exactly unless v + v overflows (|v| >= 2^1023), so
+    // off the edge axis the midpoint is the grid value itself.
+    auto mid = [](double a, double b, bool same) {
+        const bool big = ((unsigned long long)__double_as_longlong(a) & 0x7ff0000000000000ull) >= 0x7fe0000000000000ull;
+        return (same && !big) ? a : D_MUL(D_ADD(a, b), 0.5);
+    };
+    *cpt = P3{mid(c0.x, c1.x, ax != 0), mid(c0.y, c1.y, ax != 1), mid(c0.z, c1.z, ax != 2)};
     *axis = 0;
+    *hi_bit = -1;
     if (iters == 0) return 0;
-    return lookup_edge(g, *cpt, inv_dl, axis, lo, hi);
+    long long idx = -1;
+    const int st = lookup_edge(g, *cpt, inv_dl, axis, lo, hi, &idx);
+    // The first Contains of the bisection is at `hi`; when LookupEdgePoint
+    // found this vertex's own edge that is grid corner (index + 1 along the
+    // axis), whose bit the classification already wrote.
+    if (st == 0 && bits && *axis == ax && idx == (ax == 0 ? x : (ax == 1 ? y : z))) {
+        const int cx = x + (ax == 0), cy = y + (ax == 1), cz = z + (ax == 2);
+        *hi_bit = (int)((bits[((size_t)cz * g.ny + cy) * g.W + (cx >> 5)] >> (cx & 31)) & 1u);
+    }
+    return st;
 }
 
 // mcSearchPoint (mc.go:223-258) against a (folded) program; only the axis
 // coordinate moves, so the float point is updated in place.
 template <int PREC>
 __device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, int len, P3 cpt, int axis, double lo,
-                                     double hi, int iters, Counts& cnt, int* err) {
+                                     double hi, int iters, int hi_bit, Counts& cnt, int* err) {
     F3 pf = to_f3(cpt);
     auto contains = [&](P3 pt, double v) -> bool {
         if (len == FOLD_FALSE) return false;
@@ -1143,7 +1198,7 @@ __device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, in
     double fp = lo, tp = hi;
     P3 t = cpt;
     set_comp(t, axis, tp);
-    if (!contains(t, tp)) {
+    if (!(hi_bit >= 0 ? hi_bit == 1 : contains(t, tp))) {
         fp = hi;
         tp = lo;
     }
@@ -1168,13 +1223,15 @@ __device__ __forceinline__ void search_cull(const ProgView& P, bool work, const 
     const int nw = (P.n_leaves + 31) >> 5;
     float blo[3], bhi[3];
     for (int i = 0; i < 3; i++) {
-        double vlo = work ? comp(cpt, i) : CUDART_INF, vhi = work ? comp(cpt, i) : -CUDART_INF;
-        if (work && i == axis) {
-            vlo = fmin(lo, hi);
-            vhi = fmax(lo, hi);
+        float vlo = CUDART_INF_F, vhi = -CUDART_INF_F;
+        if (work) {
+            const double a = i == axis ? (lo < hi ? lo : hi) : comp(cpt, i);
+            const double b = i == axis ? (lo < hi ? hi : lo) : a;
+            vlo = __double2float_rd(a);
+            vhi = __double2float_ru(b);
         }
-        blo[i] = __double2float_rd(warp_min(vlo));
-        bhi[i] = __double2float_ru(warp_max(vhi));
+        blo[i] = warp_minf(vlo);
+        bhi[i] = warp_maxf(vhi);
     }
     uint32_t diff = 0, any = 0;
     for (int k = 0; k < nw; k++) {
@@ -1230,13 +1287,14 @@ __global__ void __launch_bounds__(128, 4) k_search(GridView g, ProgView P, Searc
         int axis = 0;
         double lo = 0, hi = 0;
         P3 cpt{0, 0, 0};
-        int status = live ? vertex_setup(g, a.keys[v], a.iters, a.inv_dl, &cpt, &axis, &lo, &hi) : 0;
+        int hi_bit = -1;
+        int status = live ? vertex_setup(g, a.bits, a.keys[v], a.iters, a.inv_dl, &cpt, &axis, &lo, &hi, &hi_bit) : 0;
         if (status == 1) atomicOr(&a.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&a.err[ER_EDGE_INDEX], 1);
         const bool work = live && a.iters != 0 && status == 0;
         if (a.cull && __any_sync(0xffffffffu, work)) search_cull(P, work, cpt, axis, lo, hi, q, cur, prev, have_prev, prog, len);
         if (live && status == 0) {
-            const P3 out = work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, a.iters, cnt, a.err) : cpt;
+            const P3 out = work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, a.iters, hi_bit, cnt, a.err) : cpt;
             a.verts[3 * v] = out.x;
             a.verts[3 * v + 1] = out.y;
             a.verts[3 * v + 2] = out.z;
@@ -1391,7 +1449,9 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
         int axis = 0;
         double lo = 0, hi = 0;
         P3 cpt{0, 0, 0};
-        const int status = live ? vertex_setup(Jp->g, keys[v], Jp->iters, Jp->inv_dl, &cpt, &axis, &lo, &hi) : 0;
+        int hi_bit = -1;
+        const int status =
+            live ? vertex_setup(Jp->g, Jp->ca.bits, keys[v], Jp->iters, Jp->inv_dl, &cpt, &axis, &lo, &hi, &hi_bit) : 0;
         if (status == 1) atomicOr(&Jp->ca.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&Jp->ca.err[ER_EDGE_INDEX], 1);
         const bool work = live && Jp->iters != 0 && status == 0;
@@ -1408,7 +1468,8 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
             if (b.cull && __any_sync(0xffffffffu, work))
                 search_cull(P, work, cpt, axis, lo, hi, q, cur, cur + nw, have_prev, prog, len);
             if (live && status == 0) {
-                const P3 out = work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, Jp->iters, cnt, Jp->ca.err) : cpt;
+                const P3 out =
+                    work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, Jp->iters, hi_bit, cnt, Jp->ca.err) : cpt;
                 verts[3 * v] = out.x;
                 verts[3 * v + 1] = out.y;
                 verts[3 * v + 2] = out.z;
@@ -1417,8 +1478,8 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
             // The batch straddles jobs: every lane runs its own job's full program.
             prev_job = -1;
             if (live && status == 0) {
-                const P3 out = work ? bisect<PREC>(Jp->P, Jp->P.ops, Jp->P.n_ops, cpt, axis, lo, hi, Jp->iters, cnt,
-                                                   Jp->ca.err)
+                const P3 out = work ? bisect<PREC>(Jp->P, Jp->P.ops, Jp->P.n_ops, cpt, axis, lo, hi, Jp->iters, hi_bit,
+                                                   cnt, Jp->ca.err)
                                     : cpt;
                 verts[3 * v] = out.x;
                 verts[3 * v + 1] = out.y;
@@ -1428,6 +1489,37 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
         __syncwarp();
     }
     flush_counts(cnt, b.stats);
+}
+
+// ------------------------------------------------------------ peak probes
+//
+// Roofline denominators for this path's kernels: dependent-chain-free FMA
+// loops (8 independent chains per thread) in FP32 and FP64, and a read loop
+// over a buffer that stays resident in L2.
+
+template <class T>
+__global__ void __launch_bounds__(256) k_peak_fma(T* out, int iters, T a, T b) {
+    T x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = (T)(threadIdx.x + k);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = x[k] * a + b;
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += x[k];
+    if (s == (T)-1.2345) out[0] = s;  // keeps the chains alive
+}
+
+__global__ void __launch_bounds__(256) k_peak_read(const uint4* buf, size_t n16, int reps, unsigned* out) {
+    unsigned acc = 0;
+    for (int r = 0; r < reps; r++)
+        for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x) {
+            const uint4 v = __ldcg(buf + i);
+            acc ^= v.x ^ v.y ^ v.z ^ v.w;
+        }
+    if (acc == 0x12345678u) out[0] = acc;
 }
 
 }  // namespace mcgpu
@@ -1518,6 +1610,7 @@ struct BatchPlan {
 
 struct mc_ctx {
     std::unique_ptr<BatchPlan> plan;
+    int tuned_ty = 0, tuned_tz = 0;  // set by mc_autotune; used when a call leaves the tile shape at 0
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
@@ -1831,8 +1924,8 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     ca.xf = ctx->xf.as<float>();
     ca.yf = ctx->yf.as<float>();
     ca.zf = ctx->zf.as<float>();
-    ca.ty = opts.tile_y > 0 ? opts.tile_y : kTileY;
-    ca.tz = opts.tile_z > 0 ? opts.tile_z : kTileZ;
+    ca.ty = opts.tile_y > 0 ? opts.tile_y : (ctx->tuned_ty > 0 ? ctx->tuned_ty : kTileY);
+    ca.tz = opts.tile_z > 0 ? opts.tile_z : (ctx->tuned_tz > 0 ? ctx->tuned_tz : kTileZ);
     ca.ntx = (nx + 31) / 32;
     ca.nty = (ny + ca.ty - 1) / ca.ty;
     ca.ntz = (nz + ca.tz - 1) / ca.tz;
@@ -1894,6 +1987,7 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     if (V > 0) {
         SearchArgs sa{};
         sa.inv_dl = nx >= 2 ? 1.0 / (X[1] - X[0]) : 0.0;
+        sa.bits = ctx->bits.as<uint32_t>();
         sa.keys = ctx->keys.as<unsigned long long>();
         sa.verts = ctx->verts.as<double>();
         sa.nverts = V;
@@ -2019,6 +2113,75 @@ mc_status mc_contains(mc_ctx* ctx, const mc_solid* solid, const double* points, 
     return MC_OK;
 }
 
+mc_status mc_measure_peaks(mc_ctx* ctx, double* fp32_tflops, double* fp64_tflops, double* l2_read_gbs) {
+    if (!ctx) return MC_ERR_ARG;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t sm = ctx->stream;
+    CK(ctx->pts.ensure(64u << 20));
+    const int blocks = ctx->sm_count * 8;
+    float ms = 0;
+    auto timed = [&](auto launch) -> float {
+        launch();  // warm-up
+        cudaEventRecord(ctx->ev[0], sm);
+        launch();
+        cudaEventRecord(ctx->ev[1], sm);
+        cudaEventSynchronize(ctx->ev[1]);
+        float t = 0;
+        cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]);
+        return t;
+    };
+    const int it32 = 4096, it64 = 256;
+    ms = timed([&] { k_peak_fma<float><<<blocks, 256, 0, sm>>>((float*)ctx->pts.p, it32, 1.0000001f, 1e-7f); });
+    if (fp32_tflops) *fp32_tflops = 2.0 * 8 * it32 * (double)blocks * 256 / (ms * 1e-3) / 1e12;
+    ms = timed([&] { k_peak_fma<double><<<blocks, 256, 0, sm>>>((double*)ctx->pts.p, it64, 1.0000001, 1e-7); });
+    if (fp64_tflops) *fp64_tflops = 2.0 * 8 * it64 * (double)blocks * 256 / (ms * 1e-3) / 1e12;
+    const size_t bytes = 48u << 20;  // resident in the 126 MB L2
+    CK(cudaMemsetAsync(ctx->pts.p, 1, bytes, sm));
+    const int reps = 20;
+    ms = timed([&] {
+        k_peak_read<<<ctx->sm_count * 4, 256, 0, sm>>>((const uint4*)ctx->pts.p, bytes / 16, reps,
+                                                       (unsigned*)((char*)ctx->pts.p + bytes));
+    });
+    if (l2_read_gbs) *l2_read_gbs = (double)bytes * reps / (ms * 1e-3) / 1e9;
+    CK(cudaGetLastError());
+    return MC_OK;
+}
+
+mc_status mc_autotune(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters, const mc_opts* opts_in,
+                      mc_opts* best, double* best_ms) {
+    if (!ctx || !solid) return fail(ctx, MC_ERR_ARG, "bad argument");
+    // Corner-tile shapes (rows = ty * tz <= 32 keeps the row-vectorised path).
+    static const int cand[][2] = {{2, 4}, {4, 2}, {4, 4}, {8, 2}, {2, 8}, {8, 4}, {4, 8}, {16, 2}, {2, 16}};
+    mc_opts o = default_opts(opts_in);
+    double best_t = 1e30;
+    int bty = kTileY, btz = kTileZ;
+    for (const auto& c : cand) {
+        o.tile_y = c[0];
+        o.tile_z = c[1];
+        double t = 1e30;
+        for (int rep = 0; rep < 3; rep++) {
+            mc_stats st{};
+            mc_status s = mc_search_device(ctx, solid, delta, iters, &o, nullptr, nullptr, &st);
+            if (s != MC_OK) return s;
+            t = std::min(t, st.ms_classify);
+        }
+        if (t < best_t) {
+            best_t = t;
+            bty = c[0];
+            btz = c[1];
+        }
+    }
+    ctx->tuned_ty = bty;
+    ctx->tuned_tz = btz;
+    if (best) {
+        *best = default_opts(opts_in);
+        best->tile_y = bty;
+        best->tile_z = btz;
+    }
+    if (best_ms) *best_ms = best_t;
+    return MC_OK;
+}
+
 mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_opts* opts_in, mc_mesh* outs,
                           mc_status* job_status) {
     if (!ctx || (n && (!jobs || !outs))) return fail(ctx, MC_ERR_ARG, "bad argument");
@@ -2029,7 +2192,9 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
     }
     if (n == 0) return MC_OK;
     CK(cudaSetDevice(ctx->device));
-    const mc_opts opts = default_opts(opts_in);
+    mc_opts opts = default_opts(opts_in);
+    if (opts.tile_y <= 0) opts.tile_y = ctx->tuned_ty > 0 ? ctx->tuned_ty : kTileY;
+    if (opts.tile_z <= 0) opts.tile_z = ctx->tuned_tz > 0 ? ctx->tuned_tz : kTileZ;
     cudaStream_t sm = ctx->stream;
 
     // Reuse the plan (and its CUDA graph) when the same batch comes back.
@@ -2086,8 +2251,8 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             J.P = jobs[i].solid->view;
             J.ca.prec = pl->prec;
             J.ca.cull = opts.cull;
-            J.ca.ty = opts.tile_y > 0 ? opts.tile_y : kTileY;
-            J.ca.tz = opts.tile_z > 0 ? opts.tile_z : kTileZ;
+            J.ca.ty = opts.tile_y > 0 ? opts.tile_y : (ctx->tuned_ty > 0 ? ctx->tuned_ty : kTileY);
+            J.ca.tz = opts.tile_z > 0 ? opts.tile_z : (ctx->tuned_tz > 0 ? ctx->tuned_tz : kTileZ);
             J.ca.ntx = (nx + 31) / 32;
             J.ca.nty = (ny + J.ca.ty - 1) / J.ca.ty;
             J.ca.ntz = (nz + J.ca.tz - 1) / J.ca.tz;
@@ -2559,6 +2724,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     if (V > 0) {
         SearchArgs sa{};
         sa.inv_dl = nx >= 2 ? 1.0 / (X[1] - X[0]) : 0.0;
+        sa.bits = bits;
         sa.keys = (const unsigned long long*)keys_base;
         sa.verts = vertices;
         sa.nverts = V;

@@ -212,6 +212,28 @@ def MarchingCubesSearchBatch(jobs, *, precision: str = "fp32", cull: bool = True
     return res
 
 
+def autotune(solid, delta: float, iters: int = 8, *, precision: str = "fp32",
+             ctx: Optional[Context] = None):
+    """Time the classification tile shapes on this solid and grid; the
+    fastest becomes the context's default.  Returns (tile_y, tile_z, ms)."""
+    ctx = ctx or (solid.ctx if isinstance(solid, DeviceSolid) else default_context())
+    ds = _as_device_solid(solid, ctx)
+    o = _opts(precision)
+    best = N.MCOpts()
+    ms = ctypes.c_double()
+    _check(N.lib().mc_autotune(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
+                               ctypes.byref(best), ctypes.byref(ms)), ctx.ptr)
+    return best.tile_y, best.tile_z, ms.value
+
+
+def measure_peaks(ctx: Optional[Context] = None):
+    """(fp32 TFLOP/s, fp64 TFLOP/s, L2 read GB/s) of this GPU (micro-kernels)."""
+    ctx = ctx or default_context()
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _check(N.lib().mc_measure_peaks(ctx.ptr, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), ctx.ptr)
+    return a.value, b.value, c.value
+
+
 def MarchingCubes(solid, delta: float, **kw) -> Mesh:
     """model3d.MarchingCubes (model3d/mc.go:14-37): the search with iters=0."""
     return MarchingCubesSearch(solid, delta, 0, **kw)

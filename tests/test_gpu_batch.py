@@ -58,3 +58,16 @@ def test_batch_job_failures_are_per_job():
     for k in (0, 3):
         ref = MarchingCubesSearch(good, jobs[k][1], 8)
         assert np.array_equal(canonical(out[k].TriangleSoup()), canonical(ref.TriangleSoup()))
+
+
+def test_autotune_keeps_results_and_peaks_are_positive():
+    from model3d_gb300 import autotune, measure_peaks
+    ds = DeviceSolid(csg_tree(2, 16, 4))
+    ref = MarchingCubesSearch(ds, 0.02, 8)
+    ty, tz, ms = autotune(ds, 0.02, 8)
+    assert ty * tz <= 32 and ms > 0
+    m = MarchingCubesSearch(ds, 0.02, 8)  # tuned shape is now the context default
+    assert np.array_equal(m.vertices.view(np.uint64), ref.vertices.view(np.uint64))
+    assert np.array_equal(m.triangles, ref.triangles)
+    f32, f64, l2 = measure_peaks()
+    assert f32 > 0 and f64 > 0 and l2 > 0
