@@ -26,6 +26,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mcgpu.h"
@@ -859,14 +860,25 @@ __device__ __forceinline__ uint32_t count_chunk(const GridView& g, const uint32_
     return cx | (cy << 6) | (cz << 12) | (nt << 18);
 }
 
+// Count and scan blocks cover kChunksPerBlock chunks: 256 threads x 8
+// chunks, thread t taking chunks t, t + 256, ... (coalesced).
+constexpr int kChunksPerBlock = 2048;
+
 __global__ void __launch_bounds__(256) k_count(GridView g, CountArgs a) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t nv = 0, nt = 0;
-    if (i < a.nchunks) a.packed[i] = count_chunk(g, a.bits, i, nv, nt);
-    block_sum2(nv, nt);
+    const long long base = (long long)blockIdx.x * kChunksPerBlock;
+    uint32_t sv = 0, st = 0;
+#pragma unroll
+    for (int k = 0; k < kChunksPerBlock / 256; k++) {
+        const long long i = base + k * 256 + threadIdx.x;
+        uint32_t nv = 0, nt = 0;
+        if (i < a.nchunks) a.packed[i] = count_chunk(g, a.bits, i, nv, nt);
+        sv += nv;
+        st += nt;
+    }
+    block_sum2(sv, st);
     if (threadIdx.x == 0) {
-        a.blocksum[2 * blockIdx.x] = nv;
-        a.blocksum[2 * blockIdx.x + 1] = nt;
+        a.blocksum[2 * blockIdx.x] = sv;
+        a.blocksum[2 * blockIdx.x + 1] = st;
     }
 }
 
@@ -905,27 +917,35 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t* blocksum, 
     }
 }
 
-// Per-chunk exclusive offsets (vertex, triangle) as two u32 arrays.
+// Per-chunk exclusive offsets (vertex, triangle) as two u32 arrays; one
+// block per kChunksPerBlock chunks, eight 256-wide scans with a carry.
 __global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* packed, const unsigned long long* blockoff,
                                                      long long nchunks, uint32_t* prefv, uint32_t* preft) {
     __shared__ uint32_t sv[256], st[256];
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t p = i < nchunks ? packed[i] : 0;
-    uint32_t v = (p & 63u) + ((p >> 6) & 63u) + ((p >> 12) & 63u), w = p >> 18;
-    int t = threadIdx.x;
-    sv[t] = v;
-    st[t] = w;
-    __syncthreads();
-    for (int o = 1; o < 256; o <<= 1) {
-        uint32_t av = t >= o ? sv[t - o] : 0, aw = t >= o ? st[t - o] : 0;
+    const int t = threadIdx.x;
+    const long long base = (long long)blockIdx.x * kChunksPerBlock;
+    unsigned long long cv = blockoff[2 * blockIdx.x], ct = blockoff[2 * blockIdx.x + 1];
+    for (int k = 0; k < kChunksPerBlock / 256; k++) {
+        const long long i = base + k * 256 + t;
+        const uint32_t p = i < nchunks ? packed[i] : 0;
+        const uint32_t v = (p & 63u) + ((p >> 6) & 63u) + ((p >> 12) & 63u), w = p >> 18;
+        sv[t] = v;
+        st[t] = w;
         __syncthreads();
-        sv[t] += av;
-        st[t] += aw;
+        for (int o = 1; o < 256; o <<= 1) {
+            const uint32_t av = t >= o ? sv[t - o] : 0, aw = t >= o ? st[t - o] : 0;
+            __syncthreads();
+            sv[t] += av;
+            st[t] += aw;
+            __syncthreads();
+        }
+        if (i < nchunks) {
+            prefv[i] = (uint32_t)(cv + sv[t] - v);
+            preft[i] = (uint32_t)(ct + st[t] - w);
+        }
+        cv += sv[255];
+        ct += st[255];
         __syncthreads();
-    }
-    if (i < nchunks) {
-        prefv[i] = (uint32_t)(blockoff[2 * blockIdx.x] + sv[t] - v);
-        preft[i] = (uint32_t)(blockoff[2 * blockIdx.x + 1] + st[t] - w);
     }
 }
 
@@ -1387,12 +1407,17 @@ __global__ void __launch_bounds__(256, 3) k_classify_batch(BatchArgs b) {
 }
 
 __global__ void __launch_bounds__(256) k_count_batch(BatchArgs b, uint32_t* packed, uint32_t* blocksum) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long base = (long long)blockIdx.x * kChunksPerBlock;
     uint32_t nv = 0, nt = 0;
-    if (i < b.nchunks) {
+    for (int k = 0; k < kChunksPerBlock / 256; k++) {
+        const long long i = base + k * 256 + threadIdx.x;
+        if (i >= b.nchunks) break;
         const int j = find_slot(b.chunk_offs, b.njobs, i);
         const JobD& J = b.jobs[j];
-        packed[i] = count_chunk(J.g, J.ca.bits, i - b.chunk_offs[j], nv, nt);
+        uint32_t a = 0, c = 0;
+        packed[i] = count_chunk(J.g, J.ca.bits, i - b.chunk_offs[j], a, c);
+        nv += a;
+        nt += c;
     }
     block_sum2(nv, nt);
     if (threadIdx.x == 0) {
@@ -1618,6 +1643,8 @@ struct mc_ctx {
     DevBuf xs, ys, zs, xf, yf, zf, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
     DevBuf pts, pout;
     unsigned long long* h_pin = nullptr;  // pinned: totals[2], stats[ST_N], errs (as ints) ...
+    unsigned char* stage[2] = {nullptr, nullptr};  // pinned staging for device-to-host mesh copies
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
     int64_t last_V = 0, last_T = 0;
     int sm_count = 152;
 };
@@ -1741,6 +1768,10 @@ void mc_destroy(mc_ctx* ctx) {
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
+    for (int b = 0; b < 2; b++) {
+        if (ctx->stage[b]) cudaFreeHost(ctx->stage[b]);
+        if (ctx->stage_ev[b]) cudaEventDestroy(ctx->stage_ev[b]);
+    }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1943,7 +1974,8 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     CK(cudaEventRecord(ctx->ev[1], sm));
 
     long long nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)g.CX * (ny - 1) * (nz - 1) : 0;
-    int nblk = (int)((nchunks + 255) / 256);
+    const int nblk = (int)((nchunks + kChunksPerBlock - 1) / kChunksPerBlock);
+    const int egrid = (int)((nchunks + 255) / 256);
     if (nchunks > 0) {
         CK(ctx->packed.ensure(nchunks * 4));
         CK(ctx->blocksum.ensure((size_t)nblk * 8));
@@ -1980,7 +2012,7 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     if (nchunks > 0 && (V > 0 || T > 0)) {
         EmitArgs ea{ctx->bits.as<uint32_t>(), ctx->packed.as<uint32_t>(), ctx->prefv.as<uint32_t>(),
                     ctx->preft.as<uint32_t>(), ctx->keys.as<unsigned long long>(), ctx->tris.as<int32_t>(), nchunks};
-        k_emit<<<nblk, 256, 0, sm>>>(g, ea);
+        k_emit<<<egrid, 256, 0, sm>>>(g, ea);
         CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ctx->ev[3], sm));
@@ -2044,15 +2076,66 @@ mc_status mc_result_device(const mc_ctx* ctx, const double** vertices, const int
     return MC_OK;
 }
 
+namespace {
+// Device-to-host copy into any host memory through two pinned 16 MiB
+// staging buffers: the DMA of one chunk overlaps the host copy of the
+// previous one, which is split over a few threads.
+constexpr size_t kStageBytes = 16u << 20;
+
+void host_copy(void* dst, const void* src, size_t n) {
+    const int nt = n >= (4u << 20) ? 4 : 1;
+    if (nt == 1) {
+        std::memcpy(dst, src, n);
+        return;
+    }
+    std::vector<std::thread> ts;
+    const size_t per = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; t++) {
+        const size_t a = t * per, b = std::min(n, a + per);
+        if (a < b) ts.emplace_back([=] { std::memcpy((char*)dst + a, (const char*)src + a, b - a); });
+    }
+    for (auto& t : ts) t.join();
+}
+
+mc_status staged_d2h(mc_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    if (!bytes) return MC_OK;
+    for (int b = 0; b < 2; b++) {
+        if (!ctx->stage[b]) CK(cudaHostAlloc((void**)&ctx->stage[b], kStageBytes, cudaHostAllocDefault));
+        if (!ctx->stage_ev[b]) CK(cudaEventCreateWithFlags(&ctx->stage_ev[b], cudaEventDisableTiming));
+    }
+    size_t pend_off[2] = {0, 0}, pend_len[2] = {0, 0};
+    int i = 0;
+    for (size_t off = 0; off < bytes; off += kStageBytes, i++) {
+        const int b = i & 1;
+        if (pend_len[b]) {
+            CK(cudaEventSynchronize(ctx->stage_ev[b]));
+            host_copy((char*)dst + pend_off[b], ctx->stage[b], pend_len[b]);
+        }
+        const size_t len = std::min(kStageBytes, bytes - off);
+        CK(cudaMemcpyAsync(ctx->stage[b], (const char*)src + off, len, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaEventRecord(ctx->stage_ev[b], ctx->stream));
+        pend_off[b] = off;
+        pend_len[b] = len;
+    }
+    for (int k = 0; k < 2; k++) {
+        const int b = (i + k) & 1;
+        if (pend_len[b]) {
+            CK(cudaEventSynchronize(ctx->stage_ev[b]));
+            host_copy((char*)dst + pend_off[b], ctx->stage[b], pend_len[b]);
+            pend_len[b] = 0;
+        }
+    }
+    return MC_OK;
+}
+}  // namespace
+
 mc_status mc_result_copy(mc_ctx* ctx, double* vertices, int32_t* triangles) {
     if (!ctx) return MC_ERR_ARG;
     CK(cudaSetDevice(ctx->device));
-    if (vertices && ctx->last_V)
-        CK(cudaMemcpyAsync(vertices, ctx->verts.p, ctx->last_V * 24, cudaMemcpyDeviceToHost, ctx->stream));
-    if (triangles && ctx->last_T)
-        CK(cudaMemcpyAsync(triangles, ctx->tris.p, ctx->last_T * 12, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-    return MC_OK;
+    mc_status st = MC_OK;
+    if (vertices && ctx->last_V) st = staged_d2h(ctx, vertices, ctx->verts.p, (size_t)ctx->last_V * 24);
+    if (st == MC_OK && triangles && ctx->last_T) st = staged_d2h(ctx, triangles, ctx->tris.p, (size_t)ctx->last_T * 12);
+    return st;
 }
 
 mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters, const mc_opts* opts,
@@ -2327,7 +2410,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             pl->hchunk_offs[d + 1] = pl->hchunk_offs[d] + pl->hjobs[d].nchunks;
         }
         pl->nchunks = pl->hchunk_offs[nd];
-        pl->nblk = (int)((pl->nchunks + 255) / 256);
+        pl->nblk = (int)((pl->nchunks + kChunksPerBlock - 1) / kChunksPerBlock);
         CK(pl->jobs.ensure(std::max(nd, 1) * sizeof(JobD)));
         CK(pl->sched_off.ensure(sched_off.size() * 8));
         CK(pl->sched_job.ensure(sched_job.size() * 4));
@@ -2393,7 +2476,8 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
     };
     auto back = [&]() -> cudaError_t {
         if (pl->nchunks > 0)
-            k_emit_batch<<<pl->nblk, 256, 0, sm>>>(ba, pl->packed.as<uint32_t>(), pl->prefv.as<uint32_t>(),
+            k_emit_batch<<<(int)((pl->nchunks + 255) / 256), 256, 0, sm>>>(ba, pl->packed.as<uint32_t>(),
+                                                                             pl->prefv.as<uint32_t>(),
                                                    pl->preft.as<uint32_t>(), pl->keys.as<unsigned long long>(),
                                                    pl->tris.as<int32_t>());
         if (nd > 0) ksb<<<pl->grid_s, 128, pl->smem_s, sm>>>(ba, pl->keys.as<unsigned long long>(), pl->verts.as<double>());
@@ -2632,7 +2716,8 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     const size_t nbits = (size_t)nz * ny * g.W;
     uint32_t* bits = (uint32_t*)cv.take(nbits * 4);
     long long nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)g.CX * (ny - 1) * (nz - 1) : 0;
-    int nblk = (int)((nchunks + 255) / 256);
+    const int nblk = (int)((nchunks + kChunksPerBlock - 1) / kChunksPerBlock);
+    const int egrid = (int)((nchunks + 255) / 256);
     uint32_t* packed = (uint32_t*)cv.take(nchunks * 4);
     uint32_t* blocksum = (uint32_t*)cv.take((size_t)nblk * 8);
     unsigned long long* blockoff = (unsigned long long*)cv.take((size_t)nblk * 16);
@@ -2719,7 +2804,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         return MC_ERR_LIMIT;  // caller's buffers too small; *n_vertices / *n_triangles say how large
     if (nchunks > 0 && (V > 0 || T > 0)) {
         EmitArgs ea{bits, packed, prefv, preft, (unsigned long long*)keys_base, triangles, nchunks};
-        k_emit<<<nblk, 256, 0, sm>>>(g, ea);
+        k_emit<<<egrid, 256, 0, sm>>>(g, ea);
     }
     if (V > 0) {
         SearchArgs sa{};

@@ -164,17 +164,17 @@ def MarchingCubesSearch(solid, delta: float, iters: int, *, precision: str = "fp
     """model3d.MarchingCubesSearch (model3d/mc.go:45-49) on the GPU."""
     ctx = ctx or (solid.ctx if isinstance(solid, DeviceSolid) else default_context())
     ds = _as_device_solid(solid, ctx)
-    out = N.MCMesh()
     o = _opts(precision, cull, tile_y, tile_z)
-    _check(N.lib().mc_search(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
-                             ctypes.byref(out)), ctx.ptr)
-    try:
-        V, T = out.n_vertices, out.n_triangles
-        verts = np.ctypeslib.as_array(out.vertices, shape=(max(V, 1) * 3,))[:V * 3].reshape(V, 3).copy()
-        tris = np.ctypeslib.as_array(out.triangles, shape=(max(T, 1) * 3,))[:T * 3].reshape(T, 3).copy()
-        stats = out.stats.as_dict()
-    finally:
-        N.lib().mc_mesh_free(ctypes.byref(out))
+    V, T = ctypes.c_int64(), ctypes.c_int64()
+    st = N.MCStats()
+    L = N.lib()
+    _check(L.mc_search_device(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
+                              ctypes.byref(V), ctypes.byref(T), ctypes.byref(st)), ctx.ptr)
+    verts = np.empty((V.value, 3), dtype=np.float64)
+    tris = np.empty((T.value, 3), dtype=np.int32)
+    _check(L.mc_result_copy(ctx.ptr, verts.ctypes.data, tris.ctypes.data), ctx.ptr)
+    stats = st.as_dict()
+    stats["d2h_bytes"] += verts.nbytes + tris.nbytes
     return Mesh(verts, tris, stats)
 
 
