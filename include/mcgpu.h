@@ -94,7 +94,8 @@ enum {
  * min/max are the node's Min()/Max() exactly as the host language computed
  * them; the library uses the root's bounds for the spacer and the bounds of
  * TRANSFORM / CHECKED / COLLIDER nodes for their containment checks, so that
- * the grid is bit-identical to the caller's own newSquareSpacer.
+ * the grid is bit-identical to the caller's own newSquareSpacer.  The bounds
+ * of other non-root nodes are not read and may be left zero.
  */
 typedef struct mc_node {
     int32_t kind;

@@ -8,7 +8,8 @@
 //     constants for the filtered predicate,
 //   * a table of box checks (TRANSFORM / CHECKED nodes) with the inverse
 //     transform steps of TRANSFORM nodes,
-//   * flattened collider trees (nodes, child lists, triangle records).
+//   * collider trees: the reference's JoinedCollider boxes, one record per
+//     triangle with its parent box, and a ray grid of candidate triangles.
 #pragma once
 
 #include <stdint.h>
@@ -68,7 +69,6 @@ constexpr int LEAF_F = 16;
 constexpr int MAX_STACK = 31;     // bit-stack depth limit
 constexpr int MAX_XDEPTH = 8;     // nested transforms
 constexpr int MAX_OPS = 1 << 16;  // program length limit
-constexpr int MAX_BVH_DEPTH = 64; // traversal frames
 
 // Inverse transform step: kind (MC_XF_*), 9 parameters.
 struct XStepD {
@@ -86,19 +86,22 @@ struct XBoxD {
     int32_t n_steps;
 };
 
-// Flattened collider tree.  Node child lists live in `child` entries:
-// c >= 0 is a node index, c < 0 is triangle (-c - 1).
+// Collider trees.  The reference counts the triangles T that its ray test
+// hits AND that its traversal reaches: every JoinedCollider box above T
+// passes the slab test (collisions.go:263-273, bvh.go:322-351).  A parent
+// box is the min/max of its children's boxes, so it lies inside every
+// ancestor's box, and fl((b - o) / r) is monotone in b for r > 0: the
+// float64 slab interval of an ancestor contains the parent's.  T is
+// therefore reached iff the slab test of its parent box passes, and only
+// that box is stored per triangle (`tri_parent`, -1 when the tree is a
+// single triangle).
 struct BvhNodeD {
     double lo[3];
     double hi[3];
-    int32_t first;  // first entry in the child list
-    int32_t count;
 };
 struct BvhNodeF {  // FP32 copy of the node box, rounded outward
     float lo[3];
     float hi[3];
-    int32_t first;
-    int32_t count;
 };
 // Per-triangle Moller-Trumbore constants with the ray direction fixed
 // (model3d/primitives.go:207-249, collisions.go:124): t0, v1, v2,
@@ -120,11 +123,34 @@ struct TriF {
     float inv_det;
     int32_t valid;
 };
+
+// Ray grid.  Every containment ray has the direction D of collisions.go:124,
+// so a ray is a point of the plane x = 0 once projected along D:
+// (a, b) = (p.y - KY p.x, p.z - KZ p.x), and t(p) = p.x / D.x grows by s
+// along o + s D.  Each valid triangle is listed in the cells its projected
+// bounding box covers, widened by a pad that exceeds every rounding error of
+// the reference's float64 test and of the float projection of the ray
+// origin, so a ray that the reference's test can hit lists that triangle in
+// its cell.  Within a cell the entries are sorted by the triangle's largest
+// t (plus the pad): a ray only tests the suffix with maxt >= t(origin),
+// since triangles entirely behind the origin have a negative scale.
+// Ill-conditioned triangles (none in ordinary meshes) go to an `all` list
+// tested by every ray of the tree.
+constexpr double RAYGRID_KY = 0.10494477243214506 / 0.5224892708603626;
+constexpr double RAYGRID_KZ = 0.43558938446126527 / 0.5224892708603626;
+constexpr double RAYGRID_INV_DX = 1.0 / 0.5224892708603626;
+struct RayEnt {
+    float maxt;   // largest t over the triangle, rounded up, plus the pad
+    int32_t tri;  // absolute triangle index
+};
 struct TreeD {
-    int32_t kind;  // 0: no triangles (nullCollider); 1: root is a node; 2: root is one triangle
-    int32_t root;  // node or triangle index (absolute)
+    int32_t kind;  // 0: no triangles (nullCollider); 1: triangles
+    int32_t n_cells;
     float mbox[3]; // per axis, an upper bound of |coordinate| over every box of the tree
-    int32_t pad;
+    float amin, bmin, inv_cs;  // grid origin (float) and 1 / cell size
+    int32_t ga, gb;            // cells along a and b
+    int32_t cell_base;         // this tree's first cell_start entry
+    int32_t all_first, all_count;  // RayEnt range tested by every ray
 };
 
 // Device view of one lowered solid (passed by value to kernels).
@@ -141,7 +167,9 @@ struct ProgView {
     const TreeD* trees;
     const BvhNodeD* nodes;
     const BvhNodeF* nodes_f;
-    const int32_t* child;
+    const int32_t* tri_parent;  // parent box of each triangle, -1 for a single-triangle tree
+    const int32_t* cell_start;  // per tree: n_cells + 1 offsets into ents
+    const RayEnt* ents;
     const TriD* tris;
     const TriF* tris_f;
     int32_t n_ops;

@@ -29,6 +29,8 @@
 #include <thread>
 #include <vector>
 
+#include <unistd.h>
+
 #include "../../include/mcgpu.h"
 #include "mc_internal.h"
 #include "mc_lower.h"
@@ -43,7 +45,7 @@ struct Counts {
 };
 
 enum StatSlot { ST_LEAF = 0, ST_ESC, ST_NODES, ST_TRIS, ST_TILES_CONST, ST_WORK, ST_N };
-enum ErrSlot { ER_BORDER = 0, ER_NOT_ON_EDGE, ER_EDGE_INDEX, ER_LIMIT, ER_N };
+enum ErrSlot { ER_BORDER = 0, ER_NOT_ON_EDGE, ER_EDGE_INDEX, ER_N };
 
 __device__ __forceinline__ void flush_counts(const Counts& c, unsigned long long* stats) {
     unsigned long long v[4] = {c.leaf, c.esc, c.nodes, c.tris};
@@ -65,58 +67,62 @@ __device__ __forceinline__ void flush_counts(const Counts& c, unsigned long long
 __device__ __noinline__ bool collider_point(const ProgView& P, const double* d, P3 p, F3 pf, bool filt, Counts& cnt,
                                             int* err) {
     if (!(p.x >= d[0] && p.y >= d[1] && p.z >= d[2] && p.x <= d[3] && p.y <= d[4] && p.z <= d[5])) return false;
-    const TreeD t = P.trees[(int)d[6]];
+    const TreeD& t = P.trees[(int)d[6]];
     if (t.kind == 0) return false;
-    auto tri_hit = [&](int i) -> int {
-        cnt.tris++;
-        if (filt) {
-            int v = ray_tri_32(P.tris_f[i], pf);
-            if (v != 2) return v;
-            cnt.esc++;
-        }
-        return ray_tri_64(P.tris[i], p);
-    };
-    if (t.kind == 2) return tri_hit(t.root) & 1;
-    RayF rf;
-    if (filt) rf = make_rayf(pf, t.mbox);
-    auto box_hit = [&](int c) -> bool {
-        cnt.nodes++;
-        if (filt) {
-            int v = ray_box_32(P.nodes_f[c], rf);
-            if (v != 2) return v == 1;
-            cnt.esc++;
-        }
-        return ray_box_64(P.nodes[c].lo, P.nodes[c].hi, p);
-    };
-    // Depth-first over child ranges; the hit count is a sum, so order is free.
-    int stk_i[MAX_BVH_DEPTH], stk_e[MAX_BVH_DEPTH];
-    int sp = 0, hits = 0;
-    if (!box_hit(t.root)) return false;
-    stk_i[0] = P.nodes[t.root].first;
-    stk_e[0] = stk_i[0] + P.nodes[t.root].count;
-    sp = 1;
-    while (sp > 0) {
-        const int i = stk_i[sp - 1];
-        if (i >= stk_e[sp - 1]) {
-            sp--;
-            continue;
-        }
-        stk_i[sp - 1] = i + 1;
-        const int c = P.child[i];
-        if (c < 0) {
-            hits += tri_hit(-c - 1);
-            continue;
-        }
-        if (!box_hit(c)) continue;
-        if (sp == MAX_BVH_DEPTH) {
-            atomicOr(&err[ER_LIMIT], 1);
-            return false;
-        }
-        const BvhNodeF& n = P.nodes_f[c];
-        stk_i[sp] = n.first;
-        stk_e[sp] = n.first + n.count;
-        sp++;
+    // The ray's cell and depth (t of the origin) on the ray grid.
+    float fa, fb, to;
+    if (filt) {
+        fa = (__fmaf_rn(-(float)RAYGRID_KY, pf.x, pf.y) - t.amin) * t.inv_cs;
+        fb = (__fmaf_rn(-(float)RAYGRID_KZ, pf.x, pf.z) - t.bmin) * t.inv_cs;
+        to = pf.x * (float)RAYGRID_INV_DX;
+    } else {
+        fa = (float)(D_MUL(D_SUB(D_SUB(p.y, D_MUL(RAYGRID_KY, p.x)), (double)t.amin), (double)t.inv_cs));
+        fb = (float)(D_MUL(D_SUB(D_SUB(p.z, D_MUL(RAYGRID_KZ, p.x)), (double)t.bmin), (double)t.inv_cs));
+        to = __double2float_rd(D_MUL(p.x, RAYGRID_INV_DX));
     }
+    RayF rf;
+    bool have_rf = false;
+    int hits = 0;
+    // Triangle i counts iff the reference's ray test hits it and the slab
+    // test of its parent box passes.
+    auto test = [&](int i) {
+        cnt.tris++;
+        int h = 2;
+        if (filt) {
+            h = ray_tri_32(P.tris_f[i], pf);
+            if (h == 2) cnt.esc++;
+        }
+        if (h == 2) h = ray_tri_64(P.tris[i], p);
+        if (!h) return;
+        const int par = P.tri_parent[i];
+        if (par < 0) {
+            hits++;
+            return;
+        }
+        cnt.nodes++;
+        int b = 2;
+        if (filt) {
+            if (!have_rf) {
+                rf = make_rayf(pf, t.mbox);
+                have_rf = true;
+            }
+            b = ray_box_32(P.nodes_f[par], rf);
+            if (b == 2) cnt.esc++;
+        }
+        if (b == 2) b = ray_box_64(P.nodes[par].lo, P.nodes[par].hi, p) ? 1 : 0;
+        hits += b;
+    };
+    if (fa >= 0.f && fb >= 0.f && fa < (float)t.ga && fb < (float)t.gb) {
+        const int c = t.cell_base + (int)fb * t.ga + (int)fa;
+        const int s = P.cell_start[c];
+        for (int k = P.cell_start[c + 1] - 1; k >= s; k--) {
+            const RayEnt e = P.ents[k];
+            if (e.maxt < to) break;  // this and every earlier entry lies behind the origin
+            test(e.tri);
+        }
+    }
+    for (int k = 0; k < t.all_count; k++) test(P.ents[t.all_first + k].tri);
+    (void)err;
     return hits & 1;
 }
 
@@ -1643,8 +1649,11 @@ struct mc_ctx {
     DevBuf xs, ys, zs, xf, yf, zf, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
     DevBuf pts, pout;
     unsigned long long* h_pin = nullptr;  // pinned: totals[2], stats[ST_N], errs (as ints) ...
-    unsigned char* stage[2] = {nullptr, nullptr};  // pinned staging for device-to-host mesh copies
-    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+    // Device buffers of destroyed solids, reused by the next mc_solid_create
+    // (stream order makes reuse safe without a synchronisation).  Solids may
+    // be destroyed from another thread than the context's, hence the lock.
+    std::mutex pool_mu;
+    std::vector<DevBuf> solid_pool;
     int64_t last_V = 0, last_T = 0;
     int sm_count = 152;
 };
@@ -1768,10 +1777,7 @@ void mc_destroy(mc_ctx* ctx) {
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
-    for (int b = 0; b < 2; b++) {
-        if (ctx->stage[b]) cudaFreeHost(ctx->stage[b]);
-        if (ctx->stage_ev[b]) cudaEventDestroy(ctx->stage_ev[b]);
-    }
+    for (DevBuf& d : ctx->solid_pool) d.release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1810,10 +1816,12 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
         {H.trees.data(), H.trees.size() * sizeof(TreeD), 0},
         {H.nodes.data(), H.nodes.size() * sizeof(BvhNodeD), 0},
         {H.nodes_f.data(), H.nodes_f.size() * sizeof(BvhNodeF), 0},
-        {H.child.data(), H.child.size() * 4, 0},
+        {H.tri_parent.data(), H.tri_parent.size() * 4, 0},
         {H.tris.data(), H.tris.size() * sizeof(TriD), 0},
         {H.tris_f.data(), H.tris_f.size() * sizeof(TriF), 0},
         {H.cull_f.data(), H.cull_f.size() * 4, 0},
+        {H.cell_start.data(), H.cell_start.size() * 4, 0},
+        {H.ents.data(), H.ents.size() * sizeof(RayEnt), 0},
     };
     size_t total = 0;
     for (auto& p : pcs) {
@@ -1821,6 +1829,17 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
         total += align256(p.bytes);
     }
     CK(cudaSetDevice(ctx->device));
+    {
+        std::lock_guard<std::mutex> lk(ctx->pool_mu);
+        for (size_t k = 0; k < ctx->solid_pool.size(); k++) {
+            DevBuf& d = ctx->solid_pool[k];
+            if (d.cap >= total && d.cap <= 4 * total + (1u << 20)) {
+                s->buf = d;
+                ctx->solid_pool.erase(ctx->solid_pool.begin() + k);
+                break;
+            }
+        }
+    }
     CK(s->buf.ensure(total));
     std::vector<unsigned char> staging(total, 0);
     for (auto& p : pcs)
@@ -1840,10 +1859,12 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
     v.trees = (const TreeD*)(b + pcs[8].off);
     v.nodes = (const BvhNodeD*)(b + pcs[9].off);
     v.nodes_f = (const BvhNodeF*)(b + pcs[10].off);
-    v.child = (const int32_t*)(b + pcs[11].off);
+    v.tri_parent = (const int32_t*)(b + pcs[11].off);
     v.tris = (const TriD*)(b + pcs[12].off);
     v.tris_f = (const TriF*)(b + pcs[13].off);
     v.cull_f = (const float*)(b + pcs[14].off);
+    v.cell_start = (const int32_t*)(b + pcs[15].off);
+    v.ents = (const RayEnt*)(b + pcs[16].off);
     v.n_ops = (int32_t)H.ops.size();
     v.n_ops_allfalse = H.n_ops_allfalse;
     v.n_leaves = (int32_t)H.leaf_kind.size();
@@ -1856,11 +1877,20 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
 
 void mc_solid_destroy(mc_solid* s) {
     if (!s) return;
-    if (s->ctx) {
-        cudaSetDevice(s->ctx->device);
-        cudaStreamSynchronize(s->ctx->stream);
+    if (s->ctx && s->buf.p && s->buf.cap <= (64u << 20)) {
+        std::lock_guard<std::mutex> lk(s->ctx->pool_mu);
+        if (s->ctx->solid_pool.size() < 16) {
+            s->ctx->solid_pool.push_back(s->buf);
+            s->buf = DevBuf{};
+        }
     }
-    s->buf.release();
+    if (s->buf.p) {
+        if (s->ctx) {
+            cudaSetDevice(s->ctx->device);
+            cudaStreamSynchronize(s->ctx->stream);
+        }
+        s->buf.release();
+    }
     delete s;
 }
 
@@ -1886,8 +1916,12 @@ mc_status mc_case_table(uint8_t counts[256], uint8_t tris[256][5][6]) {
     return build_case_table(counts, tris) == 0 ? MC_OK : MC_ERR_LIMIT;
 }
 
-mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters,
-                           const mc_opts* opts_in, int64_t* n_vertices, int64_t* n_triangles, mc_stats* stats_out) {
+namespace {
+// Everything up to the search kernel and the read-back of stats and error
+// words is enqueued; the host has waited only for the mesh totals, which
+// are in st->vertices / st->triangles.  search_finish waits for the rest.
+mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters, const mc_opts* opts_in,
+                        mc_stats* stats) {
     if (!ctx || !solid || iters < 0) return fail(ctx, MC_ERR_ARG, "bad argument");
     ctx->last_V = ctx->last_T = 0;
     mc_opts opts = default_opts(opts_in);
@@ -1999,7 +2033,6 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     CK(cudaStreamSynchronize(sm));
     const int* herr = (const int*)(hp + 2);
     if (herr[ER_BORDER]) return fail(ctx, MC_ERR_BOUNDS_INSIDE, "solid is true outside of bounds");
-    if (herr[ER_LIMIT]) return fail(ctx, MC_ERR_LIMIT, "collider traversal stack exceeded");
     const long long V = (long long)hp[0], T = (long long)hp[1];
     if (V >= ((long long)1 << 31) || T >= ((long long)1 << 31))
         return fail(ctx, MC_ERR_LIMIT, "mesh exceeds 2^31 vertices or triangles");
@@ -2039,10 +2072,19 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     CK(cudaEventRecord(ctx->ev[4], sm));
     CK(cudaMemcpyAsync(hp + 8, ctx->stats.p, ST_N * 8, cudaMemcpyDeviceToHost, sm));
     CK(cudaMemcpyAsync(hp + 2, ctx->errs.p, ER_N * 4, cudaMemcpyDeviceToHost, sm));
-    CK(cudaStreamSynchronize(sm));
+    st.h2d_bytes = (int64_t)(nx + ny + nz) * 8;
+    st.d2h_bytes = 16 + 2 * ER_N * 4 + ST_N * 8;
+    *stats = st;
+    return MC_OK;
+}
+
+mc_status search_finish(mc_ctx* ctx, mc_stats* stats) {
+    mc_stats& st = *stats;
+    CK(cudaStreamSynchronize(ctx->stream));
+    const unsigned long long* hp = ctx->h_pin;
+    const int* herr = (const int*)(hp + 2);
     if (herr[ER_NOT_ON_EDGE]) return fail(ctx, MC_ERR_NOT_ON_EDGE, "vertex not on edge");
     if (herr[ER_EDGE_INDEX]) return fail(ctx, MC_ERR_EDGE_INDEX, "index out of range");
-    if (herr[ER_LIMIT]) return fail(ctx, MC_ERR_LIMIT, "collider traversal stack exceeded");
     st.leaf_evals = (int64_t)hp[8 + ST_LEAF];
     st.escalations = (int64_t)hp[8 + ST_ESC];
     st.bvh_nodes = (int64_t)hp[8 + ST_NODES];
@@ -2059,12 +2101,20 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     st.ms_search = ms;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[4]);
     st.ms_total = ms;
-    st.h2d_bytes = (int64_t)(nx + ny + nz) * 8;
-    st.d2h_bytes = 16 + 2 * ER_N * 4 + ST_N * 8;
-    ctx->last_V = V;
-    ctx->last_T = T;
-    if (n_vertices) *n_vertices = V;
-    if (n_triangles) *n_triangles = T;
+    ctx->last_V = st.vertices;
+    ctx->last_T = st.triangles;
+    return MC_OK;
+}
+}  // namespace
+
+mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters,
+                           const mc_opts* opts, int64_t* n_vertices, int64_t* n_triangles, mc_stats* stats_out) {
+    mc_stats st{};
+    mc_status s = search_launch(ctx, solid, delta, iters, opts, &st);
+    if (s == MC_OK) s = search_finish(ctx, &st);
+    if (s != MC_OK) return s;
+    if (n_vertices) *n_vertices = st.vertices;
+    if (n_triangles) *n_triangles = st.triangles;
     if (stats_out) *stats_out = st;
     return MC_OK;
 }
@@ -2077,54 +2127,42 @@ mc_status mc_result_device(const mc_ctx* ctx, const double** vertices, const int
 }
 
 namespace {
-// Device-to-host copy into any host memory through two pinned 16 MiB
-// staging buffers: the DMA of one chunk overlaps the host copy of the
-// previous one, which is split over a few threads.
-constexpr size_t kStageBytes = 16u << 20;
-
-void host_copy(void* dst, const void* src, size_t n) {
-    const int nt = n >= (4u << 20) ? 4 : 1;
-    if (nt == 1) {
-        std::memcpy(dst, src, n);
+// Device-to-host copies of the mesh go straight into the caller's pageable
+// memory: on a Grace host the copy engine walks the host page tables and a
+// direct copy into resident pages runs at link speed.  Fresh allocations are
+// first made resident by a few threads touching one byte per page (the
+// kernel's first-touch faults are the slow part); mc_search does that while
+// the emit and search kernels run.
+void prefault(void* ptr, size_t bytes) {
+    if (!ptr || !bytes) return;
+    static const size_t page = std::max<long>(4096, sysconf(_SC_PAGESIZE));
+    const uintptr_t lo = (uintptr_t)ptr, hi = lo + bytes;
+    const size_t npages = (hi - (lo & ~(uintptr_t)(page - 1)) + page - 1) / page;
+    auto touch = [=](size_t a, size_t b) {
+        for (size_t i = a; i < b; i++) {
+            const uintptr_t q = std::max(lo, (lo & ~(uintptr_t)(page - 1)) + i * page);
+            *(volatile char*)q = 0;
+        }
+    };
+    const int nt = (int)std::min<size_t>(8, npages / 64);
+    if (nt <= 1) {
+        touch(0, npages);
         return;
     }
     std::vector<std::thread> ts;
-    const size_t per = (n + nt - 1) / nt;
+    const size_t per = (npages + nt - 1) / nt;
     for (int t = 0; t < nt; t++) {
-        const size_t a = t * per, b = std::min(n, a + per);
-        if (a < b) ts.emplace_back([=] { std::memcpy((char*)dst + a, (const char*)src + a, b - a); });
+        const size_t a = t * per, b = std::min(npages, a + per);
+        if (a < b) ts.emplace_back(touch, a, b);
     }
     for (auto& t : ts) t.join();
 }
 
-mc_status staged_d2h(mc_ctx* ctx, void* dst, const void* src, size_t bytes) {
-    if (!bytes) return MC_OK;
-    for (int b = 0; b < 2; b++) {
-        if (!ctx->stage[b]) CK(cudaHostAlloc((void**)&ctx->stage[b], kStageBytes, cudaHostAllocDefault));
-        if (!ctx->stage_ev[b]) CK(cudaEventCreateWithFlags(&ctx->stage_ev[b], cudaEventDisableTiming));
-    }
-    size_t pend_off[2] = {0, 0}, pend_len[2] = {0, 0};
-    int i = 0;
-    for (size_t off = 0; off < bytes; off += kStageBytes, i++) {
-        const int b = i & 1;
-        if (pend_len[b]) {
-            CK(cudaEventSynchronize(ctx->stage_ev[b]));
-            host_copy((char*)dst + pend_off[b], ctx->stage[b], pend_len[b]);
-        }
-        const size_t len = std::min(kStageBytes, bytes - off);
-        CK(cudaMemcpyAsync(ctx->stage[b], (const char*)src + off, len, cudaMemcpyDeviceToHost, ctx->stream));
-        CK(cudaEventRecord(ctx->stage_ev[b], ctx->stream));
-        pend_off[b] = off;
-        pend_len[b] = len;
-    }
-    for (int k = 0; k < 2; k++) {
-        const int b = (i + k) & 1;
-        if (pend_len[b]) {
-            CK(cudaEventSynchronize(ctx->stage_ev[b]));
-            host_copy((char*)dst + pend_off[b], ctx->stage[b], pend_len[b]);
-            pend_len[b] = 0;
-        }
-    }
+mc_status enqueue_mesh_copy(mc_ctx* ctx, double* vertices, int32_t* triangles) {
+    if (vertices && ctx->last_V)
+        CK(cudaMemcpyAsync(vertices, ctx->verts.p, (size_t)ctx->last_V * 24, cudaMemcpyDeviceToHost, ctx->stream));
+    if (triangles && ctx->last_T)
+        CK(cudaMemcpyAsync(triangles, ctx->tris.p, (size_t)ctx->last_T * 12, cudaMemcpyDeviceToHost, ctx->stream));
     return MC_OK;
 }
 }  // namespace
@@ -2132,30 +2170,42 @@ mc_status staged_d2h(mc_ctx* ctx, void* dst, const void* src, size_t bytes) {
 mc_status mc_result_copy(mc_ctx* ctx, double* vertices, int32_t* triangles) {
     if (!ctx) return MC_ERR_ARG;
     CK(cudaSetDevice(ctx->device));
-    mc_status st = MC_OK;
-    if (vertices && ctx->last_V) st = staged_d2h(ctx, vertices, ctx->verts.p, (size_t)ctx->last_V * 24);
-    if (st == MC_OK && triangles && ctx->last_T) st = staged_d2h(ctx, triangles, ctx->tris.p, (size_t)ctx->last_T * 12);
-    return st;
+    if (vertices) prefault(vertices, (size_t)ctx->last_V * 24);
+    if (triangles) prefault(triangles, (size_t)ctx->last_T * 12);
+    mc_status st = enqueue_mesh_copy(ctx, vertices, triangles);
+    if (st != MC_OK) return st;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MC_OK;
 }
 
 mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters, const mc_opts* opts,
                     mc_mesh* out) {
     if (!out) return fail(ctx, MC_ERR_ARG, "null output");
     std::memset(out, 0, sizeof(*out));
-    int64_t V = 0, T = 0;
-    mc_status s = mc_search_device(ctx, solid, delta, iters, opts, &V, &T, &out->stats);
+    mc_stats st{};
+    mc_status s = search_launch(ctx, solid, delta, iters, opts, &st);
     if (s != MC_OK) return s;
+    const int64_t V = st.vertices, T = st.triangles;
+    ctx->last_V = V;
+    ctx->last_T = T;
     out->vertices = (double*)std::malloc(std::max<int64_t>(V, 1) * 24);
     out->triangles = (int32_t*)std::malloc(std::max<int64_t>(T, 1) * 12);
     if (!out->vertices || !out->triangles) {
+        cudaStreamSynchronize(ctx->stream);
         mc_mesh_free(out);
         return fail(ctx, MC_ERR_OOM, "host allocation failed");
     }
-    s = mc_result_copy(ctx, out->vertices, out->triangles);
+    // Emit and search run on the device meanwhile.
+    prefault(out->vertices, (size_t)V * 24);
+    prefault(out->triangles, (size_t)T * 12);
+    s = enqueue_mesh_copy(ctx, out->vertices, out->triangles);
+    mc_status f = search_finish(ctx, &st);
+    if (s == MC_OK) s = f;
     if (s != MC_OK) {
         mc_mesh_free(out);
         return s;
     }
+    out->stats = st;
     out->n_vertices = V;
     out->n_triangles = T;
     out->stats.d2h_bytes += V * 24 + T * 12;
@@ -2192,7 +2242,6 @@ mc_status mc_contains(mc_ctx* ctx, const mc_solid* solid, const double* points, 
     CK(cudaMemcpyAsync(out, ctx->pout.p, n, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_pin + 2, ctx->errs.p, ER_N * 4, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    if (((const int*)(ctx->h_pin + 2))[ER_LIMIT]) return fail(ctx, MC_ERR_LIMIT, "collider traversal stack exceeded");
     return MC_OK;
 }
 
@@ -2559,7 +2608,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             const int* e = &herr[d * ER_N];
             st = e[ER_BORDER] ? MC_ERR_BOUNDS_INSIDE
                               : e[ER_NOT_ON_EDGE] ? MC_ERR_NOT_ON_EDGE
-                                                  : e[ER_EDGE_INDEX] ? MC_ERR_EDGE_INDEX : e[ER_LIMIT] ? MC_ERR_LIMIT : MC_OK;
+                                                  : e[ER_EDGE_INDEX] ? MC_ERR_EDGE_INDEX : MC_OK;
         }
         if (job_status) job_status[i] = st;
         if (st != MC_OK) {
@@ -2828,6 +2877,5 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         return MC_ERR_CUDA;
     if (herr[ER_NOT_ON_EDGE]) return MC_ERR_NOT_ON_EDGE;
     if (herr[ER_EDGE_INDEX]) return MC_ERR_EDGE_INDEX;
-    if (herr[ER_LIMIT]) return MC_ERR_LIMIT;
     return MC_OK;
 }

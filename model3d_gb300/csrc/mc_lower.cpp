@@ -250,6 +250,142 @@ struct TreeBuilder {
     D3 bounds_max(int c) { return c >= 0 ? nodes[c].mx : tris[-c - 1].mx; }
 };
 
+// ---------------------------------------------------------------- ray grid
+
+// Cells and entries of one tree's ray grid (layout and exactness argument at
+// RayEnt in mc_internal.h).  Pads: the float projection of a ray origin inside
+// the tree's bounds (|coordinate| <= R) errs by less than 5e-7 (R + 1) in a,
+// b and t.  The reference's float64 Moller-Trumbore test reports a hit only
+// within 50 eps (R + 1)(kappa1 + kappa2) of the triangle, in the projected
+// plane and in t, where kappa1 = |v1||v2||D| / |det| bounds the relative
+// error of det and kappa2 = max |e| / |e projected| over the edges; the pads
+// below are 8 and 20 times larger.  Triangles with 7 eps kappa1 > 1e-3,
+// whose det sign the float64 test may get wrong, are tested by every ray.
+void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, int tri_base, double R,
+                    HostProgram* P, TreeD* tree) {
+    const double eps = DBL_EPSILON / 2;
+    const D3 dh = vnormalize(kRay);
+    const double dlen = vnorm(kRay);
+    struct Box {
+        double alo, ahi, blo, bhi;
+        float maxt;
+        int tri;
+    };
+    std::vector<Box> boxes;
+    boxes.reserve(order.size());
+    std::vector<int> all;
+    std::vector<double> sizes;
+    sizes.reserve(order.size());
+    for (size_t i = 0; i < order.size(); i++) {
+        if (!P->tris[tri_base + i].valid) continue;  // parallel or det == 0: never hit
+        const Tri& tr = t[order[i]];
+        const D3 v1 = vsub(tr.p[1], tr.p[0]), v2 = vsub(tr.p[2], tr.p[0]);
+        const double det = std::fabs(vdot(vcross(kRay, v2), v1));
+        const double k1 = vnorm(v1) * vnorm(v2) * dlen / det;
+        double k2 = 0;
+        for (int e = 0; e < 3; e++) {
+            const D3 ev = vsub(tr.p[(e + 1) % 3], tr.p[e]);
+            const D3 perp = vsub(ev, vscale(dh, vdot(ev, dh)));
+            const double n = vnorm(ev), np = vnorm(perp);
+            if (n > 0) k2 = std::max(k2, n / np);
+        }
+        if (!(7 * eps * k1 <= 1e-3) || !std::isfinite(k2)) {
+            all.push_back(tri_base + (int)i);
+            continue;
+        }
+        const double pad = (R + 1) * (4e-6 + 1e3 * eps * (k1 + k2));
+        Box b{DBL_MAX, -DBL_MAX, DBL_MAX, -DBL_MAX, 0.f, tri_base + (int)i};
+        double mt = -DBL_MAX;
+        for (int k = 0; k < 3; k++) {
+            const D3& v = tr.p[k];
+            const double a = v.v[1] - RAYGRID_KY * v.v[0], bb = v.v[2] - RAYGRID_KZ * v.v[0];
+            b.alo = std::min(b.alo, a);
+            b.ahi = std::max(b.ahi, a);
+            b.blo = std::min(b.blo, bb);
+            b.bhi = std::max(b.bhi, bb);
+            mt = std::max(mt, v.v[0] * RAYGRID_INV_DX);
+        }
+        sizes.push_back(std::max(b.ahi - b.alo, b.bhi - b.blo));
+        b.alo -= pad;
+        b.ahi += pad;
+        b.blo -= pad;
+        b.bhi += pad;
+        b.maxt = f_up(mt + pad * (1 + RAYGRID_INV_DX));
+        if (!std::isfinite(b.alo + b.ahi + b.blo + b.bhi)) {
+            all.push_back(tri_base + (int)i);
+            continue;
+        }
+        boxes.push_back(b);
+    }
+    double amin = 0, amax = 0, bmin = 0, bmax = 0;
+    if (!boxes.empty()) {
+        amin = bmin = DBL_MAX;
+        amax = bmax = -DBL_MAX;
+        for (const Box& b : boxes) {
+            amin = std::min(amin, b.alo);
+            amax = std::max(amax, b.ahi);
+            bmin = std::min(bmin, b.blo);
+            bmax = std::max(bmax, b.bhi);
+        }
+    }
+    // Cell edge: half the median triangle extent (about six cells per
+    // triangle), at most 32000 cells per axis and 2^24 cells.
+    double cs = 0;
+    if (!sizes.empty()) {
+        std::nth_element(sizes.begin(), sizes.begin() + sizes.size() / 2, sizes.end());
+        cs = 0.5 * sizes[sizes.size() / 2];
+    }
+    const double ea = amax - amin, eb = bmax - bmin;
+    cs = std::max({cs, ea / 32000, eb / 32000, std::sqrt(ea * eb / (double)(1 << 24)), 1e-300});
+    if (!(cs > 0) || !std::isfinite(cs)) cs = 1;
+    const float inv_f = (float)(1 / cs);
+    const double inv = inv_f;
+    const float amin_f = f_down(amin), bmin_f = f_down(bmin);
+    const int ga = boxes.empty() ? 1 : (int)std::floor((amax - amin_f) * inv) + 1;
+    const int gb = boxes.empty() ? 1 : (int)std::floor((bmax - bmin_f) * inv) + 1;
+    // The device's float cell index errs by far less than 0.05 cells.
+    auto cell_range = [&](double lo, double hi, float org, int n, int* c0, int* c1) {
+        *c0 = std::max(0, (int)std::floor((lo - org) * inv - 0.05));
+        *c1 = std::min(n - 1, (int)std::floor((hi - org) * inv + 0.05));
+    };
+    const size_t ncell = (size_t)ga * gb;
+    std::vector<int64_t> cnt(ncell + 1, 0);
+    for (const Box& b : boxes) {
+        int a0, a1, b0, b1;
+        cell_range(b.alo, b.ahi, amin_f, ga, &a0, &a1);
+        cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
+        for (int y = b0; y <= b1; y++)
+            for (int x = a0; x <= a1; x++) cnt[(size_t)y * ga + x + 1]++;
+    }
+    for (size_t c = 0; c < ncell; c++) cnt[c + 1] += cnt[c];
+    const int64_t base = (int64_t)P->ents.size();
+    if (base + cnt[ncell] + (int64_t)all.size() >= ((int64_t)1 << 31))
+        throw LowerError(MC_ERR_LIMIT, "collider ray grid exceeds 2^31 entries");
+    P->ents.resize(base + cnt[ncell]);
+    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+    for (const Box& b : boxes) {
+        int a0, a1, b0, b1;
+        cell_range(b.alo, b.ahi, amin_f, ga, &a0, &a1);
+        cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
+        for (int y = b0; y <= b1; y++)
+            for (int x = a0; x <= a1; x++) P->ents[base + fill[(size_t)y * ga + x]++] = RayEnt{b.maxt, b.tri};
+    }
+    for (size_t c = 0; c < ncell; c++)
+        std::sort(P->ents.begin() + base + cnt[c], P->ents.begin() + base + cnt[c + 1],
+                  [](const RayEnt& x, const RayEnt& y) { return x.maxt < y.maxt || (x.maxt == y.maxt && x.tri < y.tri); });
+    tree->cell_base = (int32_t)P->cell_start.size();
+    tree->n_cells = (int32_t)ncell;
+    for (size_t c = 0; c <= ncell; c++) P->cell_start.push_back((int32_t)(base + cnt[c]));
+    tree->all_first = (int32_t)P->ents.size();
+    tree->all_count = (int32_t)all.size();
+    for (int i : all) P->ents.push_back(RayEnt{INFINITY, i});
+    tree->amin = amin_f;
+    tree->bmin = bmin_f;
+    tree->inv_cs = inv_f;
+    tree->ga = ga;
+    tree->gb = gb;
+}
+
 // ---------------------------------------------------------------- lowering
 
 struct Lowerer {
@@ -350,14 +486,12 @@ struct Lowerer {
             P->tris.push_back(d);
             P->tris_f.push_back(f);
         }
-        if (ts.n == 1) {
-            tree.kind = 2;
-            tree.root = tri_base;
-        } else if (ts.n > 1) {
+        P->tri_parent.resize(P->tris.size(), -1);
+        if (ts.n > 1) {
             TreeBuilder tb{t, {}};
             int root = tb.build(order.data(), order.size());
             int node_base = (int)P->nodes.size();
-            // Breadth-first relabelling keeps siblings adjacent.
+            // Breadth-first order keeps the upper levels together.
             std::vector<int> label(tb.nodes.size(), -1), queue = {root};
             label[root] = 0;
             for (size_t qi = 0; qi < queue.size(); qi++)
@@ -372,31 +506,29 @@ struct Lowerer {
                 const BNode& b = tb.nodes[queue[qi]];
                 BvhNodeD nd{};
                 BvhNodeF nf{};
-                nd.first = (int)P->child.size();
-                nd.count = (int)b.ch.size();
                 for (int k = 0; k < 3; k++) {
                     nd.lo[k] = b.mn.v[k];
                     nd.hi[k] = b.mx.v[k];
                     nf.lo[k] = f_down(b.mn.v[k]);
                     nf.hi[k] = f_up(b.mx.v[k]);
                 }
-                nf.first = nd.first;
-                nf.count = nd.count;
                 for (int c : b.ch)
-                    P->child.push_back(c >= 0 ? node_base + label[c] : -(tri_base + pos_of[-c - 1] + 1));
+                    if (c < 0) P->tri_parent[tri_base + pos_of[-c - 1]] = node_base + (int)qi;
                 P->nodes[node_base + qi] = nd;
                 P->nodes_f[node_base + qi] = nf;
             }
-            tree.kind = 1;
-            tree.root = node_base;
         }
-        // Coordinate magnitude bound for the FP32 ray-box filter.
+        tree.kind = ts.n > 0 ? 1 : 0;
+        // Coordinate magnitude bound for the FP32 ray-box filter and the pads.
+        double R = 0;
         for (int a = 0; a < 3; a++) {
             double m = 0;
             for (const Tri& tr : t)
                 m = std::max(m, std::max(std::fabs(tr.mn.v[a]), std::fabs(tr.mx.v[a])));
             tree.mbox[a] = f_up(m);
+            R = std::max(R, m);
         }
+        build_ray_grid(t, order, tri_base, R, P, &tree);
         int id = (int)P->trees.size();
         P->trees.push_back(tree);
         tree_of_set[set] = id;

@@ -31,7 +31,9 @@ struct HostProgram {
     std::vector<TreeD> trees;
     std::vector<BvhNodeD> nodes;
     std::vector<BvhNodeF> nodes_f;
-    std::vector<int32_t> child;
+    std::vector<int32_t> tri_parent;
+    std::vector<int32_t> cell_start;
+    std::vector<RayEnt> ents;
     std::vector<TriD> tris;
     std::vector<TriF> tris_f;
     double root_min[3] = {0, 0, 0}, root_max[3] = {0, 0, 0};

@@ -158,6 +158,34 @@ def _as_device_solid(solid, ctx):
     return DeviceSolid(solid, ctx)
 
 
+class _HostMesh:
+    """Owner of the library-allocated host arrays of one mc_mesh; the numpy
+    arrays of a Mesh keep it alive and it frees them (mc_mesh_free) last."""
+
+    def __init__(self, m):
+        self.m = N.MCMesh()
+        ctypes.pointer(self.m)[0] = m
+
+    def arrays(self):
+        m = self.m
+
+        def view(ptr, n, ctype, dtype):
+            if n == 0:
+                return np.zeros((0, 3), dtype)
+            buf = (ctype * (3 * n)).from_address(ctypes.cast(ptr, ctypes.c_void_p).value)
+            buf._owner = self
+            return np.frombuffer(buf, dtype=dtype).reshape(n, 3)
+
+        return (view(m.vertices, m.n_vertices, ctypes.c_double, np.float64),
+                view(m.triangles, m.n_triangles, ctypes.c_int32, np.int32))
+
+    def __del__(self):
+        try:
+            N.lib().mc_mesh_free(ctypes.byref(self.m))
+        except Exception:
+            pass
+
+
 def MarchingCubesSearch(solid, delta: float, iters: int, *, precision: str = "fp32",
                         cull: bool = True, ctx: Optional[Context] = None, tile_y: int = 0,
                         tile_z: int = 0) -> Mesh:
@@ -165,17 +193,11 @@ def MarchingCubesSearch(solid, delta: float, iters: int, *, precision: str = "fp
     ctx = ctx or (solid.ctx if isinstance(solid, DeviceSolid) else default_context())
     ds = _as_device_solid(solid, ctx)
     o = _opts(precision, cull, tile_y, tile_z)
-    V, T = ctypes.c_int64(), ctypes.c_int64()
-    st = N.MCStats()
-    L = N.lib()
-    _check(L.mc_search_device(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
-                              ctypes.byref(V), ctypes.byref(T), ctypes.byref(st)), ctx.ptr)
-    verts = np.empty((V.value, 3), dtype=np.float64)
-    tris = np.empty((T.value, 3), dtype=np.int32)
-    _check(L.mc_result_copy(ctx.ptr, verts.ctypes.data, tris.ctypes.data), ctx.ptr)
-    stats = st.as_dict()
-    stats["d2h_bytes"] += verts.nbytes + tris.nbytes
-    return Mesh(verts, tris, stats)
+    m = N.MCMesh()
+    _check(N.lib().mc_search(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
+                             ctypes.byref(m)), ctx.ptr)
+    verts, tris = _HostMesh(m).arrays()
+    return Mesh(verts, tris, m.stats.as_dict())
 
 
 def MarchingCubesSearchBatch(jobs, *, precision: str = "fp32", cull: bool = True,
@@ -201,12 +223,8 @@ def MarchingCubesSearchBatch(jobs, *, precision: str = "fp32", cull: bool = True
         if status[i] != N.MC_OK:
             res.append(MCError(status[i]))
             continue
-        m = outs[i]
-        V, T = m.n_vertices, m.n_triangles
-        verts = np.ctypeslib.as_array(m.vertices, shape=(max(V, 1) * 3,))[:V * 3].reshape(V, 3).copy()
-        tris = np.ctypeslib.as_array(m.triangles, shape=(max(T, 1) * 3,))[:T * 3].reshape(T, 3).copy()
-        res.append(Mesh(verts, tris, m.stats.as_dict()))
-        N.lib().mc_mesh_free(ctypes.byref(m))
+        verts, tris = _HostMesh(outs[i]).arrays()
+        res.append(Mesh(verts, tris, outs[i].stats.as_dict()))
     if st != N.MC_OK and all(not isinstance(r, MCError) for r in res):
         raise MCError(st, N.lib().mc_last_error(ctx.ptr).decode())
     return res

@@ -476,21 +476,22 @@ def GroupBounders(objs: List[Solid]) -> List[Solid]:
 # ------------------------------------------------------------ serialisation
 
 def serialize(solid: Solid):
-    """Prefix-order mc_node records and the triangle sets they refer to."""
+    """Prefix-order mc_node records and the triangle sets they refer to.
+
+    Min()/Max() are computed for the nodes whose bounds the library reads:
+    the root, colliders, transforms and checked solids."""
     recs = []
     sets: List[MeshCollider] = []
     set_ids = {}
+    zero3 = (0.0, 0.0, 0.0)
 
     def node(kind, s=None, n_children=0, n_steps=0, mesh=0, p=()):
-        r = np.zeros((), dtype=NODE_DTYPE)
-        r["kind"], r["n_children"], r["n_steps"], r["mesh"] = kind, n_children, n_steps, mesh
-        if s is not None:
-            r["min"] = s.Min().Array()
-            r["max"] = s.Max().Array()
-        pp = np.zeros(12)
-        pp[:len(p)] = p
-        r["p"] = pp
-        recs.append(r)
+        if s is not None and (not recs or kind in (COLLIDER, TRANSFORM, CHECKED)):
+            mn, mx = tuple(s.Min().Array()), tuple(s.Max().Array())
+        else:
+            mn = mx = zero3
+        pp = tuple(p) + (0.0,) * (12 - len(p))
+        recs.append((kind, n_children, n_steps, mesh, mn, mx, pp))
 
     def emit(s):
         if isinstance(s, Sphere):

@@ -251,3 +251,50 @@ def test_collider_contains_parity(oracle, prec):
     pts = np.concatenate(pts)
     ref, _ = oracle.contains(nodes, sets, pts)
     assert (Contains(s, pts, precision=prec) == ref).all()
+
+
+RAY_D = np.array([0.5224892708603626, 0.10494477243214506, 0.43558938446126527])
+
+
+def _grazing_mesh(rng):
+    """Triangles that stress the ray grid: a displaced icosphere, slivers
+    nearly parallel to the containment ray, tiny triangles and a duplicate."""
+    tris = [displaced_icosphere(5)]
+    d = RAY_D / np.linalg.norm(RAY_D)
+    for k in range(40):
+        p0 = rng.uniform(-0.8, 0.8, 3)
+        side = np.cross(d, rng.normal(size=3))
+        side /= np.linalg.norm(side)
+        tilt = 10.0 ** rng.uniform(-7.5, -2)  # angle off the ray direction
+        p1 = p0 + 0.3 * (d + tilt * np.cross(d, side))
+        p2 = p0 + 0.2 * side
+        tris.append(np.concatenate([p0, p1, p2])[None])
+    for k in range(40):
+        p0 = rng.uniform(-0.8, 0.8, 3)
+        tris.append(np.concatenate([p0, p0 + 1e-6 * rng.normal(size=3), p0 + 1e-6 * rng.normal(size=3)])[None])
+    t = np.concatenate(tris)
+    return np.concatenate([t, t[:3]])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_collider_grazing_rays(oracle, prec):
+    """Rays aimed exactly at triangle vertices, edge points and sliver
+    triangles nearly parallel to the ray: the ray-grid candidates and the
+    parent-box test reproduce the reference's traversal count."""
+    rng = np.random.default_rng(23)
+    tris = _grazing_mesh(rng)
+    s = NewColliderSolid(MeshToCollider(tris))
+    nodes, sets = serialize(s)
+    t = tris.reshape(-1, 3, 3)
+    targets = [t.reshape(-1, 3),                                   # vertices
+               0.5 * (t[:, 0] + t[:, 1]), 0.5 * (t[:, 1] + t[:, 2]),  # edge midpoints
+               (t * rng.dirichlet([1, 1, 1], size=len(t))[:, :, None]).sum(1)]
+    targets = np.concatenate(targets)
+    s_back = rng.uniform(0.0, 0.6, size=(len(targets), 1))
+    pts = targets - s_back * RAY_D[None]
+    pts = np.concatenate([pts, np.nextafter(pts, np.inf), np.nextafter(pts, -np.inf), targets])
+    ref, _ = oracle.contains(nodes, sets, pts)
+    got = Contains(s, pts, precision=prec)
+    bad = np.nonzero(got != ref)[0]
+    assert len(bad) == 0, f"{len(bad)} of {len(pts)} differ, first {pts[bad[:3]]}"
+    _check(oracle, s, 0.05, 8, modes=[(prec, True)])
