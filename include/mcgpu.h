@@ -2,19 +2,22 @@
  * mcgpu.h — C ABI of the GB300 marching-cubes library (libmcgpu.so).
  *
  * This is the drop-in boundary for model3d's MarchingCubesSearch path
- * (model3d/mc.go:45-49).  A host-language wrapper (the Go cgo binding shown
- * in INTEGRATION.md, the Python mirror in model3d_gb300/, or a C++ caller)
- * serialises its Solid tree into an array of mc_node records, the library
- * lowers it to a device program (CSG bytecode + flattened collider BVH), runs
- * corner classification, cube classification, compaction and the edge
- * bisection search on one GPU, and returns an indexed mesh.
+ * (model3d/mc.go:45-49).  A host-language wrapper (a Go cgo binding, the
+ * Python mirror in model3d_gb300/, or a C++ caller) serialises its Solid tree
+ * into an array of mc_node records, the library lowers it to a device
+ * program (CSG bytecode; collider meshes as the reference's BVH boxes plus a
+ * ray grid of candidate triangles), runs corner classification, cube
+ * classification, compaction and the edge bisection search on one GPU, and
+ * returns an indexed mesh.
  *
  * Plain C types only: pointers and sizes.  Inputs are borrowed for the
  * duration of a call.  Solids that cannot be lowered return
  * MC_ERR_NOT_LOWERABLE; there is no CPU fallback.
  *
  * Threading: one mc_ctx per host thread.  Each context owns a CUDA stream
- * and grow-only device buffers; every call is synchronous on return.
+ * and grow-only device buffers; every call is synchronous on return.  Destroy
+ * a context's solids before the context (mc_solid_destroy may run on any
+ * thread).
  */
 #ifndef MCGPU_H
 #define MCGPU_H

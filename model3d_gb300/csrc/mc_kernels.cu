@@ -835,14 +835,47 @@ __device__ __forceinline__ void block_sum2(uint32_t& a, uint32_t& b) {
     }
 }
 
+// Chunk space order.  Chunks (32 cubes of one row) are numbered tile by
+// tile: z-blocks of kChunkTZ cube planes, in each y-blocks of kChunkTY rows,
+// in each the 32-cube columns, in each the rows.  Vertex and triangle ids
+// follow the chunk order, so consecutive vertices -- the 32 that one warp of
+// the search bisects together -- stay within a few rows of one tile rather
+// than spreading along whole grid rows, and the warp's culled program keeps
+// fewer leaves.  A grid has at most 2^31 corners, so chunk indices fit int.
+constexpr int kChunkTY = 8, kChunkTZ = 8;
+
+__device__ __forceinline__ int chunk_index(const GridView& g, int c, int y, int z) {
+    const int nyc = g.ny - 1, nzc = g.nz - 1;
+    const int zb = z / kChunkTZ, yb = y / kChunkTY;
+    const int hz = min(kChunkTZ, nzc - zb * kChunkTZ), hy = min(kChunkTY, nyc - yb * kChunkTY);
+    return zb * kChunkTZ * nyc * g.CX + yb * kChunkTY * hz * g.CX + c * hy * hz + (z - zb * kChunkTZ) * hy +
+           (y - yb * kChunkTY);
+}
+
+__device__ __forceinline__ void chunk_coords(const GridView& g, int i, int* c, int* y, int* z) {
+    const int nyc = g.ny - 1, nzc = g.nz - 1;
+    const int zslab = kChunkTZ * nyc * g.CX;
+    const int zb = i / zslab;
+    int r = i - zb * zslab;
+    const int hz = min(kChunkTZ, nzc - zb * kChunkTZ);
+    const int yslab = kChunkTY * hz * g.CX;
+    const int yb = r / yslab;
+    r -= yb * yslab;
+    const int hy = min(kChunkTY, nyc - yb * kChunkTY);
+    const int col = hy * hz;
+    *c = r / col;
+    const int q = r - *c * col;
+    *z = zb * kChunkTZ + q / hy;
+    *y = yb * kChunkTY + q % hy;
+}
+
 // Counts of one 32-cube chunk (local index i of the grid's chunk space):
 // crossed x/y/z edges with base corner in the chunk and triangles of its
 // active cubes, packed as cx | cy << 6 | cz << 12 | ntri << 18.
 __device__ __forceinline__ uint32_t count_chunk(const GridView& g, const uint32_t* bits, long long i, uint32_t& nv,
                                                 uint32_t& nt) {
-    const int c = (int)(i % g.CX);
-    const long long r = i / g.CX;
-    const int y = (int)(r % (g.ny - 1)), z = (int)(r / (g.ny - 1));
+    int c, y, z;
+    chunk_coords(g, (int)i, &c, &y, &z);
     Rows R = load_rows(g, bits, c, y, z);
     const uint32_t vm = valid_mask(g, c);
     uint32_t cp[8];
@@ -974,9 +1007,8 @@ struct EmitArgs {
 __device__ __forceinline__ void emit_chunk(const GridView& g, const EmitArgs& a, long long i, uint32_t vsub) {
     uint32_t pk = a.packed[i];
     if (pk == 0) return;
-    const int c = (int)(i % g.CX);
-    const long long r = i / g.CX;
-    const int y = (int)(r % (g.ny - 1)), z = (int)(r / (g.ny - 1));
+    int c, y, z;
+    chunk_coords(g, (int)i, &c, &y, &z);
     Rows R = load_rows(g, a.bits, c, y, z);
     const uint32_t vm = valid_mask(g, c);
     uint32_t cp[8];
@@ -1002,11 +1034,10 @@ __device__ __forceinline__ void emit_chunk(const GridView& g, const EmitArgs& a,
     // rows (y+dy, z+dz) at word c, and rows (y, z+dz) / (y+dy, z) at word c+1.
     // A crossed edge never has its base corner on the last grid plane, so
     // only the chunks inside the cube index space are read.
-    const long long rowC = (long long)(g.ny - 1);
     auto base = [&](int dy, int dz, int w, uint32_t* bx, uint32_t* by, uint32_t* bz) {
         *bx = *by = *bz = 0;
         if (y + dy > g.ny - 2 || z + dz > g.nz - 2 || c + w >= g.CX) return;
-        const long long ci = ((long long)(z + dz) * rowC + (y + dy)) * g.CX + c + w;
+        const int ci = chunk_index(g, c + w, y + dy, z + dz);
         const uint32_t pv = a.prefv[ci], pn = a.packed[ci];
         *bx = pv;
         *by = pv + (pn & 63u);
