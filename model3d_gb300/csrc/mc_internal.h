@@ -180,6 +180,39 @@ struct ProgView {
     int32_t fold_cap; // longest folded program (words)
 };
 
+// ---- Bisection arithmetic on float64 bit patterns.
+// When both ends of a search edge have the same sign and exponent field E
+// (every double between them does too) the reference's midpoint
+// (f + t) / 2 is a pure mantissa operation: with K = (2^52 + M_f) +
+// (2^52 + M_t) in [2^53, 2^54 - 2], f + t rounds to RNE(K / 2) at exponent
+// E + 1 and the halving is exact, so the midpoint is RNE(K / 2) at exponent
+// E (no carry out: K / 2 < 2^53).  E must keep f + t finite (E <= 0x7fd).
+// The float rounding of such a value is RNE of its 53-bit significand to 24
+// bits at float exponent E - 896, exact for E in [897, 1150] (normal floats;
+// a carry out of the significand bumps the exponent, up to infinity).
+constexpr unsigned long long kFrac52 = (1ull << 52) - 1;
+
+__host__ __device__ inline bool bisect_bits_ok(unsigned long long a, unsigned long long b) {
+    const unsigned long long e = (a >> 52) & 0x7ff;
+    return (a >> 52) == (b >> 52) && e >= 897 && e <= 1150;
+}
+
+__host__ __device__ inline unsigned long long mid_bits(unsigned long long a, unsigned long long b) {
+    const unsigned long long K = (a & kFrac52) + (b & kFrac52) + (1ull << 53);
+    const unsigned long long h = K >> 1;
+    const unsigned long long m = h + (K & h & 1ull);  // ties to even
+    return (a & ~kFrac52) | (m & kFrac52);
+}
+
+__host__ __device__ inline uint32_t float_bits_of(unsigned long long d) {
+    const unsigned long long M = (d & kFrac52) | (1ull << 52);
+    unsigned long long m24 = M >> 29;
+    const unsigned long long rem = M & ((1ull << 29) - 1);
+    m24 += (rem > (1ull << 28) || (rem == (1ull << 28) && (m24 & 1ull))) ? 1ull : 0ull;
+    const uint32_t fe = (uint32_t)((d >> 52) & 0x7ff) - 896u;
+    return ((uint32_t)(d >> 63) << 31) | ((fe << 23) + (uint32_t)m24 - (1u << 23));
+}
+
 // Constant folding of a postfix program given which leaves are active
 // (inactive leaves are known false over the region being evaluated).
 // Writes the pruned program to q and returns its length, or FOLD_FALSE /

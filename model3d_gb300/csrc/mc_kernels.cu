@@ -199,25 +199,30 @@ __device__ bool eval_program(const ProgView& P, const uint32_t* q, int nq, P3 p,
         uint32_t op = q[i];
         uint32_t arg = op_arg(op);
         switch (op_code(op)) {
-            case OP_LEAF: st = (st << 1) | (eval_leaf<PREC>(P, arg, p, pf, cnt, err) ? 1u : 0u); break;
+            case OP_LEAF:
             case OP_JLEAVES:
-            case OP_ALEAVES: {  // short-circuit OR / AND over a leaf range
-                const uint32_t a0 = range_first(arg), e = a0 + range_count(arg);
-                const bool isor = op_code(op) == OP_JLEAVES;
+            case OP_ALEAVES:
+            case OP_JLIST: {
+                // Short-circuit OR (AND for ALEAVES) over one leaf, a leaf
+                // range or a leaf list; one call site keeps the code small.
+                const uint32_t code = op_code(op);
+                uint32_t first = arg, count = 1;
+                const uint32_t* list = nullptr;
+                if (code == OP_JLEAVES || code == OP_ALEAVES) {
+                    first = range_first(arg);
+                    count = range_count(arg);
+                } else if (code == OP_JLIST) {
+                    list = q + i + 1;
+                    count = arg;
+                    i += arg;
+                }
+                const bool isor = code != OP_ALEAVES;
                 bool v = !isor;
-                for (uint32_t l = a0; l < e; l++)
-                    if (eval_leaf<PREC>(P, l, p, pf, cnt, err) == isor) {
+                for (uint32_t k = 0; k < count; k++)
+                    if (eval_leaf<PREC>(P, list ? list[k] : first + k, p, pf, cnt, err) == isor) {
                         v = isor;
                         break;
                     }
-                st = (st << 1) | (v ? 1u : 0u);
-                break;
-            }
-            case OP_JLIST: {
-                bool v = false;
-                for (uint32_t k = 0; k < arg; k++)
-                    if (!v) v = eval_leaf<PREC>(P, q[i + 1 + k], p, pf, cnt, err);
-                i += arg;
                 st = (st << 1) | (v ? 1u : 0u);
                 break;
             }
@@ -519,25 +524,33 @@ __device__ uint32_t eval_program_rows(const ProgView& P, const uint32_t* q, int 
     for (int i = 0; i < nq; i++) {
         const uint32_t op = q[i], arg = op_arg(op);
         switch (op_code(op)) {
-            case OP_LEAF: stk[sp++] = leaf_rows<PREC>(P, arg, rc, cnt, err); break;
-            case OP_JLEAVES: {
-                const uint32_t a0 = range_first(arg), e = a0 + range_count(arg);
-                uint32_t m = 0;
-                for (uint32_t l = a0; l < e; l++) m |= leaf_rows<PREC>(P, l, rc, cnt, err);
-                stk[sp++] = m;
-                break;
-            }
-            case OP_ALEAVES: {
-                const uint32_t a0 = range_first(arg), e = a0 + range_count(arg);
-                uint32_t m = 0xffffffffu;
-                for (uint32_t l = a0; l < e; l++) m &= leaf_rows<PREC>(P, l, rc, cnt, err);
-                stk[sp++] = m;
-                break;
-            }
+            case OP_LEAF:
+            case OP_JLEAVES:
+            case OP_ALEAVES:
             case OP_JLIST: {
-                uint32_t m = 0;
-                for (uint32_t k = 0; k < arg; k++) m |= leaf_rows<PREC>(P, q[i + 1 + k], rc, cnt, err);
-                i += arg;
+                // OR (AND for ALEAVES) of the row masks of one leaf, a leaf
+                // range or a leaf list, stopping once every lane's mask is
+                // decided (the check is warp-uniform: leaf_rows shuffles).
+                const uint32_t code = op_code(op);
+                uint32_t first = arg, count = 1;
+                const uint32_t* list = nullptr;
+                if (code == OP_JLEAVES || code == OP_ALEAVES) {
+                    first = range_first(arg);
+                    count = range_count(arg);
+                } else if (code == OP_JLIST) {
+                    list = q + i + 1;
+                    count = arg;
+                    i += arg;
+                }
+                const bool isand = code == OP_ALEAVES;
+                uint32_t m = isand ? 0xffffffffu : 0u;
+                for (uint32_t k = 0; k < count; k++) {
+                    const uint32_t r = leaf_rows<PREC>(P, list ? list[k] : first + k, rc, cnt, err);
+                    m = isand ? (m & r) : (m | r);
+                    if (k + 1 < count && __all_sync(0xffffffffu, isand ? (m & rc.rowmask) == 0u
+                                                                       : (m & rc.rowmask) == rc.rowmask))
+                        break;
+                }
                 stk[sp++] = m;
                 break;
             }
@@ -1243,10 +1256,9 @@ template <int PREC>
 __device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, int len, P3 cpt, int axis, double lo,
                                      double hi, int iters, int hi_bit, Counts& cnt, int* err) {
     F3 pf = to_f3(cpt);
-    auto contains = [&](P3 pt, double v) -> bool {
+    auto contains_f = [&](P3 pt, float vf) -> bool {
         if (len == FOLD_FALSE) return false;
         if (len == FOLD_TRUE) return true;
-        const float vf = (float)v;
         if (axis == 0) pf.x = vf;
         else if (axis == 1) pf.y = vf;
         else pf.z = vf;
@@ -1255,18 +1267,35 @@ __device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, in
     double fp = lo, tp = hi;
     P3 t = cpt;
     set_comp(t, axis, tp);
-    if (!(hi_bit >= 0 ? hi_bit == 1 : contains(t, tp))) {
+    if (!(hi_bit >= 0 ? hi_bit == 1 : contains_f(t, (float)tp))) {
         fp = hi;
         tp = lo;
     }
     P3 arr = cpt;
+    unsigned long long fb = (unsigned long long)__double_as_longlong(fp);
+    unsigned long long tb = (unsigned long long)__double_as_longlong(tp);
+    // Same sign and binade (almost every edge): midpoints and their float
+    // roundings in integer arithmetic (mc_internal.h), no float64 operation.
+    const bool ibits = bisect_bits_ok(fb, tb);
+    auto midpoint = [&](unsigned long long a, unsigned long long b, float* vf) -> unsigned long long {
+        if (ibits) {
+            const unsigned long long m = mid_bits(a, b);
+            *vf = __uint_as_float(float_bits_of(m));
+            return m;
+        }
+        // x / 2 and x * 0.5 round the same real
+        const double mid = D_MUL(D_ADD(__longlong_as_double((long long)a), __longlong_as_double((long long)b)), 0.5);
+        *vf = (float)mid;
+        return (unsigned long long)__double_as_longlong(mid);
+    };
+    float vf;
     for (int k = 0; k < iters; k++) {
-        const double mid = D_MUL(D_ADD(fp, tp), 0.5);  // x / 2 and x * 0.5 round the same real
-        set_comp(arr, axis, mid);
-        if (contains(arr, mid)) tp = mid;
-        else fp = mid;
+        const unsigned long long mb = midpoint(fb, tb, &vf);
+        set_comp(arr, axis, __longlong_as_double((long long)mb));
+        if (contains_f(arr, vf)) tb = mb;
+        else fb = mb;
     }
-    set_comp(arr, axis, D_MUL(D_ADD(fp, tp), 0.5));
+    set_comp(arr, axis, __longlong_as_double((long long)midpoint(fb, tb, &vf)));
     return arr;
 }
 
@@ -1404,6 +1433,23 @@ __device__ __forceinline__ int find_slot(const long long* off, int n, long long 
     return lo;
 }
 
+// Jobs of a block's contiguous index range [first, last]: two searches by
+// one thread; every thread then searches only that (usually single) job.
+__device__ __forceinline__ void block_jobs(const long long* off, int n, long long first, long long last, int* j0,
+                                           int* j1) {
+    __shared__ int s_j[2];
+    if (threadIdx.x == 0) {
+        s_j[0] = find_slot(off, n, first);
+        s_j[1] = find_slot(off, n, last);
+    }
+    __syncthreads();
+    *j0 = s_j[0];
+    *j1 = s_j[1];
+}
+__device__ __forceinline__ int job_in(const long long* off, int j0, int j1, long long x) {
+    return j0 == j1 ? j0 : j0 + find_slot(off + j0, j1 - j0 + 1, x);
+}
+
 struct BatchArgs {
     const JobD* jobs;
     int njobs;
@@ -1445,11 +1491,13 @@ __global__ void __launch_bounds__(256, 3) k_classify_batch(BatchArgs b) {
 
 __global__ void __launch_bounds__(256) k_count_batch(BatchArgs b, uint32_t* packed, uint32_t* blocksum) {
     const long long base = (long long)blockIdx.x * kChunksPerBlock;
+    int j0, j1;
+    block_jobs(b.chunk_offs, b.njobs, base, min(b.nchunks, base + kChunksPerBlock) - 1, &j0, &j1);
     uint32_t nv = 0, nt = 0;
     for (int k = 0; k < kChunksPerBlock / 256; k++) {
         const long long i = base + k * 256 + threadIdx.x;
         if (i >= b.nchunks) break;
-        const int j = find_slot(b.chunk_offs, b.njobs, i);
+        const int j = job_in(b.chunk_offs, j0, j1, i);
         const JobD& J = b.jobs[j];
         uint32_t a = 0, c = 0;
         packed[i] = count_chunk(J.g, J.ca.bits, i - b.chunk_offs[j], a, c);
@@ -1476,9 +1524,11 @@ __global__ void k_job_bases(BatchArgs b, const uint32_t* prefv, const uint32_t* 
 
 __global__ void __launch_bounds__(256) k_emit_batch(BatchArgs b, const uint32_t* packed, const uint32_t* prefv,
                                                      const uint32_t* preft, unsigned long long* keys, int32_t* tris) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long first = (long long)blockIdx.x * blockDim.x, i = first + threadIdx.x;
+    int j0, j1;
+    block_jobs(b.chunk_offs, b.njobs, first, min(b.nchunks, first + blockDim.x) - 1, &j0, &j1);
     if (i >= b.nchunks) return;
-    const int j = find_slot(b.chunk_offs, b.njobs, i);
+    const int j = job_in(b.chunk_offs, j0, j1, i);
     const JobD& J = b.jobs[j];
     const long long c0 = b.chunk_offs[j];
     EmitArgs ea{J.ca.bits, packed + c0, prefv + c0, preft + c0, keys, tris, J.nchunks};
@@ -1501,10 +1551,17 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
     int prev_job = -1;
     const uint32_t* prog = nullptr;
     int len = 0;
+    int cj = 0;  // this lane's job and its vertex range (vertices only grow along the run)
+    long long cj_lo = 0, cj_hi = -1;
     for (long long bt = b_begin; bt < b_end; bt++) {
         const long long v = bt * 32 + lane;
         const bool live = v < nverts;
-        const int j = live ? find_slot((const long long*)b.vbase, b.njobs, v) : -1;
+        if (live && !(v >= cj_lo && v < cj_hi)) {
+            cj = find_slot((const long long*)b.vbase, b.njobs, v);
+            cj_lo = (long long)b.vbase[cj];
+            cj_hi = (long long)b.vbase[cj + 1];
+        }
+        const int j = live ? cj : -1;
         const int j0 = __shfl_sync(0xffffffffu, j, 0);
         const bool uniform = __all_sync(0xffffffffu, !live || j == j0);
         const JobD* Jp = live ? &b.jobs[j] : &b.jobs[j0];

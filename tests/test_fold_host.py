@@ -18,3 +18,14 @@ def test_fold_matches_full_program(tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad 0" in r.stdout
+
+
+def test_bisection_bit_arithmetic(tmp_path):
+    """mid_bits / float_bits_of (integer midpoint and float rounding used by
+    the search) equal IEEE (f + t) * 0.5 and (float)x on 5.5M cases."""
+    exe = tmp_path / "bits_check"
+    subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-o", str(exe),
+                    os.path.join(ROOT, "tests", "csrc", "bits_check.cpp")], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert " bad 0" in r.stdout
