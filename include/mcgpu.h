@@ -137,7 +137,10 @@ typedef struct mc_opts {
     int32_t cull;       /* 1: per-tile bounding-box culling of leaves (default); 0: off */
     int32_t tile_y;     /* corner-tile height in y (0: tuned default) */
     int32_t tile_z;     /* corner-tile depth in z (0: tuned default) */
-    int32_t reserved[4];
+    int32_t interior;   /* 1: also record each vertex's interior point (MarchingCubesInterior,
+                           model3d/mc.go:55-60) for mc_result_interior_copy; mc_search_device
+                           and mc_search only (ignored by the batch and allocation-free calls) */
+    int32_t reserved[3];
 } mc_opts;
 
 typedef struct mc_stats {
@@ -218,6 +221,18 @@ mc_status mc_result_device(const mc_ctx* ctx, const double** vertices,
                            const int32_t** triangles);
 /* Copy the last result into caller-provided host arrays (V*3, T*3). */
 mc_status mc_result_copy(mc_ctx* ctx, double* vertices, int32_t* triangles);
+/* Interior points of the last mc_search_device run with opts->interior set:
+ * V*3 float64, point i being the last inside point of vertex i's bisection
+ * (the CoordMap of MarchingCubesInterior, model3d/mc.go:55-60, :191-198,
+ * :252-255, keyed by vertex index).  MC_ERR_ARG if it was not requested. */
+mc_status mc_result_interior_copy(mc_ctx* ctx, double* interior);
+/* Mesh.Transform (model3d/mesh.go:643-645) of the last result's vertices, on
+ * the device: every vertex becomes JoinedTransform(steps).Apply(vertex), or
+ * its Inverse().Apply with inverse != 0 (transform.go:213-219; each step's
+ * Inverse as in transform.go).  steps are n_steps MC_XF_* records.  With
+ * TransformSolid of the same steps this is MarchingCubesConj
+ * (model3d/mc.go:66-71). */
+mc_status mc_result_transform(mc_ctx* ctx, const mc_node* steps, size_t n_steps, int32_t inverse);
 
 /* Solid.Contains on the GPU for n points (n x 3 float64) -> out[i] in {0,1}.
  * Same device predicates and precision modes as mc_search. */

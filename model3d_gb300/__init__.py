@@ -13,8 +13,8 @@ from .solids import (Capsule, CacheSolidBounds, ColliderSolid, Cylinder, ForceSo
                      NewRect, NotLowerable, Rect, RotateSolid, Rotation, Scale, ScaleSolid,
                      Solid, Sphere, Subtract, SubtractedSolid, Torus, TransformSolid, Translate,
                      TranslateSolid, VecScale, VecScaleSolid, serialize)
-from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesSearch,
-                 MarchingCubesSearchBatch, MCError,
+from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesConj,
+                 MarchingCubesInterior, MarchingCubesSearch, MarchingCubesSearchBatch, MCError,
                  Mesh, autotune, canonical, case_table, default_context, measure_peaks,
                  spacer_axis)
 

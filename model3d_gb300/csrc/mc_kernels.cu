@@ -133,10 +133,10 @@ __device__ __forceinline__ bool in_box(const XBoxD& b, P3 p) {
            p.z <= b.hi[2];
 }
 
-// Apply the inverse steps of a TRANSFORM node (transform.go:44-133).
-__device__ P3 apply_inverse(const ProgView& P, const XBoxD& b, P3 p) {
-    for (int s = 0; s < b.n_steps; s++) {
-        const XStepD& st = P.xstep[b.first_step + s];
+// Transform.Apply of a list of step records in order (transform.go:44-133).
+__device__ P3 apply_steps(const XStepD* steps, int n, P3 p) {
+    for (int s = 0; s < n; s++) {
+        const XStepD& st = steps[s];
         const double* v = st.v;
         switch (st.kind) {
             case MC_XF_TRANSLATE: p = P3{D_ADD(p.x, v[0]), D_ADD(p.y, v[1]), D_ADD(p.z, v[2])}; break;
@@ -149,6 +149,11 @@ __device__ P3 apply_inverse(const ProgView& P, const XBoxD& b, P3 p) {
         }
     }
     return p;
+}
+
+// The inverse steps of a TRANSFORM node.
+__device__ __forceinline__ P3 apply_inverse(const ProgView& P, const XBoxD& b, P3 p) {
+    return apply_steps(P.xstep + b.first_step, b.n_steps, p);
 }
 
 // Float64 predicate of one leaf at one point (reference operation order).
@@ -1122,6 +1127,7 @@ struct SearchArgs {
     int cull;
     int* err;
     unsigned long long* stats;
+    double* interior;  // V x 3 interior points, or null
 };
 
 __device__ __forceinline__ float warp_minf(float v) {
@@ -1219,7 +1225,7 @@ __device__ __forceinline__ int lookup_edge(const GridView& g, const P3& c, doubl
 
 // Vertex setup: edge key -> midpoint (corners[a].Mid(corners[b]),
 // mc.go:401-407) and, when iters != 0, LookupEdgePoint.  Returns the status.
-__device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* bits, unsigned long long key, int iters,
+__device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* bits, unsigned long long key, bool lookup,
                                             double inv_dl, P3* cpt, int* axis, double* lo, double* hi, int* hi_bit) {
     const int ax = (int)(key >> 60);
     const int z = (int)((key >> 40) & 0xfffff), y = (int)((key >> 20) & 0xfffff), x = (int)(key & 0xfffff);
@@ -1237,7 +1243,7 @@ __device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* b
     *cpt = P3{mid(c0.x, c1.x, ax != 0), mid(c0.y, c1.y, ax != 1), mid(c0.z, c1.z, ax != 2)};
     *axis = 0;
     *hi_bit = -1;
-    if (iters == 0) return 0;
+    if (!lookup) return 0;
     long long idx = -1;
     const int st = lookup_edge(g, *cpt, inv_dl, axis, lo, hi, &idx);
     // The first Contains of the bisection is at `hi`; when LookupEdgePoint
@@ -1254,7 +1260,7 @@ __device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* b
 // coordinate moves, so the float point is updated in place.
 template <int PREC>
 __device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, int len, P3 cpt, int axis, double lo,
-                                     double hi, int iters, int hi_bit, Counts& cnt, int* err) {
+                                     double hi, int iters, int hi_bit, Counts& cnt, int* err, double* true_point) {
     F3 pf = to_f3(cpt);
     auto contains_f = [&](P3 pt, float vf) -> bool {
         if (len == FOLD_FALSE) return false;
@@ -1296,6 +1302,7 @@ __device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, in
         else fb = mb;
     }
     set_comp(arr, axis, __longlong_as_double((long long)midpoint(fb, tb, &vf)));
+    *true_point = __longlong_as_double((long long)tb);
     return arr;
 }
 
@@ -1374,20 +1381,41 @@ __global__ void __launch_bounds__(128, 4) k_search(GridView g, ProgView P, Searc
         double lo = 0, hi = 0;
         P3 cpt{0, 0, 0};
         int hi_bit = -1;
-        int status = live ? vertex_setup(g, a.bits, a.keys[v], a.iters, a.inv_dl, &cpt, &axis, &lo, &hi, &hi_bit) : 0;
+        const bool lookup = a.iters != 0 || a.interior != nullptr;  // mc.go:182-185
+        int status = live ? vertex_setup(g, a.bits, a.keys[v], lookup, a.inv_dl, &cpt, &axis, &lo, &hi, &hi_bit) : 0;
         if (status == 1) atomicOr(&a.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&a.err[ER_EDGE_INDEX], 1);
-        const bool work = live && a.iters != 0 && status == 0;
+        const bool work = live && lookup && status == 0;
         if (a.cull && __any_sync(0xffffffffu, work)) search_cull(P, work, cpt, axis, lo, hi, q, cur, prev, have_prev, prog, len);
         if (live && status == 0) {
-            const P3 out = work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, a.iters, hi_bit, cnt, a.err) : cpt;
+            double tpt = 0;
+            const P3 out = work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, a.iters, hi_bit, cnt, a.err, &tpt) : cpt;
             a.verts[3 * v] = out.x;
             a.verts[3 * v + 1] = out.y;
             a.verts[3 * v + 2] = out.z;
+            if (a.interior) {
+                P3 in = out;
+                set_comp(in, axis, tpt);
+                a.interior[3 * v] = in.x;
+                a.interior[3 * v + 1] = in.y;
+                a.interior[3 * v + 2] = in.z;
+            }
         }
         __syncwarp();
     }
     flush_counts(cnt, a.stats);
+}
+
+// ------------------------------------------------------------ k_apply_steps
+
+// Mesh.Transform (model3d/mesh.go:643-645) of the vertex array.
+__global__ void k_apply_steps(double* verts, long long n, const XStepD* steps, int nsteps) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        P3 p = apply_steps(steps, nsteps, P3{verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]});
+        verts[3 * i] = p.x;
+        verts[3 * i + 1] = p.y;
+        verts[3 * i + 2] = p.z;
+    }
 }
 
 // ------------------------------------------------------------ k_contains
@@ -1570,10 +1598,12 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
         P3 cpt{0, 0, 0};
         int hi_bit = -1;
         const int status =
-            live ? vertex_setup(Jp->g, Jp->ca.bits, keys[v], Jp->iters, Jp->inv_dl, &cpt, &axis, &lo, &hi, &hi_bit) : 0;
+            live ? vertex_setup(Jp->g, Jp->ca.bits, keys[v], Jp->iters != 0, Jp->inv_dl, &cpt, &axis, &lo, &hi, &hi_bit)
+                 : 0;
         if (status == 1) atomicOr(&Jp->ca.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&Jp->ca.err[ER_EDGE_INDEX], 1);
         const bool work = live && Jp->iters != 0 && status == 0;
+        double tpt = 0;
         if (uniform) {
             const ProgView& P = b.jobs[j0].P;
             if (j0 != prev_job) {
@@ -1588,7 +1618,7 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
                 search_cull(P, work, cpt, axis, lo, hi, q, cur, cur + nw, have_prev, prog, len);
             if (live && status == 0) {
                 const P3 out =
-                    work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, Jp->iters, hi_bit, cnt, Jp->ca.err) : cpt;
+                    work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, Jp->iters, hi_bit, cnt, Jp->ca.err, &tpt) : cpt;
                 verts[3 * v] = out.x;
                 verts[3 * v + 1] = out.y;
                 verts[3 * v + 2] = out.z;
@@ -1598,7 +1628,7 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
             prev_job = -1;
             if (live && status == 0) {
                 const P3 out = work ? bisect<PREC>(Jp->P, Jp->P.ops, Jp->P.n_ops, cpt, axis, lo, hi, Jp->iters, hi_bit,
-                                                   cnt, Jp->ca.err)
+                                                   cnt, Jp->ca.err, &tpt)
                                     : cpt;
                 verts[3 * v] = out.x;
                 verts[3 * v + 1] = out.y;
@@ -1736,6 +1766,8 @@ struct mc_ctx {
     std::string err;
     DevBuf xs, ys, zs, xf, yf, zf, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
     DevBuf pts, pout;
+    DevBuf inner, xsteps;  // interior points of the last search; steps of mc_result_transform
+    bool has_interior = false;
     unsigned long long* h_pin = nullptr;  // pinned: totals[2], stats[ST_N], errs (as ints) ...
     // Device buffers of destroyed solids, reused by the next mc_solid_create
     // (stream order makes reuse safe without a synchronisation).  Solids may
@@ -1782,6 +1814,7 @@ mc_opts default_opts(const mc_opts* o) {
         r.cull = o->cull;
         r.tile_y = o->tile_y;
         r.tile_z = o->tile_z;
+        r.interior = o->interior;
     }
     return r;
 }
@@ -1860,7 +1893,7 @@ void mc_destroy(mc_ctx* ctx) {
     ctx->plan.reset();
     for (DevBuf* b : {&ctx->xs, &ctx->ys, &ctx->zs, &ctx->xf, &ctx->yf, &ctx->zf, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
                       &ctx->prefv, &ctx->preft, &ctx->keys, &ctx->verts, &ctx->tris, &ctx->stats, &ctx->errs,
-                      &ctx->totals, &ctx->pts, &ctx->pout})
+                      &ctx->totals, &ctx->pts, &ctx->pout, &ctx->inner, &ctx->xsteps})
         b->release();
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -2012,6 +2045,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
                         mc_stats* stats) {
     if (!ctx || !solid || iters < 0) return fail(ctx, MC_ERR_ARG, "bad argument");
     ctx->last_V = ctx->last_T = 0;
+    ctx->has_interior = false;
     mc_opts opts = default_opts(opts_in);
     const HostProgram& H = solid->host;
     if (!bounds_valid(H.root_min, H.root_max)) return fail(ctx, MC_ERR_INVALID_BOUNDS, "invalid bounds");
@@ -2149,6 +2183,10 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
         sa.cull = opts.cull;
         sa.err = ctx->errs.as<int>();
         sa.stats = ctx->stats.as<unsigned long long>();
+        if (opts.interior) {
+            CK(ctx->inner.ensure(V * 24));
+            sa.interior = ctx->inner.as<double>();
+        }
         size_t smem_s = search_smem(P);
         auto ks = opts.precision == MC_PREC_FP64 ? k_search<MC_PREC_FP64> : k_search<MC_PREC_FP32_FILTERED>;
         if (smem_s > 48 * 1024)
@@ -2201,6 +2239,7 @@ mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int
     mc_status s = search_launch(ctx, solid, delta, iters, opts, &st);
     if (s == MC_OK) s = search_finish(ctx, &st);
     if (s != MC_OK) return s;
+    ctx->has_interior = opts && opts->interior;
     if (n_vertices) *n_vertices = st.vertices;
     if (n_triangles) *n_triangles = st.triangles;
     if (stats_out) *stats_out = st;
@@ -2266,6 +2305,37 @@ mc_status mc_result_copy(mc_ctx* ctx, double* vertices, int32_t* triangles) {
     return MC_OK;
 }
 
+mc_status mc_result_interior_copy(mc_ctx* ctx, double* interior) {
+    if (!ctx || !interior) return MC_ERR_ARG;
+    if (!ctx->has_interior) return fail(ctx, MC_ERR_ARG, "the last search did not record interior points");
+    CK(cudaSetDevice(ctx->device));
+    if (!ctx->last_V) return MC_OK;
+    prefault(interior, (size_t)ctx->last_V * 24);
+    CK(cudaMemcpyAsync(interior, ctx->inner.p, (size_t)ctx->last_V * 24, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MC_OK;
+}
+
+mc_status mc_result_transform(mc_ctx* ctx, const mc_node* steps, size_t n_steps, int32_t inverse) {
+    if (!ctx || (n_steps && !steps)) return MC_ERR_ARG;
+    std::vector<XStepD> xs;
+    try {
+        xs = transform_steps(steps, n_steps, inverse != 0);
+    } catch (const LowerError& e) {
+        return fail(ctx, e.status, e.what());
+    }
+    if (xs.empty() || !ctx->last_V) return MC_OK;
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->xsteps.ensure(xs.size() * sizeof(XStepD)));
+    CK(cudaMemcpyAsync(ctx->xsteps.p, xs.data(), xs.size() * sizeof(XStepD), cudaMemcpyHostToDevice, ctx->stream));
+    const long long V = ctx->last_V;
+    k_apply_steps<<<(int)std::min<long long>((V + 255) / 256, (long long)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
+        ctx->verts.as<double>(), V, ctx->xsteps.as<XStepD>(), (int)xs.size());
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MC_OK;
+}
+
 mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters, const mc_opts* opts,
                     mc_mesh* out) {
     if (!out) return fail(ctx, MC_ERR_ARG, "null output");
@@ -2297,6 +2367,7 @@ mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t it
     out->n_vertices = V;
     out->n_triangles = T;
     out->stats.d2h_bytes += V * 24 + T * 12;
+    ctx->has_interior = opts && opts->interior;
     return MC_OK;
 }
 

@@ -720,29 +720,12 @@ struct Lowerer {
                     xb.lo[i] = nd.min[i];
                     xb.hi[i] = nd.max[i];
                 }
-                std::vector<XStepD> fwd;
-                for (int i = 0; i < nd.n_steps; i++) {
-                    if (pos >= n) fail("truncated transform steps");
-                    const mc_node& st = nodes[pos++];
-                    XStepD s{};
-                    s.kind = st.kind;
-                    switch (st.kind) {
-                        case MC_XF_TRANSLATE:  // Inverse: Offset.Scale(-1), transform.go:52-54
-                            for (int k = 0; k < 3; k++) s.v[k] = st.p[k] * -1;
-                            break;
-                        case MC_XF_SCALE: s.v[0] = 1 / st.p[0]; break;  // transform.go:83-85
-                        case MC_XF_VECSCALE:                            // Recip, transform.go:114-116
-                            for (int k = 0; k < 3; k++) s.v[k] = 1 / st.p[k];
-                            break;
-                        case MC_XF_MATRIX: inverse3(st.p, s.v); break;  // transform.go:153-155
-                        default: fail("bad transform step");
-                    }
-                    fwd.push_back(s);
-                }
-                // JoinedTransform.Inverse applies the inverses in reverse order (transform.go:213-219).
+                if (pos + (size_t)std::max(nd.n_steps, 0) > n) fail("truncated transform steps");
+                const std::vector<XStepD> inv = transform_steps(nodes + pos, std::max(nd.n_steps, 0), true);
+                pos += std::max(nd.n_steps, 0);
                 xb.first_step = (int)P->xstep.size();
-                xb.n_steps = (int)fwd.size();
-                for (int i = (int)fwd.size() - 1; i >= 0; i--) P->xstep.push_back(fwd[i]);
+                xb.n_steps = (int)inv.size();
+                P->xstep.insert(P->xstep.end(), inv.begin(), inv.end());
                 int id = (int)P->xbox.size();
                 P->xbox.push_back(xb);
                 P->has_transform = true;
@@ -845,6 +828,34 @@ const Base kBase[23] = {
     {0xff, 0, {}},
 };
 }  // namespace
+
+std::vector<XStepD> transform_steps(const mc_node* steps, size_t n, bool inverse) {
+    std::vector<XStepD> out;
+    for (size_t i = 0; i < n; i++) {
+        const mc_node& st = steps[i];
+        XStepD s{};
+        s.kind = st.kind;
+        switch (st.kind) {
+            case MC_XF_TRANSLATE:  // Inverse: Offset.Scale(-1), transform.go:52-54
+                for (int k = 0; k < 3; k++) s.v[k] = inverse ? st.p[k] * -1 : st.p[k];
+                break;
+            case MC_XF_SCALE: s.v[0] = inverse ? 1 / st.p[0] : st.p[0]; break;  // transform.go:83-85
+            case MC_XF_VECSCALE:                                              // Recip, transform.go:114-116
+                for (int k = 0; k < 3; k++) s.v[k] = inverse ? 1 / st.p[k] : st.p[k];
+                break;
+            case MC_XF_MATRIX:  // transform.go:153-155
+                if (inverse) inverse3(st.p, s.v);
+                else
+                    for (int k = 0; k < 9; k++) s.v[k] = st.p[k];
+                break;
+            default: throw LowerError(MC_ERR_BAD_PROGRAM, "bad transform step");
+        }
+        out.push_back(s);
+    }
+    // JoinedTransform.Inverse applies the inverses in reverse order (transform.go:213-219).
+    if (inverse) std::reverse(out.begin(), out.end());
+    return out;
+}
 
 int build_case_table(uint8_t counts[256], uint8_t tris[256][5][6]) {
     // The 24 rotations (allMcRotations, mc.go:312-353): closure of the

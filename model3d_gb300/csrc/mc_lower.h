@@ -46,6 +46,10 @@ struct HostProgram {
 void lower_scene(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets, size_t n_sets,
                  HostProgram* out);
 
+// Apply records of JoinedTransform(steps) (MC_XF_* records), or of its
+// Inverse() when inverse is set; throws LowerError on a bad step kind.
+std::vector<XStepD> transform_steps(const mc_node* steps, size_t n, bool inverse);
+
 // newSquareSpacer for one axis; MC_OK or MC_ERR_GRID.
 int spacer_axis(double lo, double hi, double delta, std::vector<double>* out, int64_t limit);
 

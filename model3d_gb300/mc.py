@@ -200,6 +200,52 @@ def MarchingCubesSearch(solid, delta: float, iters: int, *, precision: str = "fp
     return Mesh(verts, tris, m.stats.as_dict())
 
 
+def MarchingCubesInterior(solid, delta: float, iters: int, *, precision: str = "fp32",
+                          cull: bool = True, ctx: Optional[Context] = None):
+    """model3d.MarchingCubesInterior (model3d/mc.go:55-60) on the GPU: the
+    mesh and, for each vertex i, a point known to be inside the solid (the
+    last inside point of its bisection) as row i of a (V, 3) array -- the
+    reference's CoordMap keyed by vertex."""
+    ctx = ctx or (solid.ctx if isinstance(solid, DeviceSolid) else default_context())
+    ds = _as_device_solid(solid, ctx)
+    o = _opts(precision, cull)
+    o.interior = 1
+    V, T = ctypes.c_int64(), ctypes.c_int64()
+    st = N.MCStats()
+    L = N.lib()
+    _check(L.mc_search_device(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
+                              ctypes.byref(V), ctypes.byref(T), ctypes.byref(st)), ctx.ptr)
+    verts = np.empty((V.value, 3))
+    tris = np.empty((T.value, 3), dtype=np.int32)
+    inner = np.empty((V.value, 3))
+    _check(L.mc_result_copy(ctx.ptr, verts.ctypes.data, tris.ctypes.data), ctx.ptr)
+    _check(L.mc_result_interior_copy(ctx.ptr, inner.ctypes.data), ctx.ptr)
+    return Mesh(verts, tris, st.as_dict()), inner
+
+
+def MarchingCubesConj(solid, delta: float, iters: int, *xforms, precision: str = "fp32",
+                      cull: bool = True, ctx: Optional[Context] = None) -> Mesh:
+    """model3d.MarchingCubesConj (model3d/mc.go:66-71) on the GPU: the search
+    on TransformSolid(JoinedTransform(xforms), solid), then the inverse
+    transform applied to the mesh vertices on the device (Mesh.Transform)."""
+    from .solids import JoinedTransform, TransformSolid, transform_records
+    joined = JoinedTransform(list(xforms))
+    ctx = ctx or default_context()
+    ds = DeviceSolid(TransformSolid(joined, solid), ctx)
+    o = _opts(precision, cull)
+    V, T = ctypes.c_int64(), ctypes.c_int64()
+    st = N.MCStats()
+    L = N.lib()
+    _check(L.mc_search_device(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
+                              ctypes.byref(V), ctypes.byref(T), ctypes.byref(st)), ctx.ptr)
+    steps = transform_records(joined)
+    _check(L.mc_result_transform(ctx.ptr, steps.ctypes.data, len(steps), 1), ctx.ptr)
+    verts = np.empty((V.value, 3))
+    tris = np.empty((T.value, 3), dtype=np.int32)
+    _check(L.mc_result_copy(ctx.ptr, verts.ctypes.data, tris.ctypes.data), ctx.ptr)
+    return Mesh(verts, tris, st.as_dict())
+
+
 def MarchingCubesSearchBatch(jobs, *, precision: str = "fp32", cull: bool = True,
                              ctx: Optional[Context] = None, tile_y: int = 0, tile_z: int = 0):
     """Many MarchingCubesSearch calls in one batched launch (mc_search_batch).

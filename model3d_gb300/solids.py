@@ -475,6 +475,17 @@ def GroupBounders(objs: List[Solid]) -> List[Solid]:
 
 # ------------------------------------------------------------ serialisation
 
+def transform_records(t: Transform) -> np.ndarray:
+    """The MC_XF_* records (mc_node array) of a transform's steps in
+    JoinedTransform order."""
+    steps = t._steps()
+    out = np.zeros(len(steps), dtype=NODE_DTYPE)
+    for i, (kind, p) in enumerate(steps):
+        out[i]["kind"] = kind
+        out[i]["p"][:len(p)] = p
+    return out
+
+
 def serialize(solid: Solid):
     """Prefix-order mc_node records and the triangle sets they refer to.
 

@@ -988,7 +988,8 @@ struct KeyEq {
 extern "C" {
 
 typedef struct oracle_mesh {
-    double* tris;  // n_triangles x 9, in generation order
+    double* tris;      // n_triangles x 9, in generation order
+    double* interior;  // n_triangles x 9 when requested: each corner's interior point (mc.go:191-198)
     int64_t n_triangles;
     int64_t n_vertices;  // unique vertices (exact-coordinate dedup, model3d/mesh.go:822-849)
     int64_t nx, ny, nz;
@@ -1000,10 +1001,46 @@ typedef struct oracle_mesh {
 } oracle_mesh;
 
 void oracle_mesh_free(oracle_mesh* m) {
-    if (m && m->tris) {
-        std::free(m->tris);
-        m->tris = nullptr;
+    if (!m) return;
+    std::free(m->tris);
+    std::free(m->interior);
+    m->tris = nullptr;
+    m->interior = nullptr;
+}
+
+// Transform.Apply of JoinedTransform(steps) -- or of its Inverse()
+// (transform.go:213-219: inverses in reverse order) -- at every point,
+// in place (the mapping of Mesh.Transform, mesh.go:615-645).
+int oracle_apply_transform(const mc_node* steps, size_t n, int inverse, double* pts, int64_t n_pts) {
+    std::vector<XStep> xs;
+    for (size_t i = 0; i < n; i++) {
+        const mc_node& st = steps[i];
+        XStep x;
+        x.kind = st.kind;
+        if (st.kind == MC_XF_TRANSLATE || st.kind == MC_XF_VECSCALE) {
+            x.v = xyz(st.p[0], st.p[1], st.p[2]);
+        } else if (st.kind == MC_XF_SCALE) {
+            x.s = st.p[0];
+        } else if (st.kind == MC_XF_MATRIX) {
+            for (int k = 0; k < 9; k++) x.m.m[k] = st.p[k];
+        } else {
+            return MC_ERR_BAD_PROGRAM;
+        }
+        xs.push_back(x);
     }
+    if (inverse) {
+        std::vector<XStep> inv;
+        for (int i = (int)xs.size() - 1; i >= 0; i--) inv.push_back(xs[i].inverse());
+        xs.swap(inv);
+    }
+    for (int64_t i = 0; i < n_pts; i++) {
+        V3 c = xyz(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+        for (auto& x : xs) c = x.apply(c);
+        pts[3 * i] = c.x;
+        pts[3 * i + 1] = c.y;
+        pts[3 * i + 2] = c.z;
+    }
+    return MC_OK;
 }
 
 int oracle_case_table(uint8_t counts[256], uint8_t tris[256][5][6], int* conflicts, int* covered) {
@@ -1072,7 +1109,7 @@ int oracle_contains(const mc_node* nodes, size_t n, const mc_tri_set* sets, size
 // bounded sample of a large grid; the default covers the whole grid exactly
 // as the reference does.
 int oracle_mc_search(const mc_node* nodes, size_t n, const mc_tri_set* sets, size_t n_sets,
-                     double delta, int iters, int threads, int64_t z_begin, int64_t z_end,
+                     double delta, int iters, int threads, int64_t z_begin, int64_t z_end, int want_interior,
                      oracle_mesh* out) {
     std::memset(out, 0, sizeof(*out));
     Scene sc;
@@ -1197,13 +1234,15 @@ int oracle_mc_search(const mc_node* nodes, size_t n, const mc_tri_set* sets, siz
     }
     out->n_vertices = verts.size();
 
-    // mcSearch (mc.go:182-221).
-    if (iters != 0) {
+    // mcSearch (mc.go:182-221); MarchingCubesInterior runs it for iters == 0 too.
+    std::vector<V3> inner;
+    if (iters != 0 || want_interior) {
         V3 origin = xyz(Xs[0], Ys[0], Zs[0]);
         if (NX < 2 && !verts.empty()) return MC_ERR_EDGE_INDEX;  // Xs[1] out of range
         double dl = NX >= 2 ? Xs[1] - Xs[0] : 0;
         const std::vector<double>* vals[3] = {&Xs, &Ys, &Zs};
         std::vector<V3> outv(verts.size());
+        if (want_interior) inner.resize(verts.size());
         std::atomic<int> err2{0};
         int64_t chunk = 1024;
         parallel_for(((int64_t)verts.size() + chunk - 1) / chunk, threads, [&](int64_t c, int) {
@@ -1246,6 +1285,11 @@ int oracle_mc_search(const mc_node* nodes, size_t n, const mc_tri_set* sets, siz
                 }
                 set(arr, axis, (falseP + trueP) / 2);
                 outv[i] = arr;
+                if (want_interior) {  // mc.go:252-255
+                    V3 ip = arr;
+                    set(ip, axis, trueP);
+                    inner[i] = ip;
+                }
             }
             calls += 0;
             flush();
@@ -1266,6 +1310,15 @@ int oracle_mc_search(const mc_node* nodes, size_t n, const mc_tri_set* sets, siz
     out->n_triangles = T;
     out->tris = (double*)std::malloc(std::max<size_t>(1, soup.size()) * sizeof(double));
     if (!soup.empty()) std::memcpy(out->tris, soup.data(), soup.size() * sizeof(double));
+    if (want_interior) {
+        out->interior = (double*)std::malloc(std::max<size_t>(1, soup.size()) * sizeof(double));
+        for (int64_t i = 0; i < T * 3; i++) {
+            const V3 p = inner[tri_v[i]];
+            out->interior[3 * i] = p.x;
+            out->interior[3 * i + 1] = p.y;
+            out->interior[3 * i + 2] = p.z;
+        }
+    }
     out->contains_calls = calls;
     out->leaf_evals = leaf;
     out->bvh_nodes = ndc;

@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 class OracleMesh(ctypes.Structure):
     _fields_ = [
         ("tris", ctypes.POINTER(ctypes.c_double)),
+        ("interior", ctypes.POINTER(ctypes.c_double)),
         ("n_triangles", ctypes.c_int64),
         ("n_vertices", ctypes.c_int64),
         ("nx", ctypes.c_int64),
@@ -56,7 +57,9 @@ def lib():
         L.oracle_mc_search.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                        ctypes.c_size_t, ctypes.c_double, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
-                                       ctypes.POINTER(OracleMesh)]
+                                       ctypes.c_int, ctypes.POINTER(OracleMesh)]
+        L.oracle_apply_transform.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                             ctypes.c_void_p, ctypes.c_int64]
         L.oracle_mesh_free.argtypes = [ctypes.POINTER(OracleMesh)]
         L.oracle_contains.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                       ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int64,
@@ -92,14 +95,16 @@ class OracleError(RuntimeError):
         self.status = status
 
 
-def mc_search(nodes, sets, delta, iters, threads=None, z_range=(0, -1)):
-    """Returns dict(tris=(T,9) float64 soup in generation order, stats...)."""
+def mc_search(nodes, sets, delta, iters, threads=None, z_range=(0, -1), interior=False):
+    """Returns dict(tris=(T,9) float64 soup in generation order, stats...);
+    with interior=True also interior=(T,9): each corner's interior point
+    (MarchingCubesInterior, model3d/mc.go:55-60)."""
     nodes, arr, keep = _scene(nodes, sets)
     out = OracleMesh()
     threads = threads or os.cpu_count() or 1
     st = lib().oracle_mc_search(nodes.ctypes.data, len(nodes), ctypes.addressof(arr), len(sets),
                                 float(delta), int(iters), int(threads), int(z_range[0]),
-                                int(z_range[1]), ctypes.byref(out))
+                                int(z_range[1]), int(bool(interior)), ctypes.byref(out))
     if st != 0:
         msg = out.error.decode()
         lib().oracle_mesh_free(ctypes.byref(out))
@@ -109,8 +114,22 @@ def mc_search(nodes, sets, delta, iters, threads=None, z_range=(0, -1)):
     res = dict(tris=tris, n_vertices=out.n_vertices, nx=out.nx, ny=out.ny, nz=out.nz,
                contains_calls=out.contains_calls, leaf_evals=out.leaf_evals,
                bvh_nodes=out.bvh_nodes, bvh_tris=out.bvh_tris)
+    if interior:
+        res["interior"] = np.ctypeslib.as_array(out.interior, shape=(max(T, 1) * 9,))[:T * 9].reshape(T, 9).copy()
     lib().oracle_mesh_free(ctypes.byref(out))
     return res
+
+
+def apply_transform(steps, pts, inverse=False):
+    """JoinedTransform(steps).Apply -- or its Inverse().Apply -- at each
+    point (transform.go); steps are mc_node records of MC_XF_* kinds."""
+    steps = np.ascontiguousarray(steps)
+    out = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3).copy()
+    st = lib().oracle_apply_transform(steps.ctypes.data, len(steps), int(bool(inverse)),
+                                      out.ctypes.data, len(out))
+    if st != 0:
+        raise OracleError(st, "bad transform step")
+    return out
 
 
 def contains(nodes, sets, pts, threads=None):

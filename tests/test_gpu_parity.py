@@ -298,3 +298,43 @@ def test_collider_grazing_rays(oracle, prec):
     bad = np.nonzero(got != ref)[0]
     assert len(bad) == 0, f"{len(bad)} of {len(pts)} differ, first {pts[bad[:3]]}"
     _check(oracle, s, 0.05, 8, modes=[(prec, True)])
+
+
+@pytest.mark.parametrize("iters", [0, 3, 8])
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_marching_cubes_interior(oracle, iters, prec):
+    """MarchingCubesInterior (mc.go:55-60): same mesh as the oracle and, per
+    vertex, the oracle's interior point, bit for bit; every interior point is
+    inside the solid."""
+    from model3d_gb300 import MarchingCubesInterior
+    solids = [Sphere(XYZ(0.1, 0.0, -0.1), 0.8), csg_tree(2, 12, 4),
+              TransformSolid(Rotation(XYZ(0.3, 1, 0.2), 0.5), Cylinder(XYZ(0, 0, -0.4), XYZ(0.1, 0, 0.5), 0.3))]
+    for s in solids:
+        nodes, sets = serialize(s)
+        ref = oracle.mc_search(nodes, sets, 0.04, iters, interior=True)
+        mesh, inner = MarchingCubesInterior(s, 0.04, iters, precision=prec)
+        _same(mesh, ref)
+        want = {}
+        for c, ip in zip(ref["tris"].reshape(-1, 3).view(np.uint64), ref["interior"].reshape(-1, 3)):
+            want[c.tobytes()] = ip
+        got_v = mesh.vertices.view(np.uint64)
+        for i in range(len(mesh.vertices)):
+            assert np.array_equal(want[got_v[i].tobytes()].view(np.uint64), inner[i].view(np.uint64))
+        assert Contains(s, inner, precision="fp64").all()
+
+
+def test_marching_cubes_conj(oracle):
+    """MarchingCubesConj (mc.go:66-71): search in the transformed space, then
+    the inverse transform on the device; equals the oracle's mesh mapped by
+    JoinedTransform(xforms).Inverse()."""
+    from model3d_gb300 import JoinedTransform, MarchingCubesConj
+    from model3d_gb300.solids import transform_records
+    base = SubtractedSolid(Capsule(XYZ(-0.4, 0.1, 0), XYZ(0.5, -0.2, 0.3), 0.35), Sphere(XYZ(0.2, 0.1, 0.2), 0.3))
+    for xforms in ([Scale(1.3), Rotation(XYZ(0.2, 1, 0.3), 0.4), Translate(XYZ(0.1, -0.2, 0.05))],
+                   [VecScale(XYZ(1.5, 0.8, 1.1))], [Translate(XYZ(0.25, 0, -0.5))]):
+        joined = JoinedTransform(xforms)
+        for prec in ("fp64", "fp32"):
+            mesh = MarchingCubesConj(base, 0.03, 8, *xforms, precision=prec)
+            ref = oracle.mc_search(*serialize(TransformSolid(joined, base)), 0.03, 8)
+            back = oracle.apply_transform(transform_records(joined), ref["tris"].reshape(-1, 3), inverse=True)
+            _same(mesh, {"tris": back.reshape(-1, 9)})
