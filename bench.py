@@ -43,7 +43,7 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms."""
 
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -58,7 +58,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -232,13 +232,8 @@ def run_ours(args):
     sts64 = timed(N.MC_PREC_FP64, args.steps)
 
     ms = [s["ms_total"] for s in sts]
-    ms_step = float(np.mean(ms))
-    if ws > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
     corners = sts[0]["corners"]
-    value = ws * corners / (ms_step / 1000.0)
+    ms_step, value = replica_rate(float(np.mean(ms)), corners, ws, "cuda")
     ms64 = float(np.mean([s["ms_total"] for s in sts64]))
     value64 = ws * corners / (ms64 / 1000.0)
 
@@ -262,7 +257,7 @@ def run_ours(args):
     peaks, kind = measured_peaks()
     roof = roofline(dom, phases[dom], sts[0], peaks, kind)
 
-    others = {} if args.no_extra else other_configs(ctx, torch, flush, value)
+    others = {} if args.no_extra else other_configs(ctx, torch, flush, value, args.collider_batch)
     pk = measure_peaks(ctx)
 
     if rank == 0:
@@ -310,6 +305,18 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def replica_rate(ms_step, corners, ws, device):
+    """Whole-job rate of ws independent replicas: every rank processed
+    `corners` per step; the step time is the slowest rank's (all_reduce MAX
+    over the process group, any backend).  Returns (ms_step, corners/s)."""
+    if ws > 1:
+        import torch
+        t = torch.tensor([ms_step], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    return ms_step, ws * corners / (ms_step / 1000.0)
+
+
 def _device_rate(L, N, ctx, ds, delta, iters, prec, flush, torch, reps=3):
     import ctypes
     o = N.MCOpts()
@@ -330,7 +337,7 @@ def _device_rate(L, N, ctx, ds, delta, iters, prec, flush, torch, reps=3):
     return best
 
 
-def other_configs(ctx, torch, flush, single_rate):
+def other_configs(ctx, torch, flush, single_rate, count=16):
     """The other benchmark configurations, device time (CUDA events, best of 3
     after a warm-up): unit sphere (delta 0.01), the 1,048,820-triangle
     displaced icosphere collider on a ~256^3 grid, and 512 CSG solids in one
@@ -375,9 +382,15 @@ def other_configs(ctx, torch, flush, single_rate):
             m = MarchingCubesSearchBatch(jobs, precision=prec, ctx=ctx)
             ms.append(m[0].stats["ms_total"])
         res[prec] = (min(ms[1:]), sum(x.stats["corners"] for x in m), sum(x.NumTriangles() for x in m))
-    seq = 0.0
+    seq, big = 0.0, None
     for ds_, dd, it in jobs:
-        seq += _device_rate(L, N, ctx, ds_, dd, it, N.MC_PREC_FP32_FILTERED, flush, torch, reps=0)["ms_total"]
+        r = _device_rate(L, N, ctx, ds_, dd, it, N.MC_PREC_FP32_FILTERED, flush, torch, reps=0)
+        seq += r["ms_total"]
+        if big is None or r["corners"] > big[1]["corners"]:
+            big = ((ds_, dd, it), r)
+    (bds, bd, bit), _ = big
+    br = _device_rate(L, N, ctx, bds, bd, bit, N.MC_PREC_FP32_FILTERED, flush, torch, reps=3)
+    big_rate = br["corners"] / (br["ms_total"] / 1e3)
     corners = res["fp32"][1]
     out["batch_512_csg"] = {
         "jobs": len(jobs), "corners": corners, "triangles": res["fp32"][2],
@@ -387,13 +400,76 @@ def other_configs(ctx, torch, flush, single_rate):
         "ms_fp32_graph_replay": res["fp32"][0], "ms_fp64_graph_replay": res["fp64"][0],
         "sequential_single_calls_ms": seq,
         "batched_over_sequential": seq / res["fp32"][0],
-        "fraction_of_single_large_solid_rate": (corners / (res["fp32"][0] / 1e3)) / single_rate}
+        "fraction_of_single_large_solid_rate": (corners / (res["fp32"][0] / 1e3)) / single_rate,
+        "largest_job_alone": {"corners": br["corners"], "triangles": br["triangles"],
+                              "fp32_corners_per_s": big_rate},
+        "fraction_of_largest_job_alone_rate": (corners / (res["fp32"][0] / 1e3)) / big_rate}
+    out.update(collider_batch_line(ctx, count))
     return out
+
+
+def collider_batch_line(ctx, count):
+    """Displaced-icosphere colliders (triangles log-uniform in [20k, 2M], grid
+    sides log-uniform in [128, 512]) meshed in one batched launch, FP32-filtered
+    (graph replay) and FP64, with the two precisions' meshes compared."""
+    from model3d_gb300 import (DeviceSolid, MarchingCubesSearchBatch, MeshToCollider,
+                               NewColliderSolid)
+    from model3d_gb300.workloads import collider_batch
+    if count <= 0:
+        return {}
+    t0 = time.perf_counter()
+    meshes = collider_batch(77, count=count)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    jobs = []
+    for tris, _, side in meshes:
+        s = NewColliderSolid(MeshToCollider(tris))
+        mn, mx = s.Min(), s.Max()
+        ext = max(mx.X - mn.X, mx.Y - mn.Y, mx.Z - mn.Z)
+        jobs.append((DeviceSolid(s, ctx), ext / (side - 3), 8))
+    lower_s = time.perf_counter() - t0
+    ms = {}
+    outs = {}
+    for prec, reps in (("fp32", 3), ("fp64", 1)):
+        times = []
+        for _ in range(reps):
+            m = MarchingCubesSearchBatch(jobs, precision=prec, ctx=ctx)
+            bad = [x for x in m if not hasattr(x, "stats")]
+            if bad:
+                raise RuntimeError(f"collider batch job failed: {bad[0]}")
+            times.append(m[0].stats["ms_total"])
+        ms[prec] = min(times[1:]) if len(times) > 1 else times[0]
+        outs[prec] = m
+    same = all(np.array_equal(a.vertices.view(np.uint64), b.vertices.view(np.uint64)) and
+               np.array_equal(a.triangles, b.triangles) for a, b in zip(outs["fp32"], outs["fp64"]))
+    corners = sum(x.stats["corners"] for x in outs["fp32"])
+    st0 = outs["fp32"][0].stats  # counters of a batched launch are batch totals
+    tests = st0["bvh_tris"] + st0["bvh_nodes"]
+    esc = st0["escalations"]
+    name = f"batch_{count}_colliders" + ("" if count == 64 else "_of_the_64_mesh_configuration")
+    return {name: {
+        "jobs": count, "triangles_in": int(sum(len(t) for t, _, _ in meshes)),
+        "corners": corners, "triangles_out": sum(x.NumTriangles() for x in outs["fp32"]),
+        "fp32_corners_per_s": corners / (ms["fp32"] / 1e3),
+        "fp64_corners_per_s": corners / (ms["fp64"] / 1e3),
+        "ms_fp32_graph_replay": ms["fp32"], "ms_fp64": ms["fp64"],
+        "bit_identical_fp32_fp64": bool(same),
+        "escalation_rate": esc / max(1, tests),
+        "host_generate_s": gen_s, "host_lower_s": lower_s}}
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# each kernel on this workload, from an ncu capture of the full-size grid.
+# Below the algorithmic bytes where a kernel reads what the previous one
+# left in the 129 MB L2 (keys, corner bits) or its writes stay in L2.
+NCU_TRAFFIC = {"k_classify": 14679808, "k_count": 29755648, "k_emit": 67178240, "k_search": 39695360}
 
 
 def roofline(kernel, ms, st, peaks, kind):
     """Algorithmic bytes of one launch of the dominant kernel over its CUDA-
-    event time, against the measured HBM copy bandwidth."""
+    event time, against the measured HBM copy bandwidth.  The kernels are
+    bound by issue latency of the predicate interpreter (ALU), not by HBM,
+    so the fraction is small by construction."""
     nx, ny, nz = st["nx"], st["ny"], st["nz"]
     W = (nx + 31) // 32 + 1
     bits = nz * ny * W * 4
@@ -409,19 +485,22 @@ def roofline(kernel, ms, st, peaks, kind):
         alg = V * 8 + V * 24                        # keys read, vertices written
     achieved = alg / (ms / 1000.0) / 1e9
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    return {"kernel": kernel.replace("ms_", "k_"), "bound": "hbm", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+    name = kernel.replace("ms_", "k_")
+    return {"kernel": name, "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": NCU_TRAFFIC.get(name),
             "algorithmic_bytes": int(alg), "ms": ms, "peak_kind": kind}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
+    ap.add_argument("--collider-batch", type=int, default=16,
+                    help="meshes in the batched-collider line (64 = the full configuration)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -2794,8 +2794,11 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         m.stats.corners = (int64_t)J.g.nx * J.g.ny * J.g.nz;
         m.stats.vertices = nv;
         m.stats.triangles = nt;
+        // Counters and time are totals over the whole batched launch.
         m.stats.leaf_evals = (int64_t)hstats[ST_LEAF];
         m.stats.escalations = (int64_t)hstats[ST_ESC];
+        m.stats.bvh_nodes = (int64_t)hstats[ST_NODES];
+        m.stats.bvh_tris = (int64_t)hstats[ST_TRIS];
         m.stats.tiles_const = (int64_t)hstats[ST_TILES_CONST];
         m.stats.ms_total = ms_total;
         m.stats.d2h_bytes = nv * 24 + nt * 12;

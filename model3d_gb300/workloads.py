@@ -95,6 +95,23 @@ def csg_batch(seed: int, count: int = 512, grid_lo: int = 32, grid_hi: int = 384
     return out
 
 
+def collider_batch(seed: int, count: int = 64, tri_lo: int = 20000, tri_hi: int = 2000000,
+                   grid_lo: int = 128, grid_hi: int = 512) -> List[Tuple[np.ndarray, int, int]]:
+    """(triangles, seed, grid side) of displaced icospheres: triangle counts
+    log-uniform in [tri_lo, tri_hi] (an icosphere has 20 n^2 triangles, so n is
+    rounded), each meshed at a grid whose longest side is log-uniform in
+    [grid_lo, grid_hi] corners; delta = extent / (side - 3)."""
+    rng = SplitMix64(seed)
+    out = []
+    for i in range(count):
+        t = rng.log_uniform(tri_lo, tri_hi)
+        n = max(1, int(round(math.sqrt(t / 20))))
+        mesh_seed = int(rng.next_u64() % (1 << 31))
+        side = int(round(rng.log_uniform(grid_lo, grid_hi)))
+        out.append((displaced_icosphere(n, mesh_seed), mesh_seed, side))
+    return out
+
+
 def icosphere_triangles(n: int) -> np.ndarray:
     """(20 n^2, 9) triangles of an icosahedron with faces split n x n, on the
     unit sphere, counter-clockwise seen from outside."""
