@@ -1803,6 +1803,20 @@ mc_status fail(mc_ctx* ctx, mc_status s, const std::string& m) {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+constexpr int kTileY = 8, kTileZ = 4;  // default corner-tile rows (32 x 8 x 4 corners per warp tile)
+
+// Classification tile shape: the caller's, else one row per tile for solids
+// with colliders (a collider row costs a ray query per corner, so the grid
+// needs many small work items to fill the GPU), else the context's tuned or
+// the default shape.
+void pick_tiles(const mc_opts* user, const HostProgram& H, int tuned_ty, int tuned_tz, int* ty, int* tz) {
+    const int uy = user ? user->tile_y : 0, uz = user ? user->tile_z : 0;
+    const bool fixed = uy > 0 || uz > 0;
+    const bool small = !fixed && H.has_collider;
+    *ty = uy > 0 ? uy : (small ? 1 : (tuned_ty > 0 ? tuned_ty : kTileY));
+    *tz = uz > 0 ? uz : (small ? 1 : (tuned_tz > 0 ? tuned_tz : kTileZ));
+}
+
 mc_opts default_opts(const mc_opts* o) {
     mc_opts r{};
     r.precision = MC_PREC_FP32_FILTERED;
@@ -1819,7 +1833,6 @@ mc_opts default_opts(const mc_opts* o) {
     return r;
 }
 
-constexpr int kTileY = 8, kTileZ = 4;  // default corner-tile rows (32 x 8 x 4 corners per warp tile)
 
 size_t search_smem(const ProgView& P) {
     const size_t nw = ((size_t)P.n_leaves + 31) / 32;
@@ -2111,8 +2124,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     ca.xf = ctx->xf.as<float>();
     ca.yf = ctx->yf.as<float>();
     ca.zf = ctx->zf.as<float>();
-    ca.ty = opts.tile_y > 0 ? opts.tile_y : (ctx->tuned_ty > 0 ? ctx->tuned_ty : kTileY);
-    ca.tz = opts.tile_z > 0 ? opts.tile_z : (ctx->tuned_tz > 0 ? ctx->tuned_tz : kTileZ);
+    pick_tiles(opts_in, H, ctx->tuned_ty, ctx->tuned_tz, &ca.ty, &ca.tz);
     ca.ntx = (nx + 31) / 32;
     ca.nty = (ny + ca.ty - 1) / ca.ty;
     ca.ntz = (nz + ca.tz - 1) / ca.tz;
@@ -2442,7 +2454,8 @@ mc_status mc_autotune(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t 
                       mc_opts* best, double* best_ms) {
     if (!ctx || !solid) return fail(ctx, MC_ERR_ARG, "bad argument");
     // Corner-tile shapes (rows = ty * tz <= 32 keeps the row-vectorised path).
-    static const int cand[][2] = {{2, 4}, {4, 2}, {4, 4}, {8, 2}, {2, 8}, {8, 4}, {4, 8}, {16, 2}, {2, 16}};
+    static const int cand[][2] = {{1, 1}, {2, 1}, {1, 2}, {2, 2}, {2, 4}, {4, 2}, {4, 4},
+                                  {8, 2}, {2, 8}, {8, 4}, {4, 8}, {16, 2}, {2, 16}};
     mc_opts o = default_opts(opts_in);
     double best_t = 1e30;
     int bty = kTileY, btz = kTileZ;
@@ -2542,8 +2555,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             J.P = jobs[i].solid->view;
             J.ca.prec = pl->prec;
             J.ca.cull = opts.cull;
-            J.ca.ty = opts.tile_y > 0 ? opts.tile_y : (ctx->tuned_ty > 0 ? ctx->tuned_ty : kTileY);
-            J.ca.tz = opts.tile_z > 0 ? opts.tile_z : (ctx->tuned_tz > 0 ? ctx->tuned_tz : kTileZ);
+            pick_tiles(opts_in, jobs[i].solid->host, ctx->tuned_ty, ctx->tuned_tz, &J.ca.ty, &J.ca.tz);
             J.ca.ntx = (nx + 31) / 32;
             J.ca.nty = (ny + J.ca.ty - 1) / J.ca.ty;
             J.ca.ntz = (nz + J.ca.tz - 1) / J.ca.tz;
