@@ -233,6 +233,15 @@ mc_status mc_result_interior_copy(mc_ctx* ctx, double* interior);
  * TransformSolid of the same steps this is MarchingCubesConj
  * (model3d/mc.go:66-71). */
 mc_status mc_result_transform(mc_ctx* ctx, const mc_node* steps, size_t n_steps, int32_t inverse);
+/* EncodeSTL (model3d/export.go:20-66, fileformats/stl.go:27-58) of the last
+ * result, encoded on the device: an 80-byte zero header, the triangle count
+ * (uint32 LE), then per triangle the float32 casts of Triangle.Normal()
+ * (primitives.go:27-33, float64 in the reference's operation order) and of
+ * its three vertices, and two zero bytes -- 84 + 50 T bytes.  Triangles are
+ * in this library's order (the reference writes them in its map order).
+ * With out == NULL only *n_bytes is set; MC_ERR_ARG if cap is too small or
+ * T does not fit in uint32. */
+mc_status mc_result_stl(mc_ctx* ctx, uint8_t* out, size_t cap, size_t* n_bytes);
 
 /* Solid.Contains on the GPU for n points (n x 3 float64) -> out[i] in {0,1}.
  * Same device predicates and precision modes as mc_search. */

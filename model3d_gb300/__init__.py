@@ -14,7 +14,8 @@ from .solids import (Capsule, CacheSolidBounds, ColliderSolid, Cylinder, ForceSo
                      Solid, Sphere, Subtract, SubtractedSolid, Torus, TransformSolid, Translate,
                      TranslateSolid, VecScale, VecScaleSolid, serialize)
 from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesConj,
-                 MarchingCubesInterior, MarchingCubesSearch, MarchingCubesSearchBatch, MCError,
+                 MarchingCubesInterior, MarchingCubesSearch, MarchingCubesSearchBatch,
+                 MarchingCubesSearchSTL, MCError,
                  Mesh, autotune, canonical, case_table, default_context, measure_peaks,
                  spacer_axis)
 

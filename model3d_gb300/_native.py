@@ -35,7 +35,7 @@ EXPORTS = [
     "mc_solid_destroy", "mc_solid_bounds", "mc_spacer_axis", "mc_search", "mc_mesh_free",
     "mc_search_device", "mc_result_device", "mc_result_copy", "mc_contains", "mc_search_batch",
     "mc_case_table", "mc_version", "mc_search_noalloc", "mc_autotune",
-    "mc_measure_peaks", "mc_result_interior_copy", "mc_result_transform",
+    "mc_measure_peaks", "mc_result_interior_copy", "mc_result_transform", "mc_result_stl",
 ]
 
 
@@ -114,6 +114,7 @@ def lib():
         L.mc_result_copy.argtypes = [vp, vp, vp]
         L.mc_result_interior_copy.argtypes = [vp, vp]
         L.mc_result_transform.argtypes = [vp, vp, ctypes.c_size_t, i32]
+        L.mc_result_stl.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         L.mc_contains.argtypes = [vp, vp, vp, i64, ctypes.POINTER(MCOpts), vp]
         L.mc_search_batch.argtypes = [vp, ctypes.POINTER(MCJob), ctypes.c_size_t,
                                       ctypes.POINTER(MCOpts), ctypes.POINTER(MCMesh), vp]

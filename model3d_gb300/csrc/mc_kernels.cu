@@ -1418,6 +1418,44 @@ __global__ void k_apply_steps(double* verts, long long n, const XStepD* steps, i
     }
 }
 
+// ------------------------------------------------------------ k_encode_stl
+
+// One 50-byte STL record per triangle (fileformats/stl.go:41-58): the
+// float32 normal (Triangle.Normal = crossProduct().Normalize(), i.e.
+// c.Scale(1 / c.Norm()), primitives.go:27-33, coords.go:201-203, :379-381)
+// and vertices, then two zero bytes.  Records are 2-byte aligned.
+__global__ void k_encode_stl(const double* verts, const int32_t* tris, long long n, uint8_t* out) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        P3 v[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const long long i = tris[3 * t + k];
+            v[k] = P3{verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]};
+        }
+        const double ax = D_SUB(v[1].x, v[0].x), ay = D_SUB(v[1].y, v[0].y), az = D_SUB(v[1].z, v[0].z);
+        const double bx = D_SUB(v[2].x, v[0].x), by = D_SUB(v[2].y, v[0].y), bz = D_SUB(v[2].z, v[0].z);
+        const double cx = D_SUB(D_MUL(ay, bz), D_MUL(az, by));
+        const double cy = D_SUB(D_MUL(az, bx), D_MUL(ax, bz));
+        const double cz = D_SUB(D_MUL(ax, by), D_MUL(ay, bx));
+        const double inv = D_DIV(1.0, D_SQRT(D_ADD(D_ADD(D_MUL(cx, cx), D_MUL(cy, cy)), D_MUL(cz, cz))));
+        float rec[12] = {(float)D_MUL(cx, inv), (float)D_MUL(cy, inv), (float)D_MUL(cz, inv)};
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            rec[3 + 3 * k] = (float)v[k].x;
+            rec[4 + 3 * k] = (float)v[k].y;
+            rec[5 + 3 * k] = (float)v[k].z;
+        }
+        uint16_t* o = (uint16_t*)(out + 84 + 50 * t);
+#pragma unroll
+        for (int k = 0; k < 12; k++) {
+            const uint32_t b = __float_as_uint(rec[k]);
+            o[2 * k] = (uint16_t)(b & 0xffffu);
+            o[2 * k + 1] = (uint16_t)(b >> 16);
+        }
+        o[24] = 0;
+    }
+}
+
 // ------------------------------------------------------------ k_contains
 
 template <int PREC>
@@ -1766,7 +1804,7 @@ struct mc_ctx {
     std::string err;
     DevBuf xs, ys, zs, xf, yf, zf, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
     DevBuf pts, pout;
-    DevBuf inner, xsteps;  // interior points of the last search; steps of mc_result_transform
+    DevBuf inner, xsteps, stl;  // interior points of the last search; steps of mc_result_transform; STL bytes
     bool has_interior = false;
     unsigned long long* h_pin = nullptr;  // pinned: totals[2], stats[ST_N], errs (as ints) ...
     // Device buffers of destroyed solids, reused by the next mc_solid_create
@@ -1906,7 +1944,7 @@ void mc_destroy(mc_ctx* ctx) {
     ctx->plan.reset();
     for (DevBuf* b : {&ctx->xs, &ctx->ys, &ctx->zs, &ctx->xf, &ctx->yf, &ctx->zf, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
                       &ctx->prefv, &ctx->preft, &ctx->keys, &ctx->verts, &ctx->tris, &ctx->stats, &ctx->errs,
-                      &ctx->totals, &ctx->pts, &ctx->pout, &ctx->inner, &ctx->xsteps})
+                      &ctx->totals, &ctx->pts, &ctx->pout, &ctx->inner, &ctx->xsteps, &ctx->stl})
         b->release();
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -2344,6 +2382,32 @@ mc_status mc_result_transform(mc_ctx* ctx, const mc_node* steps, size_t n_steps,
     k_apply_steps<<<(int)std::min<long long>((V + 255) / 256, (long long)ctx->sm_count * 8), 256, 0, ctx->stream>>>(
         ctx->verts.as<double>(), V, ctx->xsteps.as<XStepD>(), (int)xs.size());
     CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MC_OK;
+}
+
+mc_status mc_result_stl(mc_ctx* ctx, uint8_t* out, size_t cap, size_t* n_bytes) {
+    if (!ctx || !n_bytes) return MC_ERR_ARG;
+    const long long T = ctx->last_T;
+    if (T > 0xffffffffLL) return fail(ctx, MC_ERR_ARG, "too many triangles for STL format");
+    const size_t bytes = 84 + 50 * (size_t)T;
+    *n_bytes = bytes;
+    if (!out) return MC_OK;
+    if (cap < bytes) return fail(ctx, MC_ERR_ARG, "STL buffer too small");
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->stl.ensure(bytes));
+    uint8_t* d = ctx->stl.as<uint8_t>();
+    uint8_t head[84] = {};
+    const uint32_t n32 = (uint32_t)T;
+    for (int k = 0; k < 4; k++) head[80 + k] = (uint8_t)(n32 >> (8 * k));  // little endian
+    CK(cudaMemcpyAsync(d, head, 84, cudaMemcpyHostToDevice, ctx->stream));
+    if (T > 0) {
+        k_encode_stl<<<(int)std::min<long long>((T + 255) / 256, (long long)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
+            ctx->verts.as<double>(), ctx->tris.as<int32_t>(), T, d);
+        CK(cudaGetLastError());
+    }
+    prefault(out, bytes);
+    CK(cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return MC_OK;
 }

@@ -246,6 +246,26 @@ def MarchingCubesConj(solid, delta: float, iters: int, *xforms, precision: str =
     return Mesh(verts, tris, st.as_dict())
 
 
+def MarchingCubesSearchSTL(solid, delta: float, iters: int, *, precision: str = "fp32",
+                           cull: bool = True, ctx: Optional[Context] = None) -> bytes:
+    """model3d.MarchingCubesSearch(...).EncodeSTL() (model3d/export.go:20-66)
+    with the binary STL encoded on the device: 84 + 50 T bytes (triangles in
+    this library's order)."""
+    ctx = ctx or (solid.ctx if isinstance(solid, DeviceSolid) else default_context())
+    ds = _as_device_solid(solid, ctx)
+    o = _opts(precision, cull)
+    V, T = ctypes.c_int64(), ctypes.c_int64()
+    st = N.MCStats()
+    L = N.lib()
+    _check(L.mc_search_device(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
+                              ctypes.byref(V), ctypes.byref(T), ctypes.byref(st)), ctx.ptr)
+    n = ctypes.c_size_t()
+    _check(L.mc_result_stl(ctx.ptr, None, 0, ctypes.byref(n)), ctx.ptr)
+    buf = np.empty(n.value, dtype=np.uint8)
+    _check(L.mc_result_stl(ctx.ptr, buf.ctypes.data, n.value, ctypes.byref(n)), ctx.ptr)
+    return buf.tobytes()
+
+
 def MarchingCubesSearchBatch(jobs, *, precision: str = "fp32", cull: bool = True,
                              ctx: Optional[Context] = None, tile_y: int = 0, tile_z: int = 0):
     """Many MarchingCubesSearch calls in one batched launch (mc_search_batch).

@@ -1008,6 +1008,29 @@ void oracle_mesh_free(oracle_mesh* m) {
     m->interior = nullptr;
 }
 
+// EncodeSTL (model3d/export.go:20-66, fileformats/stl.go:27-58) of a
+// triangle soup (T x 9 float64, in the given order): 80 zero bytes, uint32
+// LE count, then per triangle float32(Normal()), float32 vertices, 2 zero
+// bytes.  Normal = crossProduct().Normalize() (primitives.go:27-33).
+void oracle_encode_stl(const double* tris, int64_t T, uint8_t* out) {
+    std::memset(out, 0, 84);
+    const uint32_t n = (uint32_t)T;
+    std::memcpy(out + 80, &n, 4);
+    for (int64_t t = 0; t < T; t++) {
+        const double* p = tris + 9 * t;
+        V3 a = xyz(p[0], p[1], p[2]), b = xyz(p[3], p[4], p[5]), c = xyz(p[6], p[7], p[8]);
+        V3 e1 = sub(b, a), e2 = sub(c, a);
+        V3 cr = xyz(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
+        double norm = std::sqrt(cr.x * cr.x + cr.y * cr.y + cr.z * cr.z);
+        V3 nrm = scale(cr, 1 / norm);
+        float rec[12] = {(float)nrm.x, (float)nrm.y, (float)nrm.z};
+        for (int k = 0; k < 9; k++) rec[3 + k] = (float)p[k];
+        uint8_t* o = out + 84 + 50 * t;
+        std::memcpy(o, rec, 48);
+        o[48] = o[49] = 0;
+    }
+}
+
 // Transform.Apply of JoinedTransform(steps) -- or of its Inverse()
 // (transform.go:213-219: inverses in reverse order) -- at every point,
 // in place (the mapping of Mesh.Transform, mesh.go:615-645).

@@ -60,6 +60,7 @@ def lib():
                                        ctypes.c_int, ctypes.POINTER(OracleMesh)]
         L.oracle_apply_transform.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                              ctypes.c_void_p, ctypes.c_int64]
+        L.oracle_encode_stl.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
         L.oracle_mesh_free.argtypes = [ctypes.POINTER(OracleMesh)]
         L.oracle_contains.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                       ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int64,
@@ -118,6 +119,14 @@ def mc_search(nodes, sets, delta, iters, threads=None, z_range=(0, -1), interior
         res["interior"] = np.ctypeslib.as_array(out.interior, shape=(max(T, 1) * 9,))[:T * 9].reshape(T, 9).copy()
     lib().oracle_mesh_free(ctypes.byref(out))
     return res
+
+
+def encode_stl(tris):
+    """EncodeSTL (model3d/export.go) of a (T, 9) triangle soup, as bytes."""
+    t = np.ascontiguousarray(tris, dtype=np.float64).reshape(-1, 9)
+    out = np.zeros(84 + 50 * len(t), dtype=np.uint8)
+    lib().oracle_encode_stl(t.ctypes.data, len(t), out.ctypes.data)
+    return out.tobytes()
 
 
 def apply_transform(steps, pts, inverse=False):

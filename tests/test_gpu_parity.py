@@ -338,3 +338,19 @@ def test_marching_cubes_conj(oracle):
             ref = oracle.mc_search(*serialize(TransformSolid(joined, base)), 0.03, 8)
             back = oracle.apply_transform(transform_records(joined), ref["tris"].reshape(-1, 3), inverse=True)
             _same(mesh, {"tris": back.reshape(-1, 9)})
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_stl_encoding(oracle, prec):
+    """EncodeSTL on the device (mc_result_stl): header and the multiset of
+    50-byte records equal the oracle's encoding of the oracle's mesh."""
+    from model3d_gb300 import MarchingCubesSearchSTL
+    for s, d in ((csg_tree(4, 10, 3), 0.02), (NewColliderSolid(MeshToCollider(displaced_icosphere(6))), 0.05)):
+        nodes, sets = serialize(s)
+        ref = oracle.encode_stl(oracle.mc_search(nodes, sets, d, 8)["tris"])
+        got = MarchingCubesSearchSTL(s, d, 8, precision=prec)
+        assert len(got) == len(ref) and got[:84] == ref[:84]
+        def recs(b):
+            a = np.frombuffer(b[84:], dtype=np.uint8).reshape(-1, 50)
+            return a[np.lexsort(a.T[::-1])]
+        assert np.array_equal(recs(got), recs(ref))
