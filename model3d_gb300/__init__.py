@@ -13,7 +13,8 @@ from .solids import (Capsule, CacheSolidBounds, ColliderSolid, Cylinder, ForceSo
                      NewRect, NotLowerable, Rect, RotateSolid, Rotation, Scale, ScaleSolid,
                      Solid, Sphere, Subtract, SubtractedSolid, Torus, TransformSolid, Translate,
                      TranslateSolid, VecScale, VecScaleSolid, serialize)
-from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesConj,
+from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesC2F, MarchingCubesConj,
+                 MarchingCubesFilter, MarchingCubesSearchFilter,
                  MarchingCubesInterior, MarchingCubesSearch, MarchingCubesSearchBatch,
                  MarchingCubesSearchSTL, MCError,
                  Mesh, autotune, canonical, case_table, default_context, measure_peaks,

@@ -354,3 +354,28 @@ def test_stl_encoding(oracle, prec):
             a = np.frombuffer(b[84:], dtype=np.uint8).reshape(-1, 50)
             return a[np.lexsort(a.T[::-1])]
         assert np.array_equal(recs(got), recs(ref))
+
+
+def test_filter_and_c2f_match_reference_tests(oracle):
+    """The properties of mc_test.go:44-94: MarchingCubesFilter with a
+    collider's RectCollision equals MarchingCubes, MarchingCubesC2F equals
+    MarchingCubesSearch (sphere and two-box solids), here against the
+    oracle's MarchingCubes / MarchingCubesSearch."""
+    from model3d_gb300 import MarchingCubesC2F, MarchingCubesFilter, MarchingCubesSearchFilter
+    from model3d_gb300.workloads import icosphere_triangles
+    ico = icosphere_triangles(6).reshape(-1, 3, 3) + np.array([0.1, 0.3, -0.2])
+    col = NewColliderSolid(MeshToCollider(ico.reshape(-1, 9)))
+    boxes = np.concatenate([box_triangles((-1, -1, -1), (0, 0, 0)), box_triangles((0.1, 0, 0), (1, 1, 1))])
+    bcol = NewColliderSolid(MeshToCollider(boxes))
+    for s in (col, bcol):
+        ref = oracle.mc_search(*serialize(s), 0.1, 0)
+        _same(MarchingCubesFilter(s, lambda r: True, 0.1), ref)
+        ref8 = oracle.mc_search(*serialize(s), 0.1, 8)
+        _same(MarchingCubesSearchFilter(s, lambda r: True, 0.1, 8), ref8)
+    sph = Sphere(XYZ(0.1, 0.3, -0.2), 1.0)
+    _same(MarchingCubesC2F(sph, 0.1, 0.05, 0, 8), oracle.mc_search(*serialize(sph), 0.05, 8))
+    boxes2 = np.concatenate([box_triangles((-1, -1, -1), (0, 0, 0)), box_triangles((0.3, 0, 0), (1, 1, 1))])
+    b2 = NewColliderSolid(MeshToCollider(boxes2))
+    _same(MarchingCubesC2F(b2, 0.2, 0.1, 0, 8), oracle.mc_search(*serialize(b2), 0.1, 8))
+    with pytest.raises(MCError):
+        MarchingCubesC2F(sph, 0.05, 0.1, 0, 8)
