@@ -2310,6 +2310,49 @@ namespace {
 // first made resident by a few threads touching one byte per page (the
 // kernel's first-touch faults are the slow part); mc_search does that while
 // the emit and search kernels run.
+// Host arrays of returned meshes.  Large arrays come from a small
+// process-wide pool: a freed mesh's arrays are kept (resident, so the next
+// search copies into them without page faults and nothing is unmapped) and
+// handed to the next mesh that fits.  A 64-byte header holds the capacity.
+constexpr size_t kHostHead = 64;
+constexpr size_t kPoolMin = 1u << 20;  // smaller arrays go straight to malloc
+constexpr size_t kPoolKeep = 8;        // arrays kept at most
+std::mutex g_host_mu;
+std::vector<std::pair<size_t, void*>> g_host_pool;  // (capacity, base)
+
+void* host_alloc(size_t bytes) {
+    bytes = std::max<size_t>(bytes, 1);
+    if (bytes >= kPoolMin) {
+        std::lock_guard<std::mutex> lk(g_host_mu);
+        for (size_t k = 0; k < g_host_pool.size(); k++) {
+            const size_t cap = g_host_pool[k].first;
+            if (cap >= bytes && cap <= 2 * bytes) {
+                void* b = g_host_pool[k].second;
+                g_host_pool.erase(g_host_pool.begin() + k);
+                return (char*)b + kHostHead;
+            }
+        }
+    }
+    void* b = std::malloc(bytes + kHostHead);
+    if (!b) return nullptr;
+    *(size_t*)b = bytes;
+    return (char*)b + kHostHead;
+}
+
+void host_free(void* p) {
+    if (!p) return;
+    void* b = (char*)p - kHostHead;
+    const size_t cap = *(size_t*)b;
+    if (cap >= kPoolMin) {
+        std::lock_guard<std::mutex> lk(g_host_mu);
+        if (g_host_pool.size() < kPoolKeep) {
+            g_host_pool.emplace_back(cap, b);
+            return;
+        }
+    }
+    std::free(b);
+}
+
 void prefault(void* ptr, size_t bytes) {
     if (!ptr || !bytes) return;
     static const size_t page = std::max<long>(4096, sysconf(_SC_PAGESIZE));
@@ -2422,8 +2465,8 @@ mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t it
     const int64_t V = st.vertices, T = st.triangles;
     ctx->last_V = V;
     ctx->last_T = T;
-    out->vertices = (double*)std::malloc(std::max<int64_t>(V, 1) * 24);
-    out->triangles = (int32_t*)std::malloc(std::max<int64_t>(T, 1) * 12);
+    out->vertices = (double*)host_alloc((size_t)V * 24);
+    out->triangles = (int32_t*)host_alloc((size_t)T * 12);
     if (!out->vertices || !out->triangles) {
         cudaStreamSynchronize(ctx->stream);
         mc_mesh_free(out);
@@ -2449,8 +2492,8 @@ mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t it
 
 void mc_mesh_free(mc_mesh* m) {
     if (!m) return;
-    std::free(m->vertices);
-    std::free(m->triangles);
+    host_free(m->vertices);
+    host_free(m->triangles);
     m->vertices = nullptr;
     m->triangles = nullptr;
     m->n_vertices = m->n_triangles = 0;
@@ -2854,8 +2897,8 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         const long long v0 = (long long)hvb[d], nv = (long long)(hvb[d + 1] - hvb[d]);
         const long long t0 = (long long)htb[d], nt = (long long)(htb[d + 1] - htb[d]);
         mc_mesh& m = outs[i];
-        m.vertices = (double*)std::malloc(std::max<long long>(nv, 1) * 24);
-        m.triangles = (int32_t*)std::malloc(std::max<long long>(nt, 1) * 12);
+        m.vertices = (double*)host_alloc((size_t)nv * 24);
+        m.triangles = (int32_t*)host_alloc((size_t)nt * 12);
         if (!m.vertices || !m.triangles) {
             mc_mesh_free(&m);
             return fail(ctx, MC_ERR_OOM, "host allocation failed");
