@@ -1800,6 +1800,7 @@ struct mc_ctx {
     int tuned_ty = 0, tuned_tz = 0;  // set by mc_autotune; used when a call leaves the tile shape at 0
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // triangle read-back overlapping the search kernel
     cudaEvent_t ev[8] = {};
     std::string err;
     DevBuf xs, ys, zs, xf, yf, zf, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
@@ -1928,6 +1929,7 @@ mc_status mc_create(mc_ctx** out, int device) {
     c->device = device;
     CK(cudaSetDevice(device));
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     for (auto& e : c->ev) CK(cudaEventCreate(&e));
     CK(cudaMemcpyToSymbolAsync(c_table, &g_table_host, sizeof(CaseTable), 0, cudaMemcpyHostToDevice, c->stream));
     CK(cudaHostAlloc((void**)&c->h_pin, 64 * sizeof(unsigned long long), cudaHostAllocDefault));
@@ -1950,6 +1952,10 @@ void mc_destroy(mc_ctx* ctx) {
         if (e) cudaEventDestroy(e);
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     for (DevBuf& d : ctx->solid_pool) d.release();
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -2472,11 +2478,21 @@ mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t it
         mc_mesh_free(out);
         return fail(ctx, MC_ERR_OOM, "host allocation failed");
     }
-    // Emit and search run on the device meanwhile.
-    prefault(out->vertices, (size_t)V * 24);
+    // Emit and search run on the device meanwhile.  The triangles are final
+    // once emit ends (event ev[3]), so their read-back overlaps the search.
     prefault(out->triangles, (size_t)T * 12);
-    s = enqueue_mesh_copy(ctx, out->vertices, out->triangles);
+    s = MC_OK;
+    if (T) {
+        if (cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[3], 0) != cudaSuccess ||
+            cudaMemcpyAsync(out->triangles, ctx->tris.p, (size_t)T * 12, cudaMemcpyDeviceToHost, ctx->copy_stream) !=
+                cudaSuccess)
+            s = fail(ctx, MC_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    }
+    prefault(out->vertices, (size_t)V * 24);
+    if (s == MC_OK) s = enqueue_mesh_copy(ctx, out->vertices, nullptr);
     mc_status f = search_finish(ctx, &st);
+    if (cudaStreamSynchronize(ctx->copy_stream) != cudaSuccess && f == MC_OK)
+        f = fail(ctx, MC_ERR_CUDA, "triangle read-back failed");
     if (s == MC_OK) s = f;
     if (s != MC_OK) {
         mc_mesh_free(out);
