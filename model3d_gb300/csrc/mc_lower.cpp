@@ -328,12 +328,13 @@ void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, in
             bmax = std::max(bmax, b.bhi);
         }
     }
-    // Cell edge: half the median triangle extent (about six cells per
-    // triangle), at most 32000 cells per axis and 2^24 cells.
+    // Cell edge: a quarter of the median triangle extent (measured fastest
+    // of 0.25 / 0.35 / 0.5 / 0.7 on a 1M-triangle mesh: ~7 candidate tests
+    // per ray), at most 32000 cells per axis and 2^24 cells.
     double cs = 0;
     if (!sizes.empty()) {
         std::nth_element(sizes.begin(), sizes.begin() + sizes.size() / 2, sizes.end());
-        cs = 0.5 * sizes[sizes.size() / 2];
+        cs = 0.25 * sizes[sizes.size() / 2];
     }
     const double ea = amax - amin, eb = bmax - bmin;
     cs = std::max({cs, ea / 32000, eb / 32000, std::sqrt(ea * eb / (double)(1 << 24)), 1e-300});
