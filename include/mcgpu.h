@@ -17,7 +17,8 @@
  * Threading: one mc_ctx per host thread.  Each context owns a CUDA stream
  * and grow-only device buffers; every call is synchronous on return.  Destroy
  * a context's solids before the context (mc_solid_destroy may run on any
- * thread).
+ * thread); a solid that outlives its context is detached by mc_destroy and
+ * can still be destroyed, but not used.
  */
 #ifndef MCGPU_H
 #define MCGPU_H

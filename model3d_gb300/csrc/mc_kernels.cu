@@ -1813,6 +1813,7 @@ struct mc_ctx {
     // be destroyed from another thread than the context's, hence the lock.
     std::mutex pool_mu;
     std::vector<DevBuf> solid_pool;
+    std::vector<mc_solid*> solids;  // live solids; mc_destroy detaches them
     int64_t last_V = 0, last_T = 0;
     int sm_count = 152;
 };
@@ -1951,6 +1952,13 @@ void mc_destroy(mc_ctx* ctx) {
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
+    {
+        // Solids that outlive their context keep their buffers and free them
+        // on their own destroy.
+        std::lock_guard<std::mutex> lk(ctx->pool_mu);
+        for (mc_solid* s : ctx->solids) s->ctx = nullptr;
+        ctx->solids.clear();
+    }
     for (DevBuf& d : ctx->solid_pool) d.release();
     if (ctx->copy_stream) {
         cudaStreamSynchronize(ctx->copy_stream);
@@ -2049,15 +2057,21 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
     v.n_xbox = (int32_t)H.xbox.size();
     v.rows_ok = H.has_transform ? 0 : 1;
     v.fold_cap = H.fold_cap;
+    {
+        std::lock_guard<std::mutex> lk(ctx->pool_mu);
+        ctx->solids.push_back(s.get());
+    }
     *out = s.release();
     return MC_OK;
 }
 
 void mc_solid_destroy(mc_solid* s) {
     if (!s) return;
-    if (s->ctx && s->buf.p && s->buf.cap <= (64u << 20)) {
+    if (s->ctx) {
         std::lock_guard<std::mutex> lk(s->ctx->pool_mu);
-        if (s->ctx->solid_pool.size() < 16) {
+        auto& v = s->ctx->solids;
+        v.erase(std::remove(v.begin(), v.end(), s), v.end());
+        if (s->buf.p && s->buf.cap <= (64u << 20) && s->ctx->solid_pool.size() < 16) {
             s->ctx->solid_pool.push_back(s->buf);
             s->buf = DevBuf{};
         }
@@ -2066,6 +2080,8 @@ void mc_solid_destroy(mc_solid* s) {
         if (s->ctx) {
             cudaSetDevice(s->ctx->device);
             cudaStreamSynchronize(s->ctx->stream);
+        } else {
+            cudaDeviceSynchronize();
         }
         s->buf.release();
     }
@@ -2323,8 +2339,9 @@ namespace {
 constexpr size_t kHostHead = 64;
 constexpr size_t kPoolMin = 1u << 20;  // smaller arrays go straight to malloc
 constexpr size_t kPoolKeep = 8;        // arrays kept at most
-std::mutex g_host_mu;
-std::vector<std::pair<size_t, void*>> g_host_pool;  // (capacity, base)
+// Never destroyed: meshes may be freed while the process exits.
+std::mutex& g_host_mu = *new std::mutex;
+std::vector<std::pair<size_t, void*>>& g_host_pool = *new std::vector<std::pair<size_t, void*>>;  // (capacity, base)
 
 void* host_alloc(size_t bytes) {
     bytes = std::max<size_t>(bytes, 1);

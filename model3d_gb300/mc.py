@@ -12,6 +12,7 @@ per-triangle coordinates.
 from __future__ import annotations
 
 import ctypes
+import sys
 import threading
 from typing import Optional
 
@@ -57,6 +58,10 @@ class Context:
             self._p = ctypes.c_void_p()
 
     def __del__(self):
+        # At interpreter shutdown the finalisation order of contexts, solids
+        # and meshes is arbitrary; the process is ending, so release nothing.
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -113,6 +118,10 @@ class DeviceSolid:
             self._p = ctypes.c_void_p()
 
     def __del__(self):
+        # At interpreter shutdown the finalisation order of contexts, solids
+        # and meshes is arbitrary; the process is ending, so release nothing.
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -180,6 +189,8 @@ class _HostMesh:
                 view(m.triangles, m.n_triangles, ctypes.c_int32, np.int32))
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             N.lib().mc_mesh_free(ctypes.byref(self.m))
         except Exception:

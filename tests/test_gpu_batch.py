@@ -71,3 +71,15 @@ def test_autotune_keeps_results_and_peaks_are_positive():
     assert np.array_equal(m.triangles, ref.triangles)
     f32, f64, l2 = measure_peaks()
     assert f32 > 0 and f64 > 0 and l2 > 0
+
+
+def test_solid_outliving_its_context():
+    """mc_destroy detaches the context's solids; destroying them afterwards
+    frees their device buffers without touching the context."""
+    from model3d_gb300 import Context
+    ctx = Context(0)
+    ds = DeviceSolid(csg_tree(2, 4, 1), ctx)
+    m = MarchingCubesSearch(ds, 0.05, 8)
+    assert m.NumTriangles() > 0
+    ctx.close()
+    ds.close()
