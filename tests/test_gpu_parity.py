@@ -379,3 +379,27 @@ def test_filter_and_c2f_match_reference_tests(oracle):
     _same(MarchingCubesC2F(b2, 0.2, 0.1, 0, 8), oracle.mc_search(*serialize(b2), 0.1, 8))
     with pytest.raises(MCError):
         MarchingCubesC2F(sph, 0.05, 0.1, 0, 8)
+
+
+def test_grid_at_the_corner_limit():
+    """A grid just under the 2^31-corner limit meshes (FP32-filtered and FP64
+    identical; Euler characteristic 2 of a sphere); one just over it is
+    refused with MC_ERR_GRID, not truncated."""
+    s = Sphere(XYZ(0, 0, 0), 1.0)
+    a = MarchingCubesSearch(s, 2.0 / 1275, 2, precision="fp32")
+    assert 1.9e9 < a.stats["corners"] < 2 ** 31
+    b = MarchingCubesSearch(s, 2.0 / 1275, 2, precision="fp64")
+    assert np.array_equal(a.vertices.view(np.uint64), b.vertices.view(np.uint64))
+    assert np.array_equal(a.triangles, b.triangles)
+    V, T = len(a.vertices), len(a.triangles)
+    assert V - T // 2 == 2  # closed triangle mesh of genus 0: V - E + F = V - 3T/2 + T
+    with pytest.raises(MCError) as e:
+        MarchingCubesSearch(s, 2.0 / 1295, 2)
+    assert e.value.status == N.MC_ERR_GRID
+
+
+def test_long_thin_grid_near_the_key_limit(oracle):
+    """An x-extent of about 600k grid values (keys hold 20-bit indices) with a
+    solid thinner than one cell in y and z."""
+    s = Rect(XYZ(-1, 0, 0), XYZ(1, 1.5e-6, 1.5e-6))
+    _check(oracle, s, 2.0 / 600000, 8, modes=[("fp32", True), ("fp64", True)])
