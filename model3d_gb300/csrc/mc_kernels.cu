@@ -334,18 +334,23 @@ __device__ uint32_t sphere_rows32(const float* f, const double* d, const RowCtx&
     const float ez = 2.001f * U32 * (fabsf(rc.rzf) + fabsf(f[2]));
     const float dyz = __fmaf_rn(dy, dy, dz * dz);
     const float tyz = ey * (2.f * fabsf(dy) + ey) + ez * (2.f * fabsf(dz) + ez);
-    uint32_t m = 0;
+    // Decisions for all rows first (no branch in the loop, so rows overlap),
+    // then float64 for the undecided ones.
+    uint32_t in = 0, und = 0;
+#pragma unroll 4
     for (int r = 0; r < rc.nrows; r++) {
-        float S = dx2 + shf(dyz, r);
-        float E = 1.001f * (tx + shf(tyz, r) + 3.01f * U32 * S) + 1e-30f;
-        int v = decide_le(S, E, f[4], f[5]);
-        if (v == 2) {
-            cnt.esc++;
-            v = sphere_64_ni(d, row_point(rc, r));
-        }
-        m |= (uint32_t)v << r;
+        const float S = dx2 + shf(dyz, r);
+        const float E = 1.001f * (tx + shf(tyz, r) + 3.01f * U32 * S) + 1e-30f;
+        const bool yes = __fadd_ru(S, E) <= f[4], no = __fsub_rd(S, E) > f[5];
+        in |= (uint32_t)yes << r;
+        und |= (uint32_t)(!yes && !no) << r;
     }
-    return m;
+    for (uint32_t u = und; u; u &= u - 1) {
+        const int r = __ffs(u) - 1;
+        cnt.esc++;
+        if (sphere_64_ni(d, row_point(rc, r))) in |= 1u << r;
+    }
+    return in;
 }
 
 __device__ uint32_t cylinder_rows64(const double* c, const RowCtx& rc) {
@@ -376,37 +381,36 @@ __device__ uint32_t cylinder_rows32(const float* f, const double* d, const RowCt
     const float eqz = 2.001f * U32 * (fabsf(rc.rzf) + fabsf(f[2]));
     const float fyz = __fmaf_rn(qy, f[4], qz * f[5]);
     const float efyz = ay * (eqy + 4.03f * U32 * fabsf(qy)) + az * (eqz + 4.03f * U32 * fabsf(qz));
-    uint32_t m = 0;
+    uint32_t in = 0, und = 0;
+#pragma unroll 2
     for (int r = 0; r < rc.nrows; r++) {
         const float Qy = shf(qy, r), Qz = shf(qz, r), Ey = shf(eqy, r), Ez = shf(eqz, r);
         const float frac = __fmaf_rn(qx, f[3], shf(fyz, r));
         const float Ef = 1.001f * (efx + shf(efyz, r)) + 1e-30f;
         const float flo = __fsub_rd(frac, Ef), fhi = __fadd_ru(frac, Ef);
-        int v;
-        if (fhi < 0.f || flo > f[7]) {
-            v = 0;
-        } else if (!(flo >= 0.f && fhi <= f[6])) {
-            v = 2;
-        } else {
-            const float d1 = __fmaf_rn(f[3], frac, -qx);
-            const float d2 = __fmaf_rn(f[4], frac, -Qy);
-            const float d3 = __fmaf_rn(f[5], frac, -Qz);
-            const float S = __fmaf_rn(d1, d1, __fmaf_rn(d2, d2, d3 * d3));
-            const float g = 1.0001f * Ef + 1.0001f * U32 * (fabsf(frac) + Ef);
-            const float e1 = ax * g + eqx + 1.0001f * U32 * fabsf(d1);
-            const float e2 = ay * g + Ey + 1.0001f * U32 * fabsf(d2);
-            const float e3 = az * g + Ez + 1.0001f * U32 * fabsf(d3);
-            float E = e1 * (2.f * fabsf(d1) + e1) + e2 * (2.f * fabsf(d2) + e2) + e3 * (2.f * fabsf(d3) + e3);
-            E = 1.001f * (E + 3.02f * U32 * S) + 1e-30f;
-            v = decide_le(S, E, f[8], f[9]);
-        }
-        if (v == 2) {
-            cnt.esc++;
-            v = cylinder_64_ni(d, row_point(rc, r));
-        }
-        m |= (uint32_t)v << r;
+        const bool out = fhi < 0.f || flo > f[7];          // frac < 0 or frac > norm for sure
+        const bool within = flo >= 0.f && fhi <= f[6];     // 0 <= frac <= norm for sure
+        const float d1 = __fmaf_rn(f[3], frac, -qx);
+        const float d2 = __fmaf_rn(f[4], frac, -Qy);
+        const float d3 = __fmaf_rn(f[5], frac, -Qz);
+        const float S = __fmaf_rn(d1, d1, __fmaf_rn(d2, d2, d3 * d3));
+        const float g = 1.0001f * Ef + 1.0001f * U32 * (fabsf(frac) + Ef);
+        const float e1 = ax * g + eqx + 1.0001f * U32 * fabsf(d1);
+        const float e2 = ay * g + Ey + 1.0001f * U32 * fabsf(d2);
+        const float e3 = az * g + Ez + 1.0001f * U32 * fabsf(d3);
+        float E = e1 * (2.f * fabsf(d1) + e1) + e2 * (2.f * fabsf(d2) + e2) + e3 * (2.f * fabsf(d3) + e3);
+        E = 1.001f * (E + 3.02f * U32 * S) + 1e-30f;
+        const bool yes = !out && within && __fadd_ru(S, E) <= f[8];
+        const bool no = out || (within && __fsub_rd(S, E) > f[9]);
+        in |= (uint32_t)yes << r;
+        und |= (uint32_t)(!yes && !no) << r;
     }
-    return m;
+    for (uint32_t u = und; u; u &= u - 1) {
+        const int r = __ffs(u) - 1;
+        cnt.esc++;
+        if (cylinder_64_ni(d, row_point(rc, r))) in |= 1u << r;
+    }
+    return in;
 }
 
 __device__ uint32_t capsule_rows64(const double* c, const RowCtx& rc) {
@@ -444,47 +448,45 @@ __device__ uint32_t capsule_rows32(const float* f, const double* d, const RowCtx
     const float ez = 2.001f * U32 * (fabsf(rc.rzf) + fabsf(f[2]));
     const float myz = __fmaf_rn(f[7], vy, f[8] * vz);
     const float emyz = ay * (ey + 4.03f * U32 * fabsf(vy)) + az * (ez + 4.03f * U32 * fabsf(vz));
-    uint32_t m = 0;
+    uint32_t in = 0, und = 0;
+#pragma unroll 2
     for (int r = 0; r < rc.nrows; r++) {
         const float Vy = shf(vy, r), Vz = shf(vz, r), Ey = shf(ey, r), Ez = shf(ez, r);
         const float Ry = shf(rc.ryf, r), Rz = shf(rc.rzf, r);
         const float mag = __fmaf_rn(f[6], vx, shf(myz, r));
         const float Em = 1.001f * (emx + shf(emyz, r)) + 1e-30f;
         const float mlo = __fsub_rd(mag, Em), mhi = __fadd_ru(mag, Em);
-        float d1, d2, d3, e1, e2, e3;
-        int v = -1;
-        if (mlo > f[10]) {
-            d1 = rc.pxf - f[3], d2 = Ry - f[4], d3 = Rz - f[5];
-            e1 = 2.001f * U32 * (fabsf(rc.pxf) + fabsf(f[3]));
-            e2 = 2.001f * U32 * (fabsf(Ry) + fabsf(f[4]));
-            e3 = 2.001f * U32 * (fabsf(Rz) + fabsf(f[5]));
-        } else if (mhi < 0.f && mhi <= f[9]) {
-            d1 = vx, d2 = Vy, d3 = Vz;
-            e1 = ex, e2 = Ey, e3 = Ez;
-        } else if (mlo >= 0.f && mhi <= f[9]) {
-            d1 = __fmaf_rn(-f[6], mag, vx);
-            d2 = __fmaf_rn(-f[7], mag, Vy);
-            d3 = __fmaf_rn(-f[8], mag, Vz);
-            const float g = 1.0001f * Em + 1.0001f * U32 * (fabsf(mag) + Em);
-            e1 = ax * g + ex + 1.0001f * U32 * fabsf(d1);
-            e2 = ay * g + Ey + 1.0001f * U32 * fabsf(d2);
-            e3 = az * g + Ez + 1.0001f * U32 * fabsf(d3);
-        } else {
-            v = 2;
-        }
-        if (v < 0) {
-            const float S = __fmaf_rn(d1, d1, __fmaf_rn(d2, d2, d3 * d3));
-            float E = e1 * (2.f * fabsf(d1) + e1) + e2 * (2.f * fabsf(d2) + e2) + e3 * (2.f * fabsf(d3) + e3);
-            E = 1.001f * (E + 3.02f * U32 * S) + 1e-30f;
-            v = decide_le(S, E, f[11], f[12]);
-        }
-        if (v == 2) {
-            cnt.esc++;
-            v = capsule_64_ni(d, row_point(rc, r));
-        }
-        m |= (uint32_t)v << r;
+        // Closest point: s1 (mag > norm), s0 (mag < 0) or the projection;
+        // selected without branches, undecided when no case is certain.
+        const bool c1 = mlo > f[10];
+        const bool c0 = !c1 && mhi < 0.f && mhi <= f[9];
+        const bool ci = !c1 && !c0 && mlo >= 0.f && mhi <= f[9];
+        const float g = 1.0001f * Em + 1.0001f * U32 * (fabsf(mag) + Em);
+        const float i1 = __fmaf_rn(-f[6], mag, vx), i2 = __fmaf_rn(-f[7], mag, Vy), i3 = __fmaf_rn(-f[8], mag, Vz);
+        const float d1 = c1 ? rc.pxf - f[3] : (c0 ? vx : i1);
+        const float d2 = c1 ? Ry - f[4] : (c0 ? Vy : i2);
+        const float d3 = c1 ? Rz - f[5] : (c0 ? Vz : i3);
+        const float e1 = c1 ? 2.001f * U32 * (fabsf(rc.pxf) + fabsf(f[3]))
+                            : (c0 ? ex : ax * g + ex + 1.0001f * U32 * fabsf(i1));
+        const float e2 = c1 ? 2.001f * U32 * (fabsf(Ry) + fabsf(f[4]))
+                            : (c0 ? Ey : ay * g + Ey + 1.0001f * U32 * fabsf(i2));
+        const float e3 = c1 ? 2.001f * U32 * (fabsf(Rz) + fabsf(f[5]))
+                            : (c0 ? Ez : az * g + Ez + 1.0001f * U32 * fabsf(i3));
+        const float S = __fmaf_rn(d1, d1, __fmaf_rn(d2, d2, d3 * d3));
+        float E = e1 * (2.f * fabsf(d1) + e1) + e2 * (2.f * fabsf(d2) + e2) + e3 * (2.f * fabsf(d3) + e3);
+        E = 1.001f * (E + 3.02f * U32 * S) + 1e-30f;
+        const bool known = c1 || c0 || ci;
+        const bool yes = known && __fadd_ru(S, E) <= f[11];
+        const bool no = known && __fsub_rd(S, E) > f[12];
+        in |= (uint32_t)yes << r;
+        und |= (uint32_t)(!yes && !no) << r;
     }
-    return m;
+    for (uint32_t u = und; u; u &= u - 1) {
+        const int r = __ffs(u) - 1;
+        cnt.esc++;
+        if (capsule_64_ni(d, row_point(rc, r))) in |= 1u << r;
+    }
+    return in;
 }
 
 template <int PREC>
