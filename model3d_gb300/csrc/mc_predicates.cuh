@@ -205,9 +205,10 @@ __device__ __forceinline__ int cylinder_32(const float* f, F3 p) {
     float Ef = 1.001f * (ax * (eqx + 4.03f * U32 * fabsf(qx)) + ay * (eqy + 4.03f * U32 * fabsf(qy)) +
                          az * (eqz + 4.03f * U32 * fabsf(qz))) + 1e-30f;
     float flo = __fsub_rd(frac, Ef), fhi = __fadd_ru(frac, Ef);
-    if (fhi < 0.f) return 0;          // frac < 0
-    if (flo > f[7]) return 0;         // frac > norm
-    if (!(flo >= 0.f && fhi <= f[6])) return 2;
+    // Branch-free: frac < 0 or > norm for sure -> 0; not surely inside
+    // [0, norm] -> undecided; else the distance decides.
+    const bool out = fhi < 0.f || flo > f[7];
+    const bool within = flo >= 0.f && fhi <= f[6];
     float d1 = __fmaf_rn(f[3], frac, -qx);
     float d2 = __fmaf_rn(f[4], frac, -qy);
     float d3 = __fmaf_rn(f[5], frac, -qz);
@@ -218,7 +219,8 @@ __device__ __forceinline__ int cylinder_32(const float* f, F3 p) {
     float e3 = az * g + eqz + 1.0001f * U32 * fabsf(d3);
     float E = e1 * (2.f * fabsf(d1) + e1) + e2 * (2.f * fabsf(d2) + e2) + e3 * (2.f * fabsf(d3) + e3);
     E = 1.001f * (E + 3.02f * U32 * S) + 1e-30f;
-    return decide_le(S, E, f[8], f[9]);
+    const int v = decide_le(S, E, f[8], f[9]);
+    return out ? 0 : (within ? v : 2);
 }
 
 // Capsule: v2 = p - s0, mag = v.v2; closest point chosen by mag vs [0, norm].
@@ -232,30 +234,25 @@ __device__ __forceinline__ int capsule_32(const float* f, F3 p) {
     float Em = 1.001f * (ax * (ex + 4.03f * U32 * fabsf(vx)) + ay * (ey + 4.03f * U32 * fabsf(vy)) +
                          az * (ez + 4.03f * U32 * fabsf(vz))) + 1e-30f;
     float mlo = __fsub_rd(mag, Em), mhi = __fadd_ru(mag, Em);
-    float d1, d2, d3, e1, e2, e3;
-    if (mlo > f[10]) {  // mag > norm: closest = s1
-        d1 = p.x - f[3], d2 = p.y - f[4], d3 = p.z - f[5];
-        e1 = 2.001f * U32 * (fabsf(p.x) + fabsf(f[3]));
-        e2 = 2.001f * U32 * (fabsf(p.y) + fabsf(f[4]));
-        e3 = 2.001f * U32 * (fabsf(p.z) + fabsf(f[5]));
-    } else if (mhi < 0.f && mhi <= f[9]) {  // mag < 0 (and not > norm): closest = s0
-        d1 = vx, d2 = vy, d3 = vz;
-        e1 = ex, e2 = ey, e3 = ez;
-    } else if (mlo >= 0.f && mhi <= f[9]) {  // interior: closest = v*mag + s0
-        d1 = __fmaf_rn(-f[6], mag, vx);
-        d2 = __fmaf_rn(-f[7], mag, vy);
-        d3 = __fmaf_rn(-f[8], mag, vz);
-        float g = 1.0001f * Em + 1.0001f * U32 * (fabsf(mag) + Em);
-        e1 = ax * g + ex + 1.0001f * U32 * fabsf(d1);
-        e2 = ay * g + ey + 1.0001f * U32 * fabsf(d2);
-        e3 = az * g + ez + 1.0001f * U32 * fabsf(d3);
-    } else {
-        return 2;
-    }
+    // Closest point, selected without branches: s1 (mag > norm for sure),
+    // s0 (mag < 0 for sure) or the projection (0 <= mag <= norm for sure);
+    // undecided when no case is certain.
+    const bool c1 = mlo > f[10];
+    const bool c0 = !c1 && mhi < 0.f && mhi <= f[9];
+    const bool ci = !c1 && !c0 && mlo >= 0.f && mhi <= f[9];
+    const float g = 1.0001f * Em + 1.0001f * U32 * (fabsf(mag) + Em);
+    const float i1 = __fmaf_rn(-f[6], mag, vx), i2 = __fmaf_rn(-f[7], mag, vy), i3 = __fmaf_rn(-f[8], mag, vz);
+    const float d1 = c1 ? p.x - f[3] : (c0 ? vx : i1);
+    const float d2 = c1 ? p.y - f[4] : (c0 ? vy : i2);
+    const float d3 = c1 ? p.z - f[5] : (c0 ? vz : i3);
+    const float e1 = c1 ? 2.001f * U32 * (fabsf(p.x) + fabsf(f[3])) : (c0 ? ex : ax * g + ex + 1.0001f * U32 * fabsf(i1));
+    const float e2 = c1 ? 2.001f * U32 * (fabsf(p.y) + fabsf(f[4])) : (c0 ? ey : ay * g + ey + 1.0001f * U32 * fabsf(i2));
+    const float e3 = c1 ? 2.001f * U32 * (fabsf(p.z) + fabsf(f[5])) : (c0 ? ez : az * g + ez + 1.0001f * U32 * fabsf(i3));
     float S = __fmaf_rn(d1, d1, __fmaf_rn(d2, d2, d3 * d3));
     float E = e1 * (2.f * fabsf(d1) + e1) + e2 * (2.f * fabsf(d2) + e2) + e3 * (2.f * fabsf(d3) + e3);
     E = 1.001f * (E + 3.02f * U32 * S) + 1e-30f;
-    return decide_le(S, E, f[11], f[12]);
+    const int v = decide_le(S, E, f[11], f[12]);
+    return (c1 || c0 || ci) ? v : 2;
 }
 
 }  // namespace mcgpu
