@@ -764,7 +764,7 @@ void lower_scene(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets, s
                  HostProgram* P) {
     *P = HostProgram();
     if (!nodes || n_nodes == 0) throw LowerError(MC_ERR_ARG, "empty node array");
-    Lowerer L{nodes, n_nodes, sets, n_sets, P};
+    Lowerer L{nodes, n_nodes, sets, n_sets, P, 0, 0, 0, {}};
     L.lower(-1);
     if (L.pos != n_nodes) throw LowerError(MC_ERR_BAD_PROGRAM, "trailing nodes after the root");
     for (int i = 0; i < 3; i++) {

@@ -4,8 +4,6 @@ Bit-exact: every mesh is compared as the sorted list of its triangles' nine
 float64 bit patterns (triangle vertex order kept), for both precision modes
 (FP64 and FP32-filtered) and with tile culling on and off.
 """
-import math
-
 import numpy as np
 import pytest
 

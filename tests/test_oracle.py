@@ -13,10 +13,9 @@ import math
 import numpy as np
 import pytest
 
-from model3d_gb300 import (Capsule, Cylinder, IntersectedSolid, JoinedSolid, Rect, Sphere,
-                           SubtractedSolid, Torus, XYZ, serialize, MeshToCollider,
-                           NewColliderSolid, TransformSolid, Translate, Scale, VecScale,
-                           Matrix3Transform, JoinedTransform, Rotation, CacheSolidBounds)
+from model3d_gb300 import (Capsule, Cylinder, IntersectedSolid, JoinedSolid, JoinedTransform,
+                           MeshToCollider, NewColliderSolid, Rect, Rotation, Scale, Sphere, Torus,
+                           TransformSolid, Translate, VecScale, XYZ, serialize)
 from model3d_gb300.workloads import SplitMix64, csg_tree, displaced_icosphere, random_primitive
 
 
