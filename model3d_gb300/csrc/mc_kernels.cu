@@ -862,7 +862,7 @@ __device__ __forceinline__ void block_sum2(uint32_t& a, uint32_t& b) {
 // the search bisects together -- stay within a few rows of one tile rather
 // than spreading along whole grid rows, and the warp's culled program keeps
 // fewer leaves.  A grid has at most 2^31 corners, so chunk indices fit int.
-constexpr int kChunkTY = 8, kChunkTZ = 8;
+constexpr int kChunkTY = 16, kChunkTZ = 16;
 
 __device__ __forceinline__ int chunk_index(const GridView& g, int c, int y, int z) {
     const int nyc = g.ny - 1, nzc = g.nz - 1;
