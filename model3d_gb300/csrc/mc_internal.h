@@ -59,7 +59,7 @@ enum LeafKind : int32_t {
 //   RECT     : min.xyz, max.xyz
 //   CYLINDER : P2.xyz, dir.xyz, norm, TR
 //   CAPSULE  : s0.xyz, s1.xyz, v.xyz, norm, TR
-//   TORUS    : center.xyz, b1.xyz, b2.xyz, outer, T_inner
+//   TORUS    : center.xyz, b1.xyz, b2.xyz, outer, T_inner (FP32 also T_lo, T_hi)
 //   COLLIDER : min.xyz, max.xyz, (double)tree index
 constexpr int LEAF_D = 16;
 // FP32 filter constants per leaf (floats), same order rounded to float, plus

@@ -176,14 +176,15 @@ __device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf
     cnt.leaf++;
     if (PREC == MC_PREC_FP32_FILTERED) {
         const int kind = P.leaf_kind[id];
-        if (kind <= LK_CAPSULE) {
+        if (kind <= LK_TORUS) {
             const float* f = P.leaf_f + (size_t)id * LEAF_F;
             int r;
             switch (kind) {
                 case LK_SPHERE: r = sphere_32(f, pf); break;
                 case LK_RECT: r = rect_32(f, pf); break;
                 case LK_CYLINDER: r = cylinder_32(f, pf); break;
-                default: r = capsule_32(f, pf); break;
+                case LK_CAPSULE: r = capsule_32(f, pf); break;
+                default: r = torus_32(f, pf); break;
             }
             if (r != 2) return r;
             cnt.esc++;
@@ -506,9 +507,15 @@ __device__ __forceinline__ uint32_t leaf_rows(const ProgView& P, int id, const R
             for (int r = 0; r < rc.nrows; r++) {
                 const F3 pf{rc.pxf, shf(rc.ryf, r), shf(rc.rzf, r)};
                 const P3 p = row_point(rc, r);
-                bool v = (f32 && kind == LK_COLLIDER) ? collider_point(P, d, p, pf, true, cnt, err)
-                                                      : leaf64_point(P, id, p, cnt, err);
-                m |= (v ? 1u : 0u) << r;
+                int v = 2;
+                if (f32 && kind == LK_COLLIDER) {
+                    v = collider_point(P, d, p, pf, true, cnt, err) ? 1 : 0;
+                } else if (f32) {
+                    v = torus_32(f, pf);
+                    if (v == 2) cnt.esc++;
+                }
+                if (v == 2) v = leaf64_point(P, id, p, cnt, err) ? 1 : 0;
+                m |= (uint32_t)v << r;
             }
             return m;
         }

@@ -642,11 +642,13 @@ struct Lowerer {
                 double Ti = std::isinf(inner) && inner > 0 ? DBL_MAX : sqrt_threshold(inner);
                 double d[11] = {c.v[0],  c.v[1],  c.v[2],  b1.v[0], b1.v[1], b1.v[2],
                                 b2.v[0], b2.v[1], b2.v[2], outer_r, Ti};
-                float f[11];
+                float f[13];
                 for (int i = 0; i < 11; i++) f[i] = (float)d[i];
+                f[11] = f_down(Ti);  // threshold bounds of the FP32 filter
+                f[12] = f_up(Ti);
                 double ext = std::fabs(outer_r) + std::fabs(inner);
                 set_cull(vsub(c, d3(ext, ext, ext)), vadd(c, d3(ext, ext, ext)));
-                int id = add_leaf(LK_TORUS, d, 11, f, 11, cull);
+                int id = add_leaf(LK_TORUS, d, 11, f, 13, cull);
                 leaf_out(id);
                 return;
             }

@@ -255,6 +255,53 @@ __device__ __forceinline__ int capsule_32(const float* f, F3 p) {
     return (c1 || c0 || ci) ? v : 2;
 }
 
+// Torus (genericSDF ring point, shapes.go:1451-1487, as torus_64): with
+// c = p - center, x = b1.c, y = b2.c, on = |(x, y)|, s = outer / on, the ring
+// point is center + (b1 x + b2 y) s and S = |ring - p|^2 is compared with the
+// threshold.  The bound carries the errors of x and y (as the cylinder's
+// frac), of r2 = x^2 + y^2, of on = sqrt(r2) (|on - on*| <= Er2 / (on + on*)
+// + u on) and of s (relative Eon / on_lo plus the roundings of the division
+// and of outer).  Points near the axis, where that relative error exceeds
+// 1%, are undecided; so are all points the reference would treat as on the
+// axis (on == 0), which lie far inside that band.
+__device__ __forceinline__ int torus_32(const float* f, F3 p) {
+    const float cx = p.x - f[0], cy = p.y - f[1], cz = p.z - f[2];
+    const float ex = 2.001f * U32 * (fabsf(p.x) + fabsf(f[0]));
+    const float ey = 2.001f * U32 * (fabsf(p.y) + fabsf(f[1]));
+    const float ez = 2.001f * U32 * (fabsf(p.z) + fabsf(f[2]));
+    const float x = __fmaf_rn(f[3], cx, __fmaf_rn(f[4], cy, f[5] * cz));
+    const float y = __fmaf_rn(f[6], cx, __fmaf_rn(f[7], cy, f[8] * cz));
+    const float Ex = 1.001f * (fabsf(f[3]) * (ex + 4.03f * U32 * fabsf(cx)) + fabsf(f[4]) * (ey + 4.03f * U32 * fabsf(cy)) +
+                               fabsf(f[5]) * (ez + 4.03f * U32 * fabsf(cz))) + 1e-30f;
+    const float Ey = 1.001f * (fabsf(f[6]) * (ex + 4.03f * U32 * fabsf(cx)) + fabsf(f[7]) * (ey + 4.03f * U32 * fabsf(cy)) +
+                               fabsf(f[8]) * (ez + 4.03f * U32 * fabsf(cz))) + 1e-30f;
+    const float r2 = __fmaf_rn(x, x, y * y);
+    const float Er2 = 1.001f * (Ex * (2.f * fabsf(x) + Ex) + Ey * (2.f * fabsf(y) + Ey) + 3.01f * U32 * r2) + 1e-30f;
+    const float r2lo = __fsub_rd(r2, Er2);
+    if (!(r2lo > 0.f)) return 2;
+    const float on = __fsqrt_rn(r2), onlo = __fsqrt_rd(r2lo);
+    const float Eon = 1.001f * (__fdiv_ru(Er2, on + onlo) + U32 * on) + 1e-30f;
+    const float rsc = 1.001f * __fdiv_ru(Eon, onlo) + 2.01f * U32;  // relative error of s
+    if (!(rsc <= 0.01f)) return 2;
+    const float sc = __fdiv_rn(f[9], on);
+    const float xs = x * sc, ys = y * sc;
+    const float Exs = 1.01f * ((fabsf(x) + Ex) * sc * rsc + Ex * sc + U32 * fabsf(xs)) + 1e-30f;
+    const float Eys = 1.01f * ((fabsf(y) + Ey) * sc * rsc + Ey * sc + U32 * fabsf(ys)) + 1e-30f;
+    const float d1 = __fmaf_rn(f[3], xs, __fmaf_rn(f[6], ys, -cx));
+    const float d2 = __fmaf_rn(f[4], xs, __fmaf_rn(f[7], ys, -cy));
+    const float d3 = __fmaf_rn(f[5], xs, __fmaf_rn(f[8], ys, -cz));
+    const float e1 = fabsf(f[3]) * Exs + fabsf(f[6]) * Eys + ex +
+                     4.03f * U32 * (fabsf(f[3] * xs) + fabsf(f[6] * ys) + fabsf(cx));
+    const float e2 = fabsf(f[4]) * Exs + fabsf(f[7]) * Eys + ey +
+                     4.03f * U32 * (fabsf(f[4] * xs) + fabsf(f[7] * ys) + fabsf(cy));
+    const float e3 = fabsf(f[5]) * Exs + fabsf(f[8]) * Eys + ez +
+                     4.03f * U32 * (fabsf(f[5] * xs) + fabsf(f[8] * ys) + fabsf(cz));
+    const float S = __fmaf_rn(d1, d1, __fmaf_rn(d2, d2, d3 * d3));
+    float E = e1 * (2.f * fabsf(d1) + e1) + e2 * (2.f * fabsf(d2) + e2) + e3 * (2.f * fabsf(d3) + e3);
+    E = 1.001f * (E + 3.02f * U32 * S) + 1e-30f;
+    return decide_le(S, E, f[11], f[12]);
+}
+
 }  // namespace mcgpu
 
 namespace mcgpu {

@@ -401,3 +401,28 @@ def test_long_thin_grid_near_the_key_limit(oracle):
     solid thinner than one cell in y and z."""
     s = Rect(XYZ(-1, 0, 0), XYZ(1, 1.5e-6, 1.5e-6))
     _check(oracle, s, 2.0 / 600000, 8, modes=[("fp32", True), ("fp64", True)])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_torus_contains_near_surface_and_axis(oracle, prec):
+    """The FP32 torus filter: points on the tube surface and one ulp off it,
+    points on and next to the symmetry axis (the reference's on == 0 case),
+    and random points; all equal the oracle."""
+    rng = np.random.default_rng(31)
+    for center, axis, R, r in ((XYZ(0.1, -0.2, 0.3), XYZ(0.3, 1, -0.2), 0.6, 0.2),
+                               (XYZ(0, 0, 0), XYZ(0, 0, 1), 0.5, 0.25),
+                               (XYZ(0.2, 0.1, 0), XYZ(1, 1, 1), 0.3, 0.35)):
+        s = Torus(center, axis, R, r)
+        c = np.array(center.Array())
+        a = np.array(axis.Array()) / np.linalg.norm(axis.Array())
+        u = np.cross(a, [0.3, 0.5, 0.7])
+        u /= np.linalg.norm(u)
+        v = np.cross(a, u)
+        th, ph = rng.uniform(0, 2 * np.pi, (2, 4000))
+        ring = c + R * (np.cos(th)[:, None] * u + np.sin(th)[:, None] * v)
+        surf = ring + r * (np.cos(ph)[:, None] * (ring - c) / R + np.sin(ph)[:, None] * a)
+        on_axis = c + rng.uniform(-1, 1, (500, 1)) * a
+        pts = np.concatenate([surf, np.nextafter(surf, np.inf), np.nextafter(surf, -np.inf), on_axis,
+                              on_axis + 1e-9 * u, rng.uniform(-1.5, 1.5, (4000, 3)) + c])
+        ref, _ = oracle.contains(*serialize(s), pts)
+        assert (Contains(s, pts, precision=prec) == ref).all()
