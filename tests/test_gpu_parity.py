@@ -199,10 +199,10 @@ def test_contains_parity(oracle, prec):
 
 
 def test_filter_escalation_rate_is_small():
-    m = MarchingCubesSearch(csg_tree(1, 48, 16), 0.01, 8, precision="fp32")
-    st = m.stats
-    assert st["leaf_evals"] > 0
-    assert st["escalations"] <= 0.01 * st["leaf_evals"]
+    for s in (csg_tree(1, 48, 16), Torus(XYZ(0.1, -0.2, 0.3), XYZ(0.3, 1, -0.2), 0.6, 0.2)):
+        st = MarchingCubesSearch(s, 0.01, 8, precision="fp32").stats
+        assert st["leaf_evals"] > 0
+        assert st["escalations"] <= 0.01 * st["leaf_evals"]
 
 
 def _closed_oriented(tris):
