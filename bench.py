@@ -462,7 +462,7 @@ def collider_batch_line(ctx, count):
 # each kernel on this workload, from an ncu capture of the full-size grid.
 # Below the algorithmic bytes where a kernel reads what the previous one
 # left in the 129 MB L2 (keys, corner bits) or its writes stay in L2.
-NCU_TRAFFIC = {"k_classify": 14679808, "k_count": 29755648, "k_emit": 67178240, "k_search": 39695360}
+NCU_TRAFFIC = {"k_classify": 14012416, "k_count": 29758976, "k_emit": 69824768, "k_search": 39974144}
 
 
 def roofline(kernel, ms, st, peaks, kind):
