@@ -426,3 +426,22 @@ def test_torus_contains_near_surface_and_axis(oracle, prec):
                               on_axis + 1e-9 * u, rng.uniform(-1.5, 1.5, (4000, 3)) + c])
         ref, _ = oracle.contains(*serialize(s), pts)
         assert (Contains(s, pts, precision=prec) == ref).all()
+
+
+def test_result_entry_errors():
+    """Misuse of the result entry points returns statuses, not crashes."""
+    import ctypes
+    from model3d_gb300 import Context, DeviceSolid, MarchingCubesSearch
+    ctx = Context(0)
+    L = N.lib()
+    ds = DeviceSolid(Sphere(XYZ(0, 0, 0), 0.5), ctx)
+    MarchingCubesSearch(ds, 0.1, 8, ctx=ctx)   # no interior points requested
+    buf = np.zeros((10, 3))
+    assert L.mc_result_interior_copy(ctx.ptr, buf.ctypes.data) == N.MC_ERR_ARG
+    n = ctypes.c_size_t()
+    assert L.mc_result_stl(ctx.ptr, None, 0, ctypes.byref(n)) == N.MC_OK and n.value > 84
+    small = np.zeros(16, dtype=np.uint8)
+    assert L.mc_result_stl(ctx.ptr, small.ctypes.data, 16, ctypes.byref(n)) == N.MC_ERR_ARG
+    bad = np.zeros(1, dtype=serialize(Sphere(XYZ(0, 0, 0), 1.0))[0].dtype)
+    bad[0]["kind"] = 99
+    assert L.mc_result_transform(ctx.ptr, bad.ctypes.data, 1, 0) == N.MC_ERR_BAD_PROGRAM
