@@ -404,8 +404,33 @@ def other_configs(ctx, torch, flush, single_rate, count=16):
         "largest_job_alone": {"corners": br["corners"], "triangles": br["triangles"],
                               "fp32_corners_per_s": big_rate},
         "fraction_of_largest_job_alone_rate": (corners / (res["fp32"][0] / 1e3)) / big_rate}
+    out.update(metaball_line(ctx, torch, flush))
     out.update(collider_batch_line(ctx, count))
     return out
+
+
+def metaball_line(ctx, torch, flush):
+    """A 64-ball quartic MetaballSolid (metaball_blob(3, 64), 3/4 spheres and
+    1/4 capsules) at delta 0.005, FP32-filtered against FP64, with the two
+    precisions' meshes compared bit for bit."""
+    from model3d_gb300 import DeviceSolid, MarchingCubesSearch, canonical
+    from model3d_gb300 import _native as N
+    from model3d_gb300.workloads import metaball_blob
+    L = N.lib()
+    ds = DeviceSolid(metaball_blob(3, 64), ctx)
+    a = _device_rate(L, N, ctx, ds, 0.005, 8, N.MC_PREC_FP32_FILTERED, flush, torch, reps=2)
+    b = _device_rate(L, N, ctx, ds, 0.005, 8, N.MC_PREC_FP64, flush, torch, reps=1)
+    m32 = MarchingCubesSearch(ds, 0.005, 8, precision="fp32", ctx=ctx)
+    m64 = MarchingCubesSearch(ds, 0.005, 8, precision="fp64", ctx=ctx)
+    same = bool(np.array_equal(canonical(m32.TriangleSoup()), canonical(m64.TriangleSoup())))
+    return {"metaball_blob64_quartic_delta0.005": {
+        "grid": [a["nx"], a["ny"], a["nz"]], "balls": 64, "triangles": a["triangles"],
+        "fp32_corners_per_s": a["corners"] / (a["ms_total"] / 1e3),
+        "fp64_corners_per_s": b["corners"] / (b["ms_total"] / 1e3),
+        "ms_fp32": a["ms_total"], "ms_fp64": b["ms_total"],
+        "phases_ms_fp32": {k: a[k] for k in ("ms_classify", "ms_count", "ms_emit", "ms_search")},
+        "escalation_rate": a["escalations"] / max(1, a["leaf_evals"]),
+        "bit_identical_fp32_fp64": same}}
 
 
 def collider_batch_line(ctx, count):

@@ -71,6 +71,19 @@ enum {
     MC_NODE_TORUS = 5,     /* p = Center.xyz, Axis.xyz, Outer, Inner (model3d/shapes.go:1323-1365) */
     MC_NODE_COLLIDER = 6,  /* NewColliderSolid(collider) over triangle set `mesh`
                               (model3d/solid.go:247-305, collisions.go:119-212) */
+    MC_NODE_METABALL = 7,  /* WeightedMetaballSolid(f, radiusThreshold, balls, weights)
+                              (model3d/metaball.go:165-242): min/max = its bounds (the
+                              outset box, computed by the caller as the reference does);
+                              p = radiusThreshold, MC_FALLOFF_*, falloff parameter;
+                              n_children MC_NODE_BALL records follow.  With no positive
+                              weight the reference returns NewRect(Origin, Origin), and
+                              so does the library. */
+    MC_NODE_BALL = 8,      /* One metaball term (only as a child of MC_NODE_METABALL):
+                              p[0] = weight; n_steps MC_XF_* records follow (the forward
+                              transform of TransformMetaball / VecScaleMetaball, innermost
+                              first, model3d/transform.go:319-414), then one SPHERE, RECT,
+                              CYLINDER, CAPSULE or TORUS record whose MetaballField is
+                              -SDF (shapes.go:100, :255, :466, :712, :1431). */
     /* Combinators. */
     MC_NODE_JOIN = 16,      /* JoinedSolid, n_children >= 1      (model3d/solid.go:71-98)    */
     MC_NODE_SUBTRACT = 17,  /* SubtractedSolid, children = Positive, Negative (solid.go:120-142) */
@@ -86,8 +99,15 @@ enum {
     MC_XF_TRANSLATE = 32,   /* p = Offset.xyz   (model3d/transform.go:40-58)   */
     MC_XF_SCALE = 33,       /* p = Scale        (model3d/transform.go:67-89)   */
     MC_XF_VECSCALE = 34,    /* p = Scale.xyz    (model3d/transform.go:100-118) */
-    MC_XF_MATRIX = 35       /* p = Matrix3, row-major (model3d/transform.go:127-157; Rotation
+    MC_XF_MATRIX = 35,      /* p = Matrix3, row-major (model3d/transform.go:127-157; Rotation
                                and Mirror are Matrix3 transforms as well) */
+    /* Falloff functions of MC_NODE_METABALL (p[1]); p[2] is the parameter. */
+    MC_FALLOFF_POWER = 1,   /* InversePowerMetaballFalloffFunc(p[2]), p[2] a positive integer
+                               below 2^20: math.Pow(r, -p[2]), +Inf for r <= 0
+                               (model3d/metaball.go:17-28; Linear..Quintic are 1..5) */
+    MC_FALLOFF_WYVILL = 2   /* WyvillMetaballFalloffFunc(p[2]) (model3d/metaball.go:86-103).
+                               Exponential and Gaussian falloffs call math.Exp, which Go
+                               implements per architecture in assembly: not lowerable. */
 };
 
 /*

@@ -2,7 +2,7 @@
 
 The reference-facing names (Sphere, Cylinder, JoinedSolid, TransformSolid,
 MeshToCollider, NewColliderSolid, MarchingCubesSearch, ...) mirror package
-model3d of unixpickle/model3d.  Containment, cube classification, vertex
+model3d of unixpickle/model3d (metaball solids included).  Containment, cube classification, vertex
 dedup and the bisection search run in CUDA kernels for sm_103a
 (model3d_gb300/csrc); results are bit-identical to the reference algorithm.
 """
@@ -13,6 +13,13 @@ from .solids import (Capsule, CacheSolidBounds, ColliderSolid, Cylinder, ForceSo
                      NewRect, NotLowerable, Rect, RotateSolid, Rotation, Scale, ScaleSolid,
                      Solid, Sphere, Subtract, SubtractedSolid, Torus, TransformSolid, Translate,
                      TranslateSolid, VecScale, VecScaleSolid, serialize)
+from .metaballs import (CubicMetaballFalloffFunc, ExponentialMetaballFalloffFunc,
+                        GaussianMetaballFalloffFunc, InversePowerMetaballFalloffFunc,
+                        LinearMetaballFalloffFunc, MetaballSolid, QuadraticMetaballFalloffFunc,
+                        QuarticMetaballFalloffFunc, QuinticMetaballFalloffFunc, RotateMetaball,
+                        ScaleMetaball, SDFToMetaball, SignedMetaballSolid, TransformMetaball,
+                        TranslateMetaball, VecScaleMetaball, WeightedMetaballSolid,
+                        WyvillMetaballFalloffFunc)
 from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesC2F, MarchingCubesConj,
                  MarchingCubesFilter, MarchingCubesSearchFilter,
                  MarchingCubesInterior, MarchingCubesSearch, MarchingCubesSearchBatch,

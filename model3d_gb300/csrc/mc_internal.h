@@ -52,6 +52,7 @@ enum LeafKind : int32_t {
     LK_CAPSULE = 4,
     LK_TORUS = 5,
     LK_COLLIDER = 6,
+    LK_METABALL = 7,
 };
 
 // FP64 constants per leaf (doubles), kind-specific layout:
@@ -61,6 +62,7 @@ enum LeafKind : int32_t {
 //   CAPSULE  : s0.xyz, s1.xyz, v.xyz, norm, TR
 //   TORUS    : center.xyz, b1.xyz, b2.xyz, outer, T_inner (FP32 also T_lo, T_hi)
 //   COLLIDER : min.xyz, max.xyz, (double)tree index
+//   METABALL : (double)index into metas / metas_f
 constexpr int LEAF_D = 16;
 // FP32 filter constants per leaf (floats), same order rounded to float, plus
 // thresholds: [..., TR_lo, TR_hi] / [..., norm_lo, norm_hi, TR_lo, TR_hi].
@@ -153,6 +155,59 @@ struct TreeD {
     int32_t all_first, all_count;  // RayEnt range tested by every ray
 };
 
+// Kernel mode: bit 0 is the precision (MC_PREC_*); MODE_MB adds the metaball
+// leaf path.  Programs without metaball leaves run kernels built without it,
+// so the evaluation loops of the other kinds compile as if it did not exist.
+constexpr int MODE_MB = 2;
+__host__ __device__ constexpr bool mode_f32(int mode) { return (mode & 1) == 1; }
+__host__ __device__ constexpr bool mode_mb(int mode) { return (mode & MODE_MB) != 0; }
+
+// Metaball leaves: WeightedMetaballSolid (model3d/metaball.go:165-242) is
+// InBounds(lo, hi) && sum_i w_i f(-SDF_i(inv_i(c))) > thr, summed in ball
+// order in float64.  The FP32 filter brackets every -SDF_i by an absolute
+// error bound kerr * (S + |r|) (S = largest |coordinate| of the point plus the
+// largest |constant| of the ball), brackets f over that interval with directed
+// rounding, sums lower and upper bounds, and decides when the bracket (widened
+// by 2^-40 of the summed magnitudes for the float64 roundings) clears thr.
+constexpr int MAX_BALLS = 4096;
+struct MetaD {
+    double lo[3], hi[3];  // bounds of the CheckedFuncSolid
+    double thr;           // f(radiusThreshold)
+    double param;         // power k (MC_FALLOFF_POWER) or d (MC_FALLOFF_WYVILL)
+    double d2;            // d * d, as the Wyvill closure precomputes it
+    int32_t falloff;      // MC_FALLOFF_*
+    int32_t first_ball, n_balls;
+    int32_t never;        // thr is +Inf or NaN: sum > thr never holds
+};
+struct MetaF {
+    float lo_dn[3], lo_up[3], hi_dn[3], hi_up[3];  // bounds rounded down / up
+    float thr_lo, thr_hi;
+    float d_lo, d_hi, d2_lo, d2_hi;
+    int32_t k;  // power (MC_FALLOFF_POWER)
+    int32_t pad;
+};
+// One ball; constants by primitive (LK_*):
+//   SPHERE   : center.xyz, R
+//   RECT     : min.xyz, max.xyz
+//   CAPSULE  : P1.xyz, P2.xyz, axis.xyz, norm, R       (axis = (P2-P1) * (1/norm))
+//   CYLINDER : the capsule's 11, then OrthoBasis(-axis) (P1 cap) and
+//              OrthoBasis(axis) (P2 cap): b1.xyz, b2.xyz each
+//   TORUS    : center.xyz, b1.xyz, b2.xyz, outer, inner (b1, b2 = OrthoBasis(Axis))
+constexpr int BALL_C = 24;
+struct BallD {
+    int32_t kind;
+    int32_t first_step, n_steps;  // inverse transform steps in xstep, apply order
+    int32_t pad;
+    double w;
+    double c[BALL_C];
+};
+struct BallF {
+    float w_lo, w_hi;  // weight rounded down / up
+    float mag;         // largest |constant|
+    float kerr;        // error-bound factor of the kind
+    float c[BALL_C];
+};
+
 // Device view of one lowered solid (passed by value to kernels).
 struct ProgView {
     const uint32_t* ops;
@@ -172,10 +227,15 @@ struct ProgView {
     const RayEnt* ents;
     const TriD* tris;
     const TriF* tris_f;
+    const MetaD* metas;
+    const MetaF* metas_f;
+    const BallD* balls;
+    const BallF* balls_f;
     int32_t n_ops;
     int32_t n_ops_allfalse;  // -1: const false, -2: const true, else length
     int32_t n_leaves;
     int32_t n_xbox;
+    int32_t has_metaball;  // launch the kernels built with the metaball path (MODE_MB)
     int32_t rows_ok;  // no TRANSFORM node: tiles may be evaluated row-vectorised
     int32_t fold_cap; // longest folded program (words)
 };

@@ -156,12 +156,379 @@ __device__ __forceinline__ P3 apply_inverse(const ProgView& P, const XBoxD& b, P
     return apply_steps(P.xstep + b.first_step, b.n_steps, p);
 }
 
+// The instantiation of kernel template K for a precision and metaball use.
+#define MC_PICK(K, prec, mb)                                                                   \
+    ((prec) == MC_PREC_FP64 ? ((mb) ? K<MODE_MB | MC_PREC_FP64> : K<MC_PREC_FP64>)             \
+                            : ((mb) ? K<MODE_MB | MC_PREC_FP32_FILTERED> : K<MC_PREC_FP32_FILTERED>))
+
+// ------------------------------------------------------------ metaballs
+
+// math.Ldexp and math.Pow(x, -k) for x > 0 (Go math/ldexp.go, math/pow.go),
+// operation for operation: Frexp, repeated squaring of the mantissa with
+// renormalisation to [0.5, 1), one reciprocal, Ldexp.
+__device__ double go_ldexp_d(double frac, long long exp) {
+    if (frac == 0 || isinf(frac) || isnan(frac)) return frac;
+    if (fabs(frac) < 2.2250738585072014e-308) {
+        frac = D_MUL(frac, 4503599627370496.0);
+        exp -= 52;
+    }
+    unsigned long long x = (unsigned long long)__double_as_longlong(frac);
+    exp += (long long)((x >> 52) & 0x7ff) - 1023;
+    if (exp < -1075) return copysign(0.0, frac);
+    if (exp > 1023) return frac < 0 ? -INFINITY : INFINITY;
+    double m = 1;
+    if (exp < -1022) {
+        exp += 53;
+        m = 1.1102230246251565e-16;  // 2^-53
+    }
+    x &= ~(0x7ffull << 52);
+    x |= (unsigned long long)(exp + 1023) << 52;
+    return D_MUL(m, __longlong_as_double((long long)x));
+}
+
+__device__ double go_pow_neg(double x, int k) {  // math.Pow(x, -k), k >= 1
+    if (x == 1) return 1;
+    if (isnan(x)) return x;
+    if (isinf(x)) return 0;
+    int xe_i;
+    double x1 = frexp(x, &xe_i);
+    long long xe = xe_i, ae = 0;
+    double a1 = 1;
+    for (int i = k; i != 0; i >>= 1) {
+        if (xe < -(1 << 12) || (1 << 12) < xe) {
+            ae += xe;
+            break;
+        }
+        if (i & 1) {
+            a1 = D_MUL(a1, x1);
+            ae += xe;
+        }
+        x1 = D_MUL(x1, x1);
+        xe <<= 1;
+        if (x1 < .5) {
+            x1 = D_ADD(x1, x1);
+            xe--;
+        }
+    }
+    return go_ldexp_d(D_DIV(1.0, a1), -ae);
+}
+
+__device__ __forceinline__ double dist3_64(double ax, double ay, double az, double bx, double by, double bz) {
+    double d1 = D_SUB(ax, bx), d2 = D_SUB(ay, by), d3 = D_SUB(az, bz);  // Coord3D.Dist, coords.go:272-277
+    return D_SQRT(D_ADD(D_ADD(D_MUL(d1, d1), D_MUL(d2, d2)), D_MUL(d3, d3)));
+}
+
+// math.Min / math.Max: -Inf (+Inf) first, then NaN, then -0 below +0.
+__device__ __forceinline__ double go_min_d(double x, double y) {
+    if (x == -INFINITY || y == -INFINITY) return -INFINITY;
+    if (isnan(x) || isnan(y)) return x + y;
+    if (x == 0 && y == 0) return signbit(x) ? x : y;
+    return x < y ? x : y;
+}
+__device__ __forceinline__ double go_max_d(double x, double y) {
+    if (x == INFINITY || y == INFINITY) return INFINITY;
+    if (isnan(x) || isnan(y)) return x + y;
+    if (x == 0 && y == 0) return signbit(x) ? y : x;
+    return x > y ? x : y;
+}
+
+// filledCircleDist (shapes.go:783-812): basis rows b1, b2 (c + 0, c + 3),
+// proj.z given (the axis row times q).
+__device__ __forceinline__ void circle_dist_64(const double* b, double qx, double qy, double qz, double pz, double R,
+                                               double* cur) {
+    double px = D_ADD(D_ADD(D_MUL(b[0], qx), D_MUL(b[1], qy)), D_MUL(b[2], qz));
+    double py = D_ADD(D_ADD(D_MUL(b[3], qx), D_MUL(b[4], qy)), D_MUL(b[5], qz));
+    double n2 = D_SQRT(D_ADD(D_MUL(px, px), D_MUL(py, py)));
+    double d;
+    if (n2 < R) {
+        d = fabs(pz);
+    } else {
+        n2 = D_SUB(n2, R);
+        d = D_SQRT(D_ADD(D_MUL(n2, n2), D_MUL(pz, pz)));
+    }
+    if (d <= *cur) *cur = d;
+}
+
+// SDF of a ball's primitive in float64, reference order (shapes.go:100,
+// :270-317, :481-514, :746-781, :1451-1487).
+__device__ double ball_sdf_64(const BallD& b, P3 p) {
+    const double* c = b.c;
+    switch (b.kind) {
+        case LK_SPHERE: return D_SUB(c[3], dist3_64(p.x, p.y, p.z, c[0], c[1], c[2]));
+        case LK_RECT: {
+            if (!(p.x >= c[0] && p.y >= c[1] && p.z >= c[2] && p.x <= c[3] && p.y <= c[4] && p.z <= c[5])) {
+                // c.Min(MaxVal).Max(MinVal) with math.Min / math.Max
+                double nx = go_max_d(go_min_d(p.x, c[3]), c[0]), ny = go_max_d(go_min_d(p.y, c[4]), c[1]),
+                       nz = go_max_d(go_min_d(p.z, c[5]), c[2]);
+                return -dist3_64(p.x, p.y, p.z, nx, ny, nz);
+            }
+            double d = INFINITY;
+            double v[3] = {p.x, p.y, p.z};
+            for (int i = 0; i < 3; i++) {
+                double a = go_min_d(D_SUB(v[i], c[i]), D_SUB(c[3 + i], v[i]));
+                if (a < d) d = a;
+            }
+            return d;
+        }
+        case LK_CAPSULE:
+        case LK_CYLINDER: {
+            const double qx = D_SUB(p.x, c[0]), qy = D_SUB(p.y, c[1]), qz = D_SUB(p.z, c[2]);
+            const double dot = D_ADD(D_ADD(D_MUL(qx, c[6]), D_MUL(qy, c[7])), D_MUL(qz, c[8]));
+            const double nrm = c[9], R = c[10];
+            if (b.kind == LK_CAPSULE) {
+                if (dot < 0 || dot > nrm) {
+                    const double* e = dot < 0 ? c : c + 3;
+                    return D_SUB(R, dist3_64(p.x, p.y, p.z, e[0], e[1], e[2]));
+                }
+                return D_SUB(R, dist3_64(p.x, p.y, p.z, D_ADD(D_MUL(c[6], dot), c[0]),
+                                         D_ADD(D_MUL(c[7], dot), c[1]), D_ADD(D_MUL(c[8], dot), c[2])));
+            }
+            double cur = INFINITY;
+            bool contained = false;
+            if (dot >= 0 && dot < nrm) {
+                double sd = D_SUB(R, dist3_64(p.x, p.y, p.z, D_ADD(D_MUL(c[6], dot), c[0]),
+                                              D_ADD(D_MUL(c[7], dot), c[1]), D_ADD(D_MUL(c[8], dot), c[2])));
+                if (sd > 0) {
+                    contained = true;
+                    cur = sd;
+                } else {
+                    cur = -sd;
+                }
+            }
+            circle_dist_64(c + 11, qx, qy, qz, -dot, R, &cur);
+            const double rx = D_SUB(p.x, c[3]), ry = D_SUB(p.y, c[4]), rz = D_SUB(p.z, c[5]);
+            const double dot2 = D_ADD(D_ADD(D_MUL(c[6], rx), D_MUL(c[7], ry)), D_MUL(c[8], rz));
+            circle_dist_64(c + 17, rx, ry, rz, dot2, R, &cur);
+            return contained ? cur : -cur;
+        }
+        default: {  // torus
+            double cx = D_SUB(p.x, c[0]), cy = D_SUB(p.y, c[1]), cz = D_SUB(p.z, c[2]);
+            double x = D_ADD(D_ADD(D_MUL(c[3], cx), D_MUL(c[4], cy)), D_MUL(c[5], cz));
+            double y = D_ADD(D_ADD(D_MUL(c[6], cx), D_MUL(c[7], cy)), D_MUL(c[8], cz));
+            double on = D_SQRT(D_ADD(D_MUL(x, x), D_MUL(y, y)));
+            if (on == 0) {
+                x = 1;
+                y = 0;
+                on = 1;
+            }
+            double sc = D_DIV(c[9], on);
+            x = D_MUL(x, sc);
+            y = D_MUL(y, sc);
+            return D_SUB(c[10], dist3_64(D_ADD(D_MUL(c[3], x), D_MUL(c[6], y)), D_ADD(D_MUL(c[4], x), D_MUL(c[7], y)),
+                                         D_ADD(D_MUL(c[5], x), D_MUL(c[8], y)), cx, cy, cz));
+        }
+    }
+}
+
+// WeightedMetaballSolid.Contains in float64 (metaball.go:234-242).
+__device__ __noinline__ bool metaball_64(const ProgView& P, const double* ld, P3 p) {
+    const MetaD& m = P.metas[(int)ld[0]];
+    if (m.never) return false;
+    if (!(p.x >= m.lo[0] && p.y >= m.lo[1] && p.z >= m.lo[2] && p.x <= m.hi[0] && p.y <= m.hi[1] &&
+          p.z <= m.hi[2]))
+        return false;
+    double sum = 0;
+    for (int i = 0; i < m.n_balls; i++) {
+        const BallD& b = P.balls[m.first_ball + i];
+        const P3 q = b.n_steps ? apply_steps(P.xstep + b.first_step, b.n_steps, p) : p;
+        const double r = -ball_sdf_64(b, q);  // MetaballField
+        double t;
+        if (m.falloff == MC_FALLOFF_POWER) {
+            t = r <= 0 ? INFINITY : go_pow_neg(r, (int)m.param);
+        } else if (r < 0) {
+            t = INFINITY;
+        } else if (r >= m.param) {
+            t = 0;
+        } else {
+            double v = D_SUB(1.0, D_DIV(D_MUL(r, r), m.d2));
+            t = D_MUL(v, v);
+        }
+        sum = D_ADD(sum, D_MUL(b.w, t));
+    }
+    return sum > m.thr;
+}
+
+__device__ __forceinline__ float dist3_32(float x, float y, float z) { return __fsqrt_rn(x * x + y * y + z * z); }
+
+__device__ __forceinline__ void circle_dist_32(const float* b, float qx, float qy, float qz, float pz, float R,
+                                               float* cur) {
+    float px = b[0] * qx + b[1] * qy + b[2] * qz;
+    float py = b[3] * qx + b[4] * qy + b[5] * qz;
+    float n2 = __fsqrt_rn(px * px + py * py);
+    float d = n2 < R ? fabsf(pz) : __fsqrt_rn((n2 - R) * (n2 - R) + pz * pz);
+    *cur = fminf(*cur, d);
+}
+
+// -SDF of a ball in float.  Returns the absolute error bound of the value
+// against the float64 value, or +Inf when none is given (torus axis).
+__device__ float ball_field_32(int kind, const BallF& b, F3 q, float* out) {
+    const float* c = b.c;
+    float sdf, guard = 0.f;
+    switch (kind) {
+        case LK_SPHERE: sdf = c[3] - dist3_32(q.x - c[0], q.y - c[1], q.z - c[2]); break;
+        case LK_RECT: {
+            if (!(q.x >= c[0] && q.y >= c[1] && q.z >= c[2] && q.x <= c[3] && q.y <= c[4] && q.z <= c[5])) {
+                sdf = -dist3_32(q.x - fmaxf(fminf(q.x, c[3]), c[0]), q.y - fmaxf(fminf(q.y, c[4]), c[1]),
+                                q.z - fmaxf(fminf(q.z, c[5]), c[2]));
+            } else {
+                sdf = fminf(fminf(fminf(q.x - c[0], c[3] - q.x), fminf(q.y - c[1], c[4] - q.y)),
+                            fminf(q.z - c[2], c[5] - q.z));
+            }
+            break;
+        }
+        case LK_CAPSULE:
+        case LK_CYLINDER: {
+            const float qx = q.x - c[0], qy = q.y - c[1], qz = q.z - c[2];
+            const float dot = qx * c[6] + qy * c[7] + qz * c[8];
+            const float nrm = c[9], R = c[10];
+            const float t = fminf(fmaxf(dot, 0.f), nrm);
+            const float sd = R - dist3_32(qx - c[6] * t, qy - c[7] * t, qz - c[8] * t);
+            if (kind == LK_CAPSULE) {
+                sdf = sd;
+                break;
+            }
+            float cur = INFINITY;
+            bool contained = false;
+            if (dot >= 0.f && dot < nrm) {
+                contained = sd > 0.f;
+                cur = fabsf(sd);
+            }
+            circle_dist_32(c + 11, qx, qy, qz, -dot, R, &cur);
+            const float rx = q.x - c[3], ry = q.y - c[4], rz = q.z - c[5];
+            circle_dist_32(c + 17, rx, ry, rz, c[6] * rx + c[7] * ry + c[8] * rz, R, &cur);
+            sdf = contained ? cur : -cur;
+            break;
+        }
+        default: {  // torus
+            const float cx = q.x - c[0], cy = q.y - c[1], cz = q.z - c[2];
+            float x = c[3] * cx + c[4] * cy + c[5] * cz;
+            float y = c[6] * cx + c[7] * cy + c[8] * cz;
+            float on = __fsqrt_rn(x * x + y * y);
+            // Near the axis the ring point's direction is ill-determined;
+            // beyond outer/64 its error moves the distance by a bounded amount.
+            if (!(on >= fabsf(c[9]) * 0.015625f)) guard = INFINITY;
+            const float sc = c[9] / fmaxf(on, 1e-30f);
+            x *= sc;
+            y *= sc;
+            sdf = c[10] - dist3_32(c[3] * x + c[6] * y - cx, c[4] * x + c[7] * y - cy, c[5] * x + c[8] * y - cz);
+            break;
+        }
+    }
+    const float r = -sdf;
+    *out = r;
+    const float S = fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fabsf(q.z)) + b.mag;
+    return __fmul_ru(b.kerr, __fadd_ru(S, fabsf(r))) + guard;
+}
+
+__device__ __forceinline__ float powk_ru(float x, int k) {
+    float r = 1.f, b = x;
+    for (; k; k >>= 1) {
+        if (k & 1) r = __fmul_ru(r, b);
+        b = __fmul_ru(b, b);
+    }
+    return r;
+}
+__device__ __forceinline__ float powk_rd(float x, int k) {
+    float r = 1.f, b = x;
+    for (; k; k >>= 1) {
+        if (k & 1) r = __fmul_rd(r, b);
+        b = __fmul_rd(b, b);
+    }
+    return r;
+}
+
+// FP32 filter of metaball_64: 1/0 when decided, 2 otherwise.
+__device__ __noinline__ int metaball_32(const ProgView& P, const double* ld, P3 p, F3 pf) {
+    const int id = (int)ld[0];
+    const MetaD& md = P.metas[id];
+    const MetaF& m = P.metas_f[id];
+    if (md.never) return 0;
+    // InBounds: pf = fl(p) with fl monotone, so pf < fl_down(lo) implies p < lo.
+    if (pf.x < m.lo_dn[0] || pf.y < m.lo_dn[1] || pf.z < m.lo_dn[2] || pf.x > m.hi_up[0] || pf.y > m.hi_up[1] ||
+        pf.z > m.hi_up[2])
+        return 0;
+    if (!(pf.x > m.lo_up[0] && pf.y > m.lo_up[1] && pf.z > m.lo_up[2] && pf.x < m.hi_dn[0] && pf.y < m.hi_dn[1] &&
+          pf.z < m.hi_dn[2]) &&
+        !(p.x >= md.lo[0] && p.y >= md.lo[1] && p.z >= md.lo[2] && p.x <= md.hi[0] && p.y <= md.hi[1] &&
+          p.z <= md.hi[2]))
+        return 0;
+    const bool power = md.falloff == MC_FALLOFF_POWER;
+    float slo = 0.f, shi = 0.f, sabs = 0.f;
+    for (int i = 0; i < md.n_balls; i++) {
+        const BallD& bd = P.balls[md.first_ball + i];
+        const BallF& b = P.balls_f[md.first_ball + i];
+        const F3 q = bd.n_steps ? to_f3(apply_steps(P.xstep + bd.first_step, bd.n_steps, p)) : pf;
+        float r;
+        const float E = ball_field_32(bd.kind, b, q, &r);
+        const float rlo = __fsub_rd(r, E), rhi = __fadd_ru(r, E);
+        if (!(rlo == rlo) || !(rhi == rhi)) return 2;
+        float tlo, thi;  // bracket of f(r) for r in [rlo, rhi]
+        if (power) {
+            tlo = rhi <= 0.f ? INFINITY : __frcp_rd(powk_ru(rhi, m.k));
+            thi = rlo <= 0.f ? INFINITY : __frcp_ru(powk_rd(rlo, m.k));
+        } else {
+            if (rhi < 0.f) {
+                tlo = INFINITY;
+            } else if (rhi >= m.d_lo) {
+                tlo = 0.f;
+            } else {
+                const float v = fmaxf(__fsub_rd(1.f, __fdiv_ru(__fmul_ru(rhi, rhi), m.d2_lo)), 0.f);
+                tlo = __fmul_rd(v, v);
+            }
+            if (rlo < 0.f) {
+                thi = INFINITY;
+            } else if (rlo >= m.d_hi) {
+                thi = 0.f;
+            } else {
+                const float v = __fsub_ru(1.f, __fdiv_rd(__fmul_rd(rlo, rlo), m.d2_hi));
+                thi = __fmul_ru(v, v);
+            }
+        }
+        float lo, hi;
+        if (b.w_lo > 0.f) {
+            lo = __fmul_rd(b.w_lo, tlo);
+            hi = __fmul_ru(b.w_hi, thi);
+        } else if (b.w_hi < 0.f) {
+            lo = __fmul_rd(b.w_lo, thi);
+            hi = __fmul_ru(b.w_hi, tlo);
+        } else {  // weight 0 (or below the float range): 0 * Inf is NaN
+            if (thi == INFINITY) return 2;
+            lo = __fmul_rd(b.w_lo, thi);
+            hi = __fmul_ru(b.w_hi, thi);
+        }
+        slo = __fadd_rd(slo, lo);
+        shi = __fadd_ru(shi, hi);
+        const float wabs = fmaxf(fabsf(b.w_lo), fabsf(b.w_hi));
+        sabs = __fadd_ru(sabs, __fmul_ru(wabs, power ? thi : fmaxf(thi, 1.f)));
+    }
+    if (!(slo == slo) || !(shi == shi)) return 2;
+    if (slo == INFINITY) return 1;   // a certain +Inf term and no possible -Inf term
+    if (shi == -INFINITY) return 0;  // a certain -Inf term and no possible +Inf term
+    const float margin = __fmul_ru(sabs, 9.094947e-13f);  // 2^-40
+    if (__fsub_rd(slo, margin) > m.thr_hi) return 1;
+    if (__fadd_ru(shi, margin) <= m.thr_lo) return 0;
+    return 2;
+}
+
 // Float64 predicate of one leaf at one point (reference operation order).
 // Out of line: it is the rare path (escalations, tori, colliders) of the
 // filtered kernels, and keeping it out keeps their hot loops small.
+// In FP32 modes a metaball leaf tries its filter first (pf = fl(p) as
+// everywhere): metaball leaves share this call site with the escalations of
+// the other kinds.
+template <int MODE>
 __device__ __noinline__ bool leaf64_point(const ProgView& P, int id, P3 p, Counts& cnt, int* err) {
     const double* d = P.leaf_d + (size_t)id * LEAF_D;
-    switch (P.leaf_kind[id]) {
+    const int kind = P.leaf_kind[id];
+    if (mode_mb(MODE) && kind == LK_METABALL) {
+        if (mode_f32(MODE)) {
+            const int r = metaball_32(P, d, p, to_f3(p));
+            if (r != 2) return r;
+            cnt.esc++;
+        }
+        return metaball_64(P, d, p);
+    }
+    switch (kind) {
         case LK_SPHERE: return sphere_64(d, p);
         case LK_RECT: return rect_64(d, p);
         case LK_CYLINDER: return cylinder_64(d, p);
@@ -174,7 +541,7 @@ __device__ __noinline__ bool leaf64_point(const ProgView& P, int id, P3 p, Count
 template <int PREC>
 __device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf, Counts& cnt, int* err) {
     cnt.leaf++;
-    if (PREC == MC_PREC_FP32_FILTERED) {
+    if (mode_f32(PREC)) {
         const int kind = P.leaf_kind[id];
         if (kind <= LK_TORUS) {
             const float* f = P.leaf_f + (size_t)id * LEAF_F;
@@ -192,7 +559,7 @@ __device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf
             return collider_point(P, P.leaf_d + (size_t)id * LEAF_D, p, pf, true, cnt, err);
         }
     }
-    return leaf64_point(P, id, p, cnt, err);
+    return leaf64_point<PREC>(P, id, p, cnt, err);
 }
 
 // Evaluate a (possibly folded) postfix program at p.  Bit stack: top = bit 0.
@@ -496,13 +863,13 @@ __device__ __forceinline__ uint32_t leaf_rows(const ProgView& P, int id, const R
     const double* d = P.leaf_d + (size_t)id * LEAF_D;
     const float* f = P.leaf_f + (size_t)id * LEAF_F;
     cnt.leaf += rc.nrows;
-    constexpr bool f32 = PREC == MC_PREC_FP32_FILTERED;
+    constexpr bool f32 = mode_f32(PREC);
     switch (kind) {
         case LK_RECT: return rect_rows(d, rc);
         case LK_SPHERE: return f32 ? sphere_rows32(f, d, rc, cnt) : sphere_rows64(d, rc);
         case LK_CYLINDER: return f32 ? cylinder_rows32(f, d, rc, cnt) : cylinder_rows64(d, rc);
         case LK_CAPSULE: return f32 ? capsule_rows32(f, d, rc, cnt) : capsule_rows64(d, rc);
-        default: {  // torus, collider: point by point
+        default: {  // torus, collider, metaball: point by point
             uint32_t m = 0;
             for (int r = 0; r < rc.nrows; r++) {
                 const F3 pf{rc.pxf, shf(rc.ryf, r), shf(rc.rzf, r)};
@@ -510,11 +877,11 @@ __device__ __forceinline__ uint32_t leaf_rows(const ProgView& P, int id, const R
                 int v = 2;
                 if (f32 && kind == LK_COLLIDER) {
                     v = collider_point(P, d, p, pf, true, cnt, err) ? 1 : 0;
-                } else if (f32) {
+                } else if (f32 && kind == LK_TORUS) {
                     v = torus_32(f, pf);
                     if (v == 2) cnt.esc++;
                 }
-                if (v == 2) v = leaf64_point(P, id, p, cnt, err) ? 1 : 0;
+                if (v == 2) v = leaf64_point<PREC>(P, id, p, cnt, err) ? 1 : 0;
                 m |= (uint32_t)v << r;
             }
             return m;
@@ -1788,6 +2155,7 @@ struct BatchPlan {
     std::vector<long long> hchunk_offs;
     long long nitems = 0, nchunks = 0;
     int nblk = 0, fold_words = 0, grid_c = 1, grid_s = 1, prec = 1;
+    bool has_metaball = false;
     size_t smem_c = 0, smem_s = 0;
     long long cap_V = -1, cap_T = -1;
     cudaGraphExec_t exec = nullptr;
@@ -2017,6 +2385,10 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
         {H.cull_f.data(), H.cull_f.size() * 4, 0},
         {H.cell_start.data(), H.cell_start.size() * 4, 0},
         {H.ents.data(), H.ents.size() * sizeof(RayEnt), 0},
+        {H.metas.data(), H.metas.size() * sizeof(MetaD), 0},
+        {H.metas_f.data(), H.metas_f.size() * sizeof(MetaF), 0},
+        {H.balls.data(), H.balls.size() * sizeof(BallD), 0},
+        {H.balls_f.data(), H.balls_f.size() * sizeof(BallF), 0},
     };
     size_t total = 0;
     for (auto& p : pcs) {
@@ -2060,11 +2432,16 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
     v.cull_f = (const float*)(b + pcs[14].off);
     v.cell_start = (const int32_t*)(b + pcs[15].off);
     v.ents = (const RayEnt*)(b + pcs[16].off);
+    v.metas = (const MetaD*)(b + pcs[17].off);
+    v.metas_f = (const MetaF*)(b + pcs[18].off);
+    v.balls = (const BallD*)(b + pcs[19].off);
+    v.balls_f = (const BallF*)(b + pcs[20].off);
     v.n_ops = (int32_t)H.ops.size();
     v.n_ops_allfalse = H.n_ops_allfalse;
     v.n_leaves = (int32_t)H.leaf_kind.size();
     v.n_xbox = (int32_t)H.xbox.size();
     v.rows_ok = H.has_transform ? 0 : 1;
+    v.has_metaball = H.metas.empty() ? 0 : 1;
     v.fold_cap = H.fold_cap;
     {
         std::lock_guard<std::mutex> lk(ctx->pool_mu);
@@ -2200,7 +2577,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     long long ntiles = (long long)ca.ntx * ca.nty * ca.ntz;
     st.tiles = ntiles;
     const size_t smem_c = classify_smem(P);
-    auto kc = opts.precision == MC_PREC_FP64 ? k_classify<MC_PREC_FP64> : k_classify<MC_PREC_FP32_FILTERED>;
+    auto kc = MC_PICK(k_classify, opts.precision, P.has_metaball);
     if (smem_c > 48 * 1024) CK(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kc, 256, smem_c));
@@ -2269,7 +2646,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
             sa.interior = ctx->inner.as<double>();
         }
         size_t smem_s = search_smem(P);
-        auto ks = opts.precision == MC_PREC_FP64 ? k_search<MC_PREC_FP64> : k_search<MC_PREC_FP32_FILTERED>;
+        auto ks = MC_PICK(k_search, opts.precision, P.has_metaball);
         if (smem_s > 48 * 1024)
             CK(cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s));
         int grid_s = (int)std::min<long long>((V + 127) / 128, (long long)ctx->sm_count * 16);
@@ -2555,7 +2932,7 @@ mc_status mc_contains(mc_ctx* ctx, const mc_solid* solid, const double* points, 
     CK(cudaMemsetAsync(ctx->stats.p, 0, ST_N * 8, ctx->stream));
     CK(cudaMemcpyAsync(ctx->pts.p, points, n * 24, cudaMemcpyHostToDevice, ctx->stream));
     int grid = (int)std::min<long long>((n + 255) / 256, (long long)ctx->sm_count * 16);
-    auto kk = opts.precision == MC_PREC_FP64 ? k_contains<MC_PREC_FP64> : k_contains<MC_PREC_FP32_FILTERED>;
+    auto kk = MC_PICK(k_contains, opts.precision, solid->view.has_metaball);
     kk<<<grid, 256, 0, ctx->stream>>>(solid->view, ctx->pts.as<double>(), n, ctx->pout.as<uint8_t>(),
                                       ctx->errs.as<int>(), ctx->stats.as<unsigned long long>());
     CK(cudaGetLastError());
@@ -2732,6 +3109,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             const int nw = (J.P.n_leaves + 31) / 32;
             fold_words = std::max(fold_words, (J.P.fold_cap + 2 * nw + 3) & ~3);
             lay.push_back(L);
+            pl->has_metaball = pl->has_metaball || J.P.has_metaball;
             pl->hjobs.push_back(J);
         }
         const int nd = (int)pl->hjobs.size();
@@ -2800,8 +3178,8 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         CK(cudaStreamSynchronize(sm));  // host vectors die at scope end
         pl->smem_c = (size_t)8 * fold_words * 4;
         pl->smem_s = (size_t)4 * fold_words * 4;
-        auto kcb = pl->prec == MC_PREC_FP64 ? k_classify_batch<MC_PREC_FP64> : k_classify_batch<MC_PREC_FP32_FILTERED>;
-        auto ksb = pl->prec == MC_PREC_FP64 ? k_search_batch<MC_PREC_FP64> : k_search_batch<MC_PREC_FP32_FILTERED>;
+        auto kcb = MC_PICK(k_classify_batch, pl->prec, pl->has_metaball);
+        auto ksb = MC_PICK(k_search_batch, pl->prec, pl->has_metaball);
         if (pl->smem_c > 48 * 1024) CK(cudaFuncSetAttribute(kcb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl->smem_c));
         if (pl->smem_s > 48 * 1024) CK(cudaFuncSetAttribute(ksb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl->smem_s));
         int occ = 1;
@@ -2825,8 +3203,8 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
     ba.stats = pl->stats.as<unsigned long long>();
     ba.fold_words = pl->fold_words;
     ba.cull = opts.cull;
-    auto kcb = pl->prec == MC_PREC_FP64 ? k_classify_batch<MC_PREC_FP64> : k_classify_batch<MC_PREC_FP32_FILTERED>;
-    auto ksb = pl->prec == MC_PREC_FP64 ? k_search_batch<MC_PREC_FP64> : k_search_batch<MC_PREC_FP32_FILTERED>;
+    auto kcb = MC_PICK(k_classify_batch, pl->prec, pl->has_metaball);
+    auto ksb = MC_PICK(k_search_batch, pl->prec, pl->has_metaball);
     auto front = [&]() -> cudaError_t {
         cudaMemsetAsync(pl->stats.p, 0, ST_N * 8, sm);
         cudaMemsetAsync(pl->errs.p, 0, std::max(nd, 1) * ER_N * 4, sm);
@@ -3074,6 +3452,10 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         {Z.data(), Z.size() * 8, nullptr},                 {H.cull_f.data(), H.cull_f.size() * 4, nullptr},
         {XF.data(), XF.size() * 4, nullptr},               {YF.data(), YF.size() * 4, nullptr},
         {ZF.data(), ZF.size() * 4, nullptr},
+        {H.metas.data(), H.metas.size() * sizeof(MetaD), nullptr},
+        {H.metas_f.data(), H.metas_f.size() * sizeof(MetaF), nullptr},
+        {H.balls.data(), H.balls.size() * sizeof(BallD), nullptr},
+        {H.balls_f.data(), H.balls_f.size() * sizeof(BallF), nullptr},
     };
     for (auto& p : up) p.dst = cv.take(p.bytes);
     int* errs = (int*)cv.take(ER_N * 4);
@@ -3125,11 +3507,16 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     P.xbox = (const XBoxD*)up[6].dst;
     P.xstep = (const XStepD*)up[7].dst;
     P.cull_f = (const float*)up[11].dst;
+    P.metas = (const MetaD*)up[15].dst;
+    P.metas_f = (const MetaF*)up[16].dst;
+    P.balls = (const BallD*)up[17].dst;
+    P.balls_f = (const BallF*)up[18].dst;
     P.n_ops = (int32_t)H.ops.size();
     P.n_ops_allfalse = H.n_ops_allfalse;
     P.n_leaves = (int32_t)H.leaf_kind.size();
     P.n_xbox = (int32_t)H.xbox.size();
     P.rows_ok = H.has_transform ? 0 : 1;
+    P.has_metaball = H.metas.empty() ? 0 : 1;
     P.fold_cap = H.fold_cap;
 
     int sms = 152;
@@ -3152,7 +3539,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     const size_t smem_c = classify_smem(P);
     if (smem_c > 48 * 1024) return MC_ERR_LIMIT;
     long long items = (long long)ca.nty * ca.ntz;
-    auto kc = opts.precision == MC_PREC_FP64 ? k_classify<MC_PREC_FP64> : k_classify<MC_PREC_FP32_FILTERED>;
+    auto kc = MC_PICK(k_classify, opts.precision, P.has_metaball);
     kc<<<(int)std::max<long long>(1, std::min<long long>((items + 7) / 8, (long long)sms * 4)), 256, smem_c, sm>>>(
         g, P, ca);
     if (nchunks > 0) {
@@ -3191,7 +3578,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         sa.err = errs;
         sa.stats = stats;
         if (search_smem(P) > 48 * 1024) return MC_ERR_LIMIT;
-        auto ks = opts.precision == MC_PREC_FP64 ? k_search<MC_PREC_FP64> : k_search<MC_PREC_FP32_FILTERED>;
+        auto ks = MC_PICK(k_search, opts.precision, P.has_metaball);
         ks<<<(int)std::min<long long>((V + 127) / 128, (long long)sms * 16), 128, search_smem(P), sm>>>(g, P, sa);
     }
     if (cudaGetLastError() != cudaSuccess) return MC_ERR_CUDA;

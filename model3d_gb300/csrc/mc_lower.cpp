@@ -108,6 +108,31 @@ void ortho_basis(D3 c, D3* o1, D3* o2) {
     *o2 = vnormalize(b2);
 }
 
+// math.Ldexp (Go math/ldexp.go): exact for normal results; a subnormal
+// result is scaled into range and multiplied by 2^-53 (one rounding).
+double go_ldexp(double frac, long exp) {
+    if (frac == 0 || std::isinf(frac) || std::isnan(frac)) return frac;
+    if (std::fabs(frac) < DBL_MIN) {  // normalize
+        frac *= 4503599627370496.0;
+        exp -= 52;
+    }
+    uint64_t x;
+    std::memcpy(&x, &frac, 8);
+    exp += (long)((x >> 52) & 0x7ff) - 1023;
+    if (exp < -1075) return std::copysign(0.0, frac);
+    if (exp > 1023) return frac < 0 ? -HUGE_VAL : HUGE_VAL;
+    double m = 1;
+    if (exp < -1022) {
+        exp += 53;
+        m = 1.0 / 9007199254740992.0;
+    }
+    x &= ~(0x7ffull << 52);
+    x |= (uint64_t)(exp + 1023) << 52;
+    double f;
+    std::memcpy(&f, &x, 8);
+    return m * f;
+}
+
 // Matrix3 inverse (model3d/matrix.go:56-92).
 void inverse3(const double* m, double* r) {
     double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
@@ -387,6 +412,48 @@ void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, in
     tree->gb = gb;
 }
 
+}  // namespace
+
+// math.Pow(x, y) for integer y (Go math/pow.go): special cases for x = 1,
+// NaN and +Inf, then x = x1 * 2^xe by Frexp, the product of x1 powers over
+// the bits of |y| by repeated squaring renormalised to [0.5, 1), one
+// reciprocal for y < 0, and Ldexp.
+double go_pow_int(double x, long y) {
+    if (y == 0 || x == 1) return 1;
+    if (y == 1) return x;
+    if (std::isnan(x)) return x;
+    if (std::isinf(x) && x > 0) return y < 0 ? 0.0 : HUGE_VAL;
+    if (!(x > 0)) throw LowerError(MC_ERR_BAD_PROGRAM, "go_pow_int: x must be positive");
+    double a1 = 1;
+    long ae = 0;
+    int xe_i;
+    double x1 = std::frexp(x, &xe_i);
+    long xe = xe_i;
+    for (long i = y < 0 ? -y : y; i != 0; i >>= 1) {
+        if (xe < -(1 << 12) || (1 << 12) < xe) {
+            ae += xe;
+            break;
+        }
+        if (i & 1) {
+            a1 *= x1;
+            ae += xe;
+        }
+        x1 *= x1;
+        xe <<= 1;
+        if (x1 < .5) {
+            x1 += x1;
+            xe--;
+        }
+    }
+    if (y < 0) {
+        a1 = 1 / a1;
+        ae = -ae;
+    }
+    return go_ldexp(a1, ae);
+}
+
+namespace {
+
 // ---------------------------------------------------------------- lowering
 
 struct Lowerer {
@@ -431,6 +498,163 @@ struct Lowerer {
             P->cull_f.push_back(i < 3 ? f_down(cull[i]) : f_up(cull[i]));
         }
         return id;
+    }
+
+    // WeightedMetaballSolid: one LK_METABALL leaf over the ball records.
+    template <class SetCull>
+    void lower_metaball(const mc_node& nd, SetCull& set_cull, double* cull) {
+        if (nd.n_children < 0) fail("negative ball count");
+        if (nd.n_children > MAX_BALLS) throw LowerError(MC_ERR_LIMIT, "more than 4096 metaballs");
+        const int falloff = (int)nd.p[1];
+        const double param = nd.p[2];
+        if (falloff == MC_FALLOFF_POWER) {
+            if (!(param >= 1 && param < (1 << 20)) || param != std::floor(param))
+                throw LowerError(MC_ERR_NOT_LOWERABLE, "falloff power must be an integer in [1, 2^20)");
+        } else if (falloff == MC_FALLOFF_WYVILL) {
+            if (!(param > 0)) fail("WyvillMetaballFalloffFunc needs d > 0");
+        } else {
+            throw LowerError(MC_ERR_NOT_LOWERABLE, "metaball falloff has no device lowering");
+        }
+        MetaD md{};
+        MetaF mf{};
+        md.falloff = falloff;
+        md.param = param;
+        md.d2 = param * param;
+        // threshold := f(radiusThreshold) (metaball.go:180)
+        const double rt = nd.p[0];
+        double thr;
+        if (falloff == MC_FALLOFF_POWER) {
+            thr = rt <= 0 ? HUGE_VAL : go_pow_int(rt, -(long)param);
+        } else if (rt < 0) {
+            thr = HUGE_VAL;
+        } else if (rt >= param) {
+            thr = 0;
+        } else {
+            double ratio2 = (rt * rt) / md.d2;
+            double value = 1 - ratio2;
+            thr = value * value;
+        }
+        md.thr = thr;
+        md.never = thr < HUGE_VAL ? 0 : 1;  // +Inf or NaN
+        for (int i = 0; i < 3; i++) {
+            md.lo[i] = nd.min[i];
+            md.hi[i] = nd.max[i];
+            mf.lo_dn[i] = f_down(nd.min[i]);
+            mf.lo_up[i] = f_up(nd.min[i]);
+            mf.hi_dn[i] = f_down(nd.max[i]);
+            mf.hi_up[i] = f_up(nd.max[i]);
+        }
+        mf.thr_lo = f_down(thr);
+        mf.thr_hi = f_up(thr);
+        mf.d_lo = f_down(param);
+        mf.d_hi = f_up(param);
+        mf.d2_lo = f_down(md.d2);
+        mf.d2_hi = f_up(md.d2);
+        mf.k = falloff == MC_FALLOFF_POWER ? (int32_t)param : 0;
+        md.first_ball = (int32_t)P->balls.size();
+        md.n_balls = nd.n_children;
+        bool any_pos = false;
+        for (int i = 0; i < nd.n_children; i++) {
+            if (pos >= n || nodes[pos].kind != MC_NODE_BALL) fail("metaball child is not a MC_NODE_BALL");
+            const mc_node& bn = nodes[pos++];
+            if (bn.n_children != 1) fail("MC_NODE_BALL needs one primitive child");
+            const int ns = std::max(bn.n_steps, 0);
+            if (pos + (size_t)ns > n) fail("truncated ball transform steps");
+            const std::vector<XStepD> inv = transform_steps(nodes + pos, ns, true);
+            pos += ns;
+            if (pos >= n) fail("truncated ball");
+            const mc_node& pr = nodes[pos++];
+            BallD bd{};
+            BallF bf{};
+            bd.w = bn.p[0];
+            any_pos = any_pos || bd.w > 0;
+            bd.first_step = (int32_t)P->xstep.size();
+            bd.n_steps = (int32_t)inv.size();
+            P->xstep.insert(P->xstep.end(), inv.begin(), inv.end());
+            auto pp = [&](int o) { return d3(pr.p[o], pr.p[o + 1], pr.p[o + 2]); };
+            auto put = [&](int o, D3 v) {
+                for (int k = 0; k < 3; k++) bd.c[o + k] = v.v[k];
+            };
+            int K = 16, nc = 0;
+            switch (pr.kind) {
+                case MC_NODE_SPHERE:
+                    put(0, pp(0));
+                    bd.c[3] = pr.p[3];
+                    nc = 4;
+                    break;
+                case MC_NODE_RECT:
+                    put(0, pp(0));
+                    put(3, pp(3));
+                    nc = 6;
+                    break;
+                case MC_NODE_CAPSULE:
+                case MC_NODE_CYLINDER: {  // shapes.go:481-484, :747-749
+                    D3 p1 = pp(0), p2 = pp(3);
+                    D3 v = vsub(p2, p1);
+                    double nrm = vnorm(v);
+                    D3 axis = vscale(v, 1 / nrm);
+                    put(0, p1);
+                    put(3, p2);
+                    put(6, axis);
+                    bd.c[9] = nrm;
+                    bd.c[10] = pr.p[6];
+                    nc = 11;
+                    K = 64;
+                    if (pr.kind == MC_NODE_CYLINDER) {  // filledCircleDist bases, shapes.go:775-776
+                        D3 b1, b2;
+                        ortho_basis(vscale(axis, -1), &b1, &b2);
+                        put(11, b1);
+                        put(14, b2);
+                        ortho_basis(axis, &b1, &b2);
+                        put(17, b1);
+                        put(20, b2);
+                        nc = 23;
+                        K = 96;
+                    }
+                    break;
+                }
+                case MC_NODE_TORUS: {  // shapes.go:1451-1487
+                    D3 b1, b2;
+                    ortho_basis(pp(3), &b1, &b2);
+                    put(0, pp(0));
+                    put(3, b1);
+                    put(6, b2);
+                    bd.c[9] = pr.p[6];
+                    bd.c[10] = pr.p[7];
+                    nc = 11;
+                    K = 128;
+                    break;
+                }
+                default: fail("a ball's primitive must be a sphere, rect, cylinder, capsule or torus");
+            }
+            bd.kind = pr.kind;
+            double mag = 0;
+            for (int k = 0; k < nc; k++) {
+                bf.c[k] = (float)bd.c[k];
+                mag = std::max(mag, std::fabs(bd.c[k]));
+            }
+            bf.mag = f_up(mag);
+            bf.kerr = (float)K * 5.9604645e-08f;
+            bf.w_lo = f_down(bd.w);
+            bf.w_hi = f_up(bd.w);
+            P->balls.push_back(bd);
+            P->balls_f.push_back(bf);
+        }
+        if (!any_pos) {  // NewRect(Origin, Origin) (metaball.go:186-188)
+            P->balls.resize(md.first_ball);
+            P->balls_f.resize(md.first_ball);
+            double d[6] = {0, 0, 0, 0, 0, 0};
+            float f[6] = {0, 0, 0, 0, 0, 0};
+            set_cull(d3(0, 0, 0), d3(0, 0, 0));
+            leaf_out(add_leaf(LK_RECT, d, 6, f, 6, cull));
+            return;
+        }
+        double d[1] = {(double)P->metas.size()};
+        float f[1] = {0};
+        P->metas.push_back(md);
+        P->metas_f.push_back(mf);
+        set_cull(d3(nd.min[0], nd.min[1], nd.min[2]), d3(nd.max[0], nd.max[1], nd.max[2]));
+        leaf_out(add_leaf(LK_METABALL, d, 1, f, 1, cull));
     }
 
     int lower_collider(int set) {
@@ -542,13 +766,16 @@ struct Lowerer {
     size_t subtree_end(size_t p) {
         if (p >= n) fail("truncated node array");
         const mc_node& nd = nodes[p];
-        size_t q = p + 1 + (nd.kind == MC_NODE_TRANSFORM ? (size_t)std::max(0, nd.n_steps) : 0);
-        int nc = (nd.kind >= MC_NODE_JOIN && nd.kind <= MC_NODE_CHECKED) ? nd.n_children : 0;
+        size_t q = p + 1 + ((nd.kind == MC_NODE_TRANSFORM || nd.kind == MC_NODE_BALL)
+                                ? (size_t)std::max(0, nd.n_steps) : 0);
+        int nc = (nd.kind >= MC_NODE_JOIN && nd.kind <= MC_NODE_CHECKED) || nd.kind == MC_NODE_METABALL ||
+                         nd.kind == MC_NODE_BALL
+                     ? nd.n_children : 0;
         if (nc < 0) fail("negative child count");
         for (int i = 0; i < nc; i++) q = subtree_end(q);
         return q;
     }
-    static bool is_leaf_kind(int k) { return k >= MC_NODE_SPHERE && k <= MC_NODE_COLLIDER; }
+    static bool is_leaf_kind(int k) { return k >= MC_NODE_SPHERE && k <= MC_NODE_METABALL; }
 
     int last_leaf = -1;
     bool emit_leaves = true;
@@ -661,6 +888,10 @@ struct Lowerer {
                 int id = add_leaf(LK_COLLIDER, d, 7, f, 1, cull);
                 P->has_collider = true;
                 leaf_out(id);
+                return;
+            }
+            case MC_NODE_METABALL: {  // metaball.go:165-242
+                lower_metaball(nd, set_cull, cull);
                 return;
             }
             case MC_NODE_JOIN:

@@ -36,6 +36,10 @@ struct HostProgram {
     std::vector<RayEnt> ents;
     std::vector<TriD> tris;
     std::vector<TriF> tris_f;
+    std::vector<MetaD> metas;
+    std::vector<MetaF> metas_f;
+    std::vector<BallD> balls;
+    std::vector<BallF> balls_f;
     double root_min[3] = {0, 0, 0}, root_max[3] = {0, 0, 0};
     int max_stack = 0, max_xdepth = 0;
     bool has_collider = false;
@@ -49,6 +53,9 @@ void lower_scene(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets, s
 // Apply records of JoinedTransform(steps) (MC_XF_* records), or of its
 // Inverse() when inverse is set; throws LowerError on a bad step kind.
 std::vector<XStepD> transform_steps(const mc_node* steps, size_t n, bool inverse);
+
+// math.Pow(x, y) for integer y, 0 < |y| < 2^20, x > 0 finite (Go math/pow.go).
+double go_pow_int(double x, long y);
 
 // newSquareSpacer for one axis; MC_OK or MC_ERR_GRID.
 int spacer_axis(double lo, double hi, double delta, std::vector<double>* out, int64_t limit);

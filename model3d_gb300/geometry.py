@@ -93,6 +93,15 @@ class Coord3D:
     def Sum(self) -> float:
         return self.X + self.Y + self.Z
 
+    def Abs(self) -> "Coord3D":
+        return Coord3D(abs(self.X), abs(self.Y), abs(self.Z))
+
+    def MaxCoord(self) -> float:
+        """model3d/coords.go:357-371 (NaN and ties follow its comparisons)."""
+        if self.X > self.Y:
+            return self.X if self.X > self.Z else self.Z
+        return self.Y if self.Y > self.Z else self.Z
+
     def ProjectOut(self, c1: "Coord3D") -> "Coord3D":
         normed = c1.Normalize()
         return self.Sub(normed.Scale(normed.Dot(self)))

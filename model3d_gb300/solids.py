@@ -19,7 +19,7 @@ import numpy as np
 from .geometry import Coord3D, Matrix3, XYZ, go_max, go_min, NewMatrix3Rotation
 
 # Node kinds (include/mcgpu.h).
-SPHERE, RECT, CYLINDER, CAPSULE, TORUS, COLLIDER = 1, 2, 3, 4, 5, 6
+SPHERE, RECT, CYLINDER, CAPSULE, TORUS, COLLIDER, METABALL, BALL = 1, 2, 3, 4, 5, 6, 7, 8
 JOIN, SUBTRACT, INTERSECT, TRANSFORM, CHECKED = 16, 17, 18, 19, 20
 XF_TRANSLATE, XF_SCALE, XF_VECSCALE, XF_MATRIX = 32, 33, 34, 35
 
@@ -293,8 +293,14 @@ class JoinedTransform(Transform):
         return out
 
 
+class OrthoMatrix3Transform(Matrix3Transform):
+    """orthoMatrix3Transform: a distance-preserving Matrix3Transform
+    (model3d/transform.go:159-190)."""
+
+
 def Rotation(axis: Coord3D, theta: float) -> Matrix3Transform:
-    return Matrix3Transform(NewMatrix3Rotation(axis, theta))
+    """model3d/transform.go:165-172."""
+    return OrthoMatrix3Transform(NewMatrix3Rotation(axis, theta))
 
 
 class _TransformedSolid(Solid):
@@ -491,13 +497,15 @@ def serialize(solid: Solid):
 
     Min()/Max() are computed for the nodes whose bounds the library reads:
     the root, colliders, transforms and checked solids."""
+    from .metaballs import FALLOFF_POWER, MAX_POWER, MetaballSolidT, ball_steps
+
     recs = []
     sets: List[MeshCollider] = []
     set_ids = {}
     zero3 = (0.0, 0.0, 0.0)
 
     def node(kind, s=None, n_children=0, n_steps=0, mesh=0, p=()):
-        if s is not None and (not recs or kind in (COLLIDER, TRANSFORM, CHECKED)):
+        if s is not None and (not recs or kind in (COLLIDER, TRANSFORM, CHECKED, METABALL)):
             mn, mx = tuple(s.Min().Array()), tuple(s.Max().Array())
         else:
             mn = mx = zero3
@@ -542,6 +550,18 @@ def serialize(solid: Solid):
         elif isinstance(s, _CheckedSolid):
             node(CHECKED, s, n_children=1)
             emit(s.solid)
+        elif isinstance(s, MetaballSolidT):
+            f = s.falloff
+            if f.kind == 0 or (f.kind == FALLOFF_POWER and
+                               (f.param != int(f.param) or f.param >= MAX_POWER)):
+                raise NotLowerable("this falloff has no device lowering")
+            node(METABALL, s, n_children=len(s.balls), p=[s.radiusThreshold, f.kind, f.param])
+            for mb, w in zip(s.balls, s.weights):
+                steps, prim = ball_steps(mb)
+                node(BALL, None, n_children=1, n_steps=len(steps), p=[w])
+                for kind, p in steps:
+                    node(kind, None, p=p)
+                emit(prim)
         else:
             raise NotLowerable(f"{type(s).__name__} has no device lowering")
 

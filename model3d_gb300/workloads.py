@@ -11,6 +11,10 @@ stream with a fixed seed, so the oracle and the GPU see identical bytes.
                            triangles), projected to the unit sphere and
                            displaced radially by r = 1 + 0.15 * mean of 8
                            sinusoids sin(f_k * (u_k . p) + phi_k), f_k in 1..6.
+  metaball_blob(seed, n)   MetaballSolid of n balls, 3/4 spheres and 1/4
+                           capsules: centres U[-0.7,0.7]^3, radii U[0.05,0.2],
+                           capsule half-lengths U[0.05,0.25] along random unit
+                           axes; quartic falloff, radiusThreshold 0.1.
 """
 from __future__ import annotations
 
@@ -21,6 +25,7 @@ import numpy as np
 
 from .geometry import XYZ, Coord3D
 from .solids import (Capsule, Cylinder, JoinedSolid, Rect, Sphere, Solid, SubtractedSolid)
+from .metaballs import MetaballSolid
 
 _M64 = (1 << 64) - 1
 
@@ -110,6 +115,22 @@ def collider_batch(seed: int, count: int = 64, tri_lo: int = 20000, tri_hi: int 
         side = int(round(rng.log_uniform(grid_lo, grid_hi)))
         out.append((displaced_icosphere(n, mesh_seed), mesh_seed, side))
     return out
+
+
+def metaball_blob(seed: int, n: int = 64, falloff=None, radius_threshold: float = 0.1) -> Solid:
+    """MetaballSolid(falloff, radius_threshold, n balls) (falloff None: quartic)."""
+    rng = SplitMix64(seed)
+    balls = []
+    for _ in range(n):
+        c = XYZ(rng.uniform(-0.7, 0.7), rng.uniform(-0.7, 0.7), rng.uniform(-0.7, 0.7))
+        r = rng.uniform(0.05, 0.2)
+        if rng.next_u64() % 4 == 0:
+            axis = rng.unit_vector()
+            half = rng.uniform(0.05, 0.25)
+            balls.append(Capsule(c.Add(axis.Scale(half)), c.Sub(axis.Scale(half)), r))
+        else:
+            balls.append(Sphere(c, r))
+    return MetaballSolid(falloff, radius_threshold, *balls)
 
 
 def icosphere_triangles(n: int) -> np.ndarray:

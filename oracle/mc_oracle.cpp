@@ -171,6 +171,8 @@ struct Solid {
     virtual V3 Min() const = 0;
     virtual V3 Max() const = 0;
     virtual bool Contains(V3 c) const = 0;
+    // SDF (negative outside), for the primitives that are metaballs.
+    virtual double SDF(V3) const { throw std::runtime_error("not a metaball primitive"); }
 };
 
 // Sphere (model3d/shapes.go:13-31).
@@ -183,6 +185,7 @@ struct Sphere : Solid {
         tl_leaf++;
         return dist(c, center) <= radius;
     }
+    double SDF(V3 c) const override { return radius - dist(c, center); }  // shapes.go:100-102
 };
 
 // Rect (model3d/shapes.go:145-173).
@@ -193,6 +196,15 @@ struct RectS : Solid {
     bool Contains(V3 c) const override {
         tl_leaf++;
         return veq(vmin(c, mn), mn) && veq(vmax(c, mx), mx);
+    }
+    double SDF(V3 c) const override {  // genericSDF, shapes.go:270-317
+        if (!(veq(vmin(c, mn), mn) && veq(vmax(c, mx), mx))) return -dist(c, vmax(vmin(c, mx), mn));
+        double d = std::numeric_limits<double>::infinity();
+        for (int i = 0; i < 3; i++) {
+            double axisD = go_min(at(c, i) - at(mn, i), at(mx, i) - at(c, i));
+            if (axisD < d) d = axisD;
+        }
+        return d;
     }
 };
 
@@ -225,6 +237,7 @@ struct Cylinder : Solid {
         V3 projection = add(p2, scale(direction, frac));
         return dist(projection, p) <= radius;
     }
+    double SDF(V3 c) const override;
 };
 
 // Segment (model3d/primitives.go:543-594).
@@ -259,7 +272,56 @@ struct Capsule : Solid {
         Segment seg = new_segment(p1, p2);
         return dist(c, segment_closest(seg, c)) <= radius;
     }
+    double SDF(V3 c) const override {  // genericSDF, shapes.go:481-514
+        V3 v = sub(p2, p1);
+        double nrm = norm(v);
+        V3 axis = scale(v, 1 / nrm);
+        double d = dot(sub(c, p1), axis);
+        if (d < 0 || d > nrm) return radius - dist(c, d < 0 ? p1 : p2);  // proxy Sphere.SDF
+        return radius - dist(c, segment_closest(Segment{p1, p2}, c));   // Segment{P1, P2}.Dist
+    }
 };
+
+// filledCircleDist (model3d/shapes.go:783-812) without the normal/point outputs.
+void filled_circle_dist(V3 c, V3 center, V3 axis, double radius, double* cur) {
+    V3 b1, b2;
+    ortho_basis(axis, &b1, &b2);
+    M3 mat;  // NewMatrix3Columns(b1, b2, axis).Transpose(): rows b1, b2, axis
+    double rows[9] = {b1.x, b1.y, b1.z, b2.x, b2.y, b2.z, axis.x, axis.y, axis.z};
+    for (int i = 0; i < 9; i++) mat.m[i] = rows[i];
+    V3 proj = mul_column(mat, sub(c, center));
+    double norm2 = std::sqrt(proj.x * proj.x + proj.y * proj.y);  // proj.XY().Norm()
+    if (norm2 < radius) {
+        double d = std::fabs(proj.z);
+        if (d <= *cur) *cur = d;
+    } else {
+        norm2 -= radius;
+        double d = std::sqrt(norm2 * norm2 + proj.z * proj.z);
+        if (d <= *cur) *cur = d;
+    }
+}
+
+// Cylinder.genericSDF (model3d/shapes.go:746-781).
+double Cylinder::SDF(V3 c) const {
+    V3 axis = sub(p2, p1);
+    double nrm = norm(axis);
+    axis = scale(axis, 1 / nrm);
+    double d_ = std::numeric_limits<double>::infinity();
+    bool contained = false;
+    double d = dot(axis, sub(c, p1));
+    if (d >= 0 && d < nrm) {
+        double sd = radius - dist(c, segment_closest(Segment{p1, p2}, c));
+        if (sd > 0) {
+            contained = true;
+            d_ = sd;
+        } else {
+            d_ = -sd;
+        }
+    }
+    filled_circle_dist(c, p1, scale(axis, -1), radius, &d_);
+    filled_circle_dist(c, p2, axis, radius, &d_);
+    return contained ? d_ : -d_;
+}
 
 // Torus (model3d/shapes.go:1323-1365, genericSDF :1451-1487).
 struct Torus : Solid {
@@ -279,7 +341,7 @@ struct Torus : Solid {
                        outer);
         return add(add(off, center), extra);
     }
-    double SDF(V3 c) const {
+    double SDF(V3 c) const override {
         V3 b1, b2;
         ortho_basis(axis, &b1, &b2);
         V3 centered = sub(c, center);
@@ -450,6 +512,180 @@ struct Checked : Solid {
     V3 Max() const override { return mx; }
     bool Contains(V3 c) const override {
         return veq(vmin(c, mn), mn) && veq(vmax(c, mx), mx) && child->Contains(c);
+    }
+};
+
+// --------------------------------------------------------------- metaballs
+
+// math.Ldexp (Go math/ldexp.go): normal results exact; a subnormal result is
+// scaled into range and multiplied by 2^-53 (one rounding).
+double go_ldexp(double frac, long exp) {
+    if (frac == 0 || std::isinf(frac) || std::isnan(frac)) return frac;
+    if (std::fabs(frac) < 2.2250738585072014e-308) {  // normalize
+        frac *= 4503599627370496.0;
+        exp -= 52;
+    }
+    uint64_t x;
+    std::memcpy(&x, &frac, 8);
+    exp += (long)((x >> 52) & 0x7ff) - 1023;
+    if (exp < -1075) return std::copysign(0.0, frac);
+    if (exp > 1023) return frac < 0 ? -HUGE_VAL : HUGE_VAL;
+    double m = 1;
+    if (exp < -1022) {
+        exp += 53;
+        m = 1.0 / 9007199254740992.0;
+    }
+    x &= ~(0x7ffull << 52);
+    x |= (uint64_t)(exp + 1023) << 52;
+    double f;
+    std::memcpy(&f, &x, 8);
+    return m * f;
+}
+
+// math.Pow(x, y) for integer y, 0 < |y| < 2^20, x > 0 finite (Go math/pow.go):
+// Frexp, repeated squaring over the bits of |y| with renormalisation to
+// [0.5, 1), one reciprocal for y < 0, Ldexp.
+double go_pow_int(double x, long y) {
+    if (y == 0 || x == 1) return 1;
+    if (y == 1) return x;
+    double a1 = 1;
+    long ae = 0;
+    int xe_i;
+    double x1 = std::frexp(x, &xe_i);
+    long xe = xe_i;
+    for (long i = y < 0 ? -y : y; i != 0; i >>= 1) {
+        if (xe < -(1 << 12) || (1 << 12) < xe) {
+            ae += xe;
+            break;
+        }
+        if (i & 1) {
+            a1 *= x1;
+            ae += xe;
+        }
+        x1 *= x1;
+        xe <<= 1;
+        if (x1 < .5) {
+            x1 += x1;
+            xe--;
+        }
+    }
+    if (y < 0) {
+        a1 = 1 / a1;
+        ae = -ae;
+    }
+    return go_ldexp(a1, ae);
+}
+
+// The lowerable MetaballFalloffFuncs (model3d/metaball.go:17-103).
+struct Falloff {
+    int kind = MC_FALLOFF_POWER;
+    double param = 4, d2 = 0;
+    double operator()(double r) const {
+        if (kind == MC_FALLOFF_POWER) {  // InversePowerMetaballFalloffFunc
+            if (r <= 0) return HUGE_VAL;
+            return go_pow_int(r, -(long)param);
+        }
+        if (r < 0) return HUGE_VAL;  // WyvillMetaballFalloffFunc
+        if (r >= param) return 0;
+        double ratio2 = (r * r) / d2;
+        double value = 1 - ratio2;
+        return value * value;
+    }
+};
+
+// One metaball: a primitive (MetaballField = -SDF) inside TransformMetaball /
+// VecScaleMetaball wrappers, flattened to forward steps innermost first
+// (model3d/transform.go:319-414).
+struct Ball {
+    double w = 0;
+    std::vector<XStep> fwd, inv;
+    std::unique_ptr<Solid> prim;
+    V3 Min() const {
+        V3 a = prim->Min(), b = prim->Max();
+        for (auto& s : fwd) s.apply_bounds(&a, &b);  // ApplyBounds of each wrapper
+        return a;
+    }
+    V3 Max() const {
+        V3 a = prim->Min(), b = prim->Max();
+        for (auto& s : fwd) s.apply_bounds(&a, &b);
+        return b;
+    }
+    double field(V3 c) const {
+        for (auto& s : inv) c = s.apply(c);  // the wrappers' inverse applies, outermost first
+        return -prim->SDF(c);
+    }
+    // MetaballDistBound: the outermost wrapper's inverse ApplyDistance first
+    // (transform.go:56, :87, :186, :339-341, :399-401).
+    double dist_bound(double d) const {
+        for (int i = (int)fwd.size() - 1; i >= 0; i--) {
+            const XStep& s = fwd[i];
+            if (s.kind == MC_XF_SCALE) {
+                d = d * (1 / s.s);
+            } else if (s.kind == MC_XF_VECSCALE) {
+                V3 a = xyz(std::fabs(s.v.x), std::fabs(s.v.y), std::fabs(s.v.z));
+                double mx = a.x > a.y ? (a.x > a.z ? a.x : a.z) : (a.y > a.z ? a.y : a.z);  // MaxCoord
+                d = d * (1 / mx);
+            }
+        }
+        return d;
+    }
+};
+
+// WeightedMetaballSolid (model3d/metaball.go:165-242): the bounds by the
+// outset search, then CheckedFuncSolid of the weighted falloff sum.
+struct MetaballS : Solid {
+    Falloff f;
+    double threshold = 0;
+    std::vector<Ball> balls;
+    V3 mn, mx;
+    void init(double radius_threshold) {
+        threshold = f(radius_threshold);
+        bool any = false;
+        for (auto& b : balls) {
+            if (!(b.w > 0)) continue;
+            if (!any) {
+                mn = b.Min();
+                mx = b.Max();
+                any = true;
+            } else {
+                mn = vmin(mn, b.Min());
+                mx = vmax(mx, b.Max());
+            }
+        }
+        if (!any) throw std::runtime_error("metaball without positive weights");
+        auto value_for_outset = [&](double x) {
+            double sum = 0;
+            for (auto& b : balls)
+                if (b.w > 0) sum += b.w * f(b.dist_bound(x));
+            return sum;
+        };
+        double max_outset = dist(mx, mn);
+        double min_outset = max_outset * 1e-8;
+        for (int i = 0; i < 32; i++) {
+            if (value_for_outset(max_outset) > threshold)
+                max_outset *= 2.0;
+            else
+                break;
+        }
+        if (value_for_outset(max_outset) > threshold) throw std::runtime_error("could not find maximum outset");
+        for (int i = 0; i < 32; i++) {
+            double mid = (min_outset + max_outset) / 2;
+            if (value_for_outset(mid) > threshold)
+                min_outset = mid;
+            else
+                max_outset = mid;
+        }
+        mn = add_scalar(mn, -max_outset);
+        mx = add_scalar(mx, max_outset);
+    }
+    V3 Min() const override { return mn; }
+    V3 Max() const override { return mx; }
+    bool Contains(V3 c) const override {
+        tl_leaf++;
+        if (!in_bounds(mn, mx, c)) return false;
+        double sum = 0;
+        for (auto& b : balls) sum += b.w * f(b.field(c));
+        return sum > threshold;
     }
 };
 
@@ -680,6 +916,27 @@ struct Parser {
 
     V3 pv(const mc_node& nd, int off) { return xyz(nd.p[off], nd.p[off + 1], nd.p[off + 2]); }
 
+    std::vector<XStep> parse_steps(int n_steps) {
+        std::vector<XStep> out;
+        for (int i = 0; i < n_steps; i++) {
+            if (pos >= n) throw std::runtime_error("truncated transform");
+            const mc_node& st = nodes[pos++];
+            XStep x;
+            x.kind = st.kind;
+            if (st.kind == MC_XF_TRANSLATE || st.kind == MC_XF_VECSCALE) {
+                x.v = pv(st, 0);
+            } else if (st.kind == MC_XF_SCALE) {
+                x.s = st.p[0];
+            } else if (st.kind == MC_XF_MATRIX) {
+                for (int k = 0; k < 9; k++) x.m.m[k] = st.p[k];
+            } else {
+                throw std::runtime_error("bad transform step");
+            }
+            out.push_back(x);
+        }
+        return out;
+    }
+
     std::unique_ptr<Solid> parse() {
         if (pos >= n) throw std::runtime_error("truncated node array");
         const mc_node& nd = nodes[pos++];
@@ -769,24 +1026,42 @@ struct Parser {
             case MC_NODE_TRANSFORM: {
                 if (nd.n_children != 1) throw std::runtime_error("transform needs 1 child");
                 auto s = std::make_unique<Transformed>();
-                for (int i = 0; i < nd.n_steps; i++) {
-                    if (pos >= n) throw std::runtime_error("truncated transform");
-                    const mc_node& st = nodes[pos++];
-                    XStep x;
-                    x.kind = st.kind;
-                    if (st.kind == MC_XF_TRANSLATE || st.kind == MC_XF_VECSCALE) {
-                        x.v = pv(st, 0);
-                    } else if (st.kind == MC_XF_SCALE) {
-                        x.s = st.p[0];
-                    } else if (st.kind == MC_XF_MATRIX) {
-                        for (int k = 0; k < 9; k++) x.m.m[k] = st.p[k];
-                    } else {
-                        throw std::runtime_error("bad transform step");
-                    }
-                    s->fwd.push_back(x);
-                }
+                s->fwd = parse_steps(nd.n_steps);
                 s->child = parse();
                 s->init();
+                return s;
+            }
+            case MC_NODE_METABALL: {
+                if (nd.n_children < 0) throw std::runtime_error("negative ball count");
+                auto s = std::make_unique<MetaballS>();
+                s->f.kind = (int)nd.p[1];
+                s->f.param = nd.p[2];
+                if (s->f.kind == MC_FALLOFF_WYVILL) {
+                    if (!(nd.p[2] > 0)) throw std::runtime_error("Wyvill d must be positive");
+                    s->f.d2 = nd.p[2] * nd.p[2];
+                } else if (s->f.kind != MC_FALLOFF_POWER || !(nd.p[2] >= 1 && nd.p[2] < (1 << 20)) ||
+                           nd.p[2] != std::floor(nd.p[2])) {
+                    throw std::runtime_error("falloff not lowerable");
+                }
+                bool any_pos = false;
+                for (int i = 0; i < nd.n_children; i++) {
+                    if (pos >= n || nodes[pos].kind != MC_NODE_BALL) throw std::runtime_error("metaball child is not a ball");
+                    const mc_node& bn = nodes[pos++];
+                    Ball b;
+                    b.w = bn.p[0];
+                    any_pos = any_pos || b.w > 0;
+                    b.fwd = parse_steps(bn.n_steps);
+                    for (int k = (int)b.fwd.size() - 1; k >= 0; k--) b.inv.push_back(b.fwd[k].inverse());
+                    if (pos >= n || nodes[pos].kind < MC_NODE_SPHERE || nodes[pos].kind > MC_NODE_TORUS)
+                        throw std::runtime_error("ball primitive must be a sphere, rect, cylinder, capsule or torus");
+                    b.prim = parse();
+                    s->balls.push_back(std::move(b));
+                }
+                if (!any_pos) {  // NewRect(Origin, Origin), metaball.go:186-188
+                    auto r = std::make_unique<RectS>();
+                    return r;
+                }
+                s->init(nd.p[0]);
                 return s;
             }
             case MC_NODE_CHECKED: {

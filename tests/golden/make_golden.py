@@ -22,7 +22,7 @@ sys.path.insert(0, ROOT)
 
 from model3d_gb300 import (Cylinder, MeshToCollider, NewColliderSolid, Rotation, Sphere,  # noqa: E402
                            SubtractedSolid, TransformSolid, XYZ, canonical, serialize)
-from model3d_gb300.workloads import box_triangles, csg_tree, displaced_icosphere  # noqa: E402
+from model3d_gb300.workloads import box_triangles, csg_tree, displaced_icosphere, metaball_blob  # noqa: E402
 
 
 def cases():
@@ -38,6 +38,7 @@ def cases():
                                            Sphere(XYZ(0.1, 0, 0.3), 0.25))), 0.04, 8),
         "collider_two_boxes_delta0.1_iters8": (NewColliderSolid(MeshToCollider(boxes)), 0.1, 8),
         "collider_icosphere8_delta0.05_iters8": (NewColliderSolid(MeshToCollider(displaced_icosphere(8))), 0.05, 8),
+        "metaball_blob_2_12_delta0.04_iters8": (metaball_blob(2, 12), 0.04, 8),
     }
 
 

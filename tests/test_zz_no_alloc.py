@@ -18,7 +18,7 @@ import pytest
 
 from model3d_gb300 import MarchingCubesSearch, Sphere, XYZ, serialize
 from model3d_gb300 import _native as N
-from model3d_gb300.workloads import csg_tree
+from model3d_gb300.workloads import csg_tree, metaball_blob
 
 pytestmark = pytest.mark.gpu
 
@@ -40,7 +40,8 @@ def test_noalloc_matches_allocating_entry_point_on_consecutive_calls():
     torch = pytest.importorskip("torch")
     cases = [(csg_tree(3, 12, 4), 0.015, 8),      # larger grid first ...
              (Sphere(XYZ(0.1, 0.3, -0.2), 0.6), 0.05, 8),  # ... then a smaller one over its leftovers
-             (csg_tree(3, 12, 4), 0.015, 8)]
+             (csg_tree(3, 12, 4), 0.015, 8),
+             (metaball_blob(4, 16), 0.02, 8)]             # metaball leaves take the same path
     for solid, delta, iters in cases:
         ref = MarchingCubesSearch(solid, delta, iters)
         V, T = len(ref.vertices), len(ref.triangles)
