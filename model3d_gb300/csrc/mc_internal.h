@@ -182,17 +182,28 @@ struct MetaD {
 struct MetaF {
     float lo_dn[3], lo_up[3], hi_dn[3], hi_up[3];  // bounds rounded down / up
     float thr_lo, thr_hi;
-    float d_lo, d_hi, d2_lo, d2_hi;
-    int32_t k;  // power (MC_FALLOFF_POWER)
-    int32_t pad;
+    float d_lo, d_hi;
+    float inv_d2_lo, inv_d2_hi;  // bounds of 1 / (d * d) (Wyvill)
+    float eps_pow;    // relative error bound of the float r^-k (k <= 64), with margin
+    int32_t k;        // power (MC_FALLOFF_POWER)
+    int32_t esc_all;  // parameters outside the filter's range: always float64
 };
-// One ball; constants by primitive (LK_*):
+// One ball; float64 constants by primitive (LK_*), for the exact path:
 //   SPHERE   : center.xyz, R
 //   RECT     : min.xyz, max.xyz
 //   CAPSULE  : P1.xyz, P2.xyz, axis.xyz, norm, R       (axis = (P2-P1) * (1/norm))
 //   CYLINDER : the capsule's 11, then OrthoBasis(-axis) (P1 cap) and
 //              OrthoBasis(axis) (P2 cap): b1.xyz, b2.xyz each
 //   TORUS    : center.xyz, b1.xyz, b2.xyz, outer, inner (b1, b2 = OrthoBasis(Axis))
+// The FP32 filter works relative to an anchor A (the sphere's and torus's
+// centre, the rect's centre, the capsule's and cylinder's P1), so that its
+// rounding errors scale with the distance to the ball, not with the
+// coordinates.  Float constants, relative to A:
+//   SPHERE   : R
+//   RECT     : (min - A).xyz, (max - A).xyz
+//   CAPSULE  : (P2 - A).xyz, axis.xyz, norm, R
+//   CYLINDER : the capsule's 8, then the four basis vectors
+//   TORUS    : b1.xyz, b2.xyz, outer, inner
 constexpr int BALL_C = 24;
 struct BallD {
     int32_t kind;
@@ -203,8 +214,12 @@ struct BallD {
 };
 struct BallF {
     float w_lo, w_hi;  // weight rounded down / up
-    float mag;         // largest |constant|
-    float kerr;        // error-bound factor of the kind
+    float mag;         // largest |relative constant| (lengths, radii, offsets from A)
+    float kint;        // internal rounding factor of the kind (times u)
+    int32_t kind;      // as BallD, so the common path reads one record
+    int32_t n_steps;
+    float a[3];        // the anchor rounded to float
+    float amag;        // max |a|
     float c[BALL_C];
 };
 

@@ -359,31 +359,37 @@ __device__ __forceinline__ void circle_dist_32(const float* b, float qx, float q
     *cur = fminf(*cur, d);
 }
 
-// -SDF of a ball in float.  Returns the absolute error bound of the value
-// against the float64 value, or +Inf when none is given (torus axis).
-__device__ float ball_field_32(int kind, const BallF& b, F3 q, float* out) {
+// -SDF of a ball in float, in coordinates relative to the ball's anchor.
+// Returns an absolute error bound of the value against the float64 value
+// (+Inf near a torus axis).  The float offset q = fl(pf - a) is within
+// e = u (|p| + |a| + |q|) per coordinate of p - A, so, the SDF being
+// 1-Lipschitz, the offset costs at most sqrt(3) e; the rest is the kind's own
+// rounding, kint (|q| + mag + |r|), with kint derived per kind as for the
+// other filters (products and sums of bounded terms, each sqrt a half-ulp
+// of its argument plus one rounding, branch flips continuous in the point).
+__device__ float ball_field_32(const BallF& b, F3 pf, float* out) {
     const float* c = b.c;
+    const float qx = pf.x - b.a[0], qy = pf.y - b.a[1], qz = pf.z - b.a[2];
     float sdf, guard = 0.f;
-    switch (kind) {
-        case LK_SPHERE: sdf = c[3] - dist3_32(q.x - c[0], q.y - c[1], q.z - c[2]); break;
+    switch (b.kind) {
+        case LK_SPHERE: sdf = c[0] - dist3_32(qx, qy, qz); break;
         case LK_RECT: {
-            if (!(q.x >= c[0] && q.y >= c[1] && q.z >= c[2] && q.x <= c[3] && q.y <= c[4] && q.z <= c[5])) {
-                sdf = -dist3_32(q.x - fmaxf(fminf(q.x, c[3]), c[0]), q.y - fmaxf(fminf(q.y, c[4]), c[1]),
-                                q.z - fmaxf(fminf(q.z, c[5]), c[2]));
+            if (!(qx >= c[0] && qy >= c[1] && qz >= c[2] && qx <= c[3] && qy <= c[4] && qz <= c[5])) {
+                sdf = -dist3_32(qx - fmaxf(fminf(qx, c[3]), c[0]), qy - fmaxf(fminf(qy, c[4]), c[1]),
+                                qz - fmaxf(fminf(qz, c[5]), c[2]));
             } else {
-                sdf = fminf(fminf(fminf(q.x - c[0], c[3] - q.x), fminf(q.y - c[1], c[4] - q.y)),
-                            fminf(q.z - c[2], c[5] - q.z));
+                sdf = fminf(fminf(fminf(qx - c[0], c[3] - qx), fminf(qy - c[1], c[4] - qy)),
+                            fminf(qz - c[2], c[5] - qz));
             }
             break;
         }
         case LK_CAPSULE:
         case LK_CYLINDER: {
-            const float qx = q.x - c[0], qy = q.y - c[1], qz = q.z - c[2];
-            const float dot = qx * c[6] + qy * c[7] + qz * c[8];
-            const float nrm = c[9], R = c[10];
+            const float dot = qx * c[3] + qy * c[4] + qz * c[5];
+            const float nrm = c[6], R = c[7];
             const float t = fminf(fmaxf(dot, 0.f), nrm);
-            const float sd = R - dist3_32(qx - c[6] * t, qy - c[7] * t, qz - c[8] * t);
-            if (kind == LK_CAPSULE) {
+            const float sd = R - dist3_32(qx - c[3] * t, qy - c[4] * t, qz - c[5] * t);
+            if (b.kind == LK_CAPSULE) {
                 sdf = sd;
                 break;
             }
@@ -393,31 +399,32 @@ __device__ float ball_field_32(int kind, const BallF& b, F3 q, float* out) {
                 contained = sd > 0.f;
                 cur = fabsf(sd);
             }
-            circle_dist_32(c + 11, qx, qy, qz, -dot, R, &cur);
-            const float rx = q.x - c[3], ry = q.y - c[4], rz = q.z - c[5];
-            circle_dist_32(c + 17, rx, ry, rz, c[6] * rx + c[7] * ry + c[8] * rz, R, &cur);
+            circle_dist_32(c + 8, qx, qy, qz, -dot, R, &cur);
+            const float rx = qx - c[0], ry = qy - c[1], rz = qz - c[2];
+            circle_dist_32(c + 14, rx, ry, rz, c[3] * rx + c[4] * ry + c[5] * rz, R, &cur);
             sdf = contained ? cur : -cur;
             break;
         }
         default: {  // torus
-            const float cx = q.x - c[0], cy = q.y - c[1], cz = q.z - c[2];
-            float x = c[3] * cx + c[4] * cy + c[5] * cz;
-            float y = c[6] * cx + c[7] * cy + c[8] * cz;
+            float x = c[0] * qx + c[1] * qy + c[2] * qz;
+            float y = c[3] * qx + c[4] * qy + c[5] * qz;
             float on = __fsqrt_rn(x * x + y * y);
             // Near the axis the ring point's direction is ill-determined;
             // beyond outer/64 its error moves the distance by a bounded amount.
-            if (!(on >= fabsf(c[9]) * 0.015625f)) guard = INFINITY;
-            const float sc = c[9] / fmaxf(on, 1e-30f);
+            if (!(on >= fabsf(c[6]) * 0.015625f)) guard = INFINITY;
+            const float sc = c[6] / fmaxf(on, 1e-30f);
             x *= sc;
             y *= sc;
-            sdf = c[10] - dist3_32(c[3] * x + c[6] * y - cx, c[4] * x + c[7] * y - cy, c[5] * x + c[8] * y - cz);
+            sdf = c[7] - dist3_32(c[0] * x + c[3] * y - qx, c[1] * x + c[4] * y - qy, c[2] * x + c[5] * y - qz);
             break;
         }
     }
     const float r = -sdf;
     *out = r;
-    const float S = fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fabsf(q.z)) + b.mag;
-    return __fmul_ru(b.kerr, __fadd_ru(S, fabsf(r))) + guard;
+    const float P = fmaxf(fmaxf(fabsf(pf.x), fabsf(pf.y)), fabsf(pf.z));
+    const float Q = fmaxf(fmaxf(fabsf(qx), fabsf(qy)), fabsf(qz));
+    const float eq = __fmul_ru(1.0506e-07f, __fadd_ru(__fadd_ru(P, b.amag), Q));  // 1.74 * 1.01 u (...)
+    return __fadd_ru(eq, __fmul_ru(b.kint, __fadd_ru(__fadd_ru(Q, b.mag), fabsf(r)))) + guard;
 }
 
 __device__ __forceinline__ float powk_ru(float x, int k) {
@@ -437,6 +444,39 @@ __device__ __forceinline__ float powk_rd(float x, int k) {
     return r;
 }
 
+__device__ __forceinline__ float powk_rn(float x, int k) {
+    float r = 1.f, b = x;
+    for (; k; k >>= 1) {
+        if (k & 1) r = __fmul_rn(r, b);
+        b = __fmul_rn(b, b);
+    }
+    return r;
+}
+
+// Bracket [tlo, thi] of r^-k over r in [rlo, rhi] (rlo <= r <= rhi, E =
+// rhi - r): +Inf where r <= 0 is possible.  The fast form computes r^-k once,
+// to nearest, and widens it by the relative change of r^-k over the
+// interval: with rho >= E / rlo and k rho <= 1/4, (1 + rho)^-k >= 1 - k rho
+// (convexity) and (1 - rho)^-k <= 1 + 2 k rho.  __fdividef is within 2 ulp
+// for divisors in [2^-126, 2^126].  Otherwise directed rounding throughout.
+__device__ __forceinline__ void power_bracket(const MetaF& m, float r, float E, float rlo, float rhi, float* tlo,
+                                              float* thi) {
+    if (m.k <= 64 && rlo >= 1.1754944e-38f && rhi <= 8.5e37f) {
+        const float pk = powk_rn(r, m.k);
+        if (pk >= 1.1754944e-38f && pk <= 8.5e37f) {
+            const float tf = __fdividef(1.f, pk);
+            const float krho = __fmul_ru((float)m.k, __fmul_ru(__fdividef(E, rlo), 1.0000005f));
+            if (krho <= 0.25f) {
+                *thi = __fmul_ru(tf, __fadd_ru(1.f, __fadd_ru(__fmul_ru(2.f, krho), m.eps_pow)));
+                *tlo = __fmul_rd(tf, __fsub_rd(1.f, __fadd_ru(krho, m.eps_pow)));
+                return;
+            }
+        }
+    }
+    *tlo = rhi <= 0.f ? INFINITY : __frcp_rd(powk_ru(rhi, m.k));
+    *thi = rlo <= 0.f ? INFINITY : __frcp_ru(powk_rd(rlo, m.k));
+}
+
 // FP32 filter of metaball_64: 1/0 when decided, 2 otherwise.
 __device__ __noinline__ int metaball_32(const ProgView& P, const double* ld, P3 p, F3 pf) {
     const int id = (int)ld[0];
@@ -452,27 +492,30 @@ __device__ __noinline__ int metaball_32(const ProgView& P, const double* ld, P3 
         !(p.x >= md.lo[0] && p.y >= md.lo[1] && p.z >= md.lo[2] && p.x <= md.hi[0] && p.y <= md.hi[1] &&
           p.z <= md.hi[2]))
         return 0;
+    if (m.esc_all) return 2;
     const bool power = md.falloff == MC_FALLOFF_POWER;
     float slo = 0.f, shi = 0.f, sabs = 0.f;
     for (int i = 0; i < md.n_balls; i++) {
-        const BallD& bd = P.balls[md.first_ball + i];
         const BallF& b = P.balls_f[md.first_ball + i];
-        const F3 q = bd.n_steps ? to_f3(apply_steps(P.xstep + bd.first_step, bd.n_steps, p)) : pf;
+        F3 q = pf;
+        if (b.n_steps) {
+            const BallD& bd = P.balls[md.first_ball + i];
+            q = to_f3(apply_steps(P.xstep + bd.first_step, bd.n_steps, p));
+        }
         float r;
-        const float E = ball_field_32(bd.kind, b, q, &r);
+        const float E = ball_field_32(b, q, &r);
         const float rlo = __fsub_rd(r, E), rhi = __fadd_ru(r, E);
         if (!(rlo == rlo) || !(rhi == rhi)) return 2;
         float tlo, thi;  // bracket of f(r) for r in [rlo, rhi]
         if (power) {
-            tlo = rhi <= 0.f ? INFINITY : __frcp_rd(powk_ru(rhi, m.k));
-            thi = rlo <= 0.f ? INFINITY : __frcp_ru(powk_rd(rlo, m.k));
+            power_bracket(m, r, E, rlo, rhi, &tlo, &thi);
         } else {
             if (rhi < 0.f) {
                 tlo = INFINITY;
             } else if (rhi >= m.d_lo) {
                 tlo = 0.f;
             } else {
-                const float v = fmaxf(__fsub_rd(1.f, __fdiv_ru(__fmul_ru(rhi, rhi), m.d2_lo)), 0.f);
+                const float v = fmaxf(__fsub_rd(1.f, __fmul_ru(__fmul_ru(rhi, rhi), m.inv_d2_hi)), 0.f);
                 tlo = __fmul_rd(v, v);
             }
             if (rlo < 0.f) {
@@ -480,7 +523,7 @@ __device__ __noinline__ int metaball_32(const ProgView& P, const double* ld, P3 
             } else if (rlo >= m.d_hi) {
                 thi = 0.f;
             } else {
-                const float v = __fsub_ru(1.f, __fdiv_rd(__fmul_rd(rlo, rlo), m.d2_hi));
+                const float v = __fsub_ru(1.f, __fmul_rd(__fmul_rd(rlo, rlo), m.inv_d2_lo));
                 thi = __fmul_ru(v, v);
             }
         }

@@ -548,9 +548,16 @@ struct Lowerer {
         mf.thr_hi = f_up(thr);
         mf.d_lo = f_down(param);
         mf.d_hi = f_up(param);
-        mf.d2_lo = f_down(md.d2);
-        mf.d2_hi = f_up(md.d2);
+        {  // 1 / d2 rounded in float64 (relative error 2^-53), then widened and rounded outward
+            const double inv = 1 / md.d2;
+            mf.inv_d2_lo = f_down(inv * (1 - 0x1p-50));
+            mf.inv_d2_hi = f_up(inv * (1 + 0x1p-50));
+        }
         mf.k = falloff == MC_FALLOFF_POWER ? (int32_t)param : 0;
+        // r^k by binary powering: squarings double the relative error, so at
+        // most (k + popcount(k)) u <= 2k u, then 2 ulp (4u) for __fdividef.
+        mf.eps_pow = (float)((2.0 * mf.k + 6.0) * 0x1p-24 * 1.5);
+        mf.esc_all = falloff == MC_FALLOFF_WYVILL && !(md.d2 > 1e-30 && md.d2 < 1e30) ? 1 : 0;
         md.first_ball = (int32_t)P->balls.size();
         md.n_balls = nd.n_children;
         bool any_pos = false;
@@ -575,18 +582,38 @@ struct Lowerer {
             auto put = [&](int o, D3 v) {
                 for (int k = 0; k < 3; k++) bd.c[o + k] = v.v[k];
             };
-            int K = 16, nc = 0;
+            int nc = 0, nf = 0;  // double and float constant counts
+            double fc[BALL_C] = {0};  // float constants before rounding
+            D3 A = d3(0, 0, 0);
+            // kint: the kind's own rounding error bound in units of u times
+            // (|q| + mag + |r|) (see ball_field_32): sphere 2.5 n + R + |r| with
+            // n <= |r| + R; rect 1.74 mag + 4.24 |r|; capsule 3.74 norm + 8.3 |q| +
+            // 5.24 (R + |r|); the cylinder's caps add projections on rounded
+            // bases; the torus adds the ring direction (<= 11.4 e_xy beyond
+            // outer/64 of its axis).
+            double kint = 5;
             switch (pr.kind) {
                 case MC_NODE_SPHERE:
                     put(0, pp(0));
                     bd.c[3] = pr.p[3];
                     nc = 4;
+                    A = pp(0);
+                    fc[0] = pr.p[3];
+                    nf = 1;
                     break;
-                case MC_NODE_RECT:
+                case MC_NODE_RECT: {
                     put(0, pp(0));
                     put(3, pp(3));
                     nc = 6;
+                    A = vscale(vadd(pp(0), pp(3)), 0.5);
+                    for (int k = 0; k < 3; k++) {
+                        fc[k] = pr.p[k] - A.v[k];
+                        fc[3 + k] = pr.p[3 + k] - A.v[k];
+                    }
+                    nf = 6;
+                    kint = 6;
                     break;
+                }
                 case MC_NODE_CAPSULE:
                 case MC_NODE_CYLINDER: {  // shapes.go:481-484, :747-749
                     D3 p1 = pp(0), p2 = pp(3);
@@ -599,17 +626,28 @@ struct Lowerer {
                     bd.c[9] = nrm;
                     bd.c[10] = pr.p[6];
                     nc = 11;
-                    K = 64;
+                    A = p1;
+                    for (int k = 0; k < 3; k++) {
+                        fc[k] = p2.v[k] - p1.v[k];
+                        fc[3 + k] = axis.v[k];
+                    }
+                    fc[6] = nrm;
+                    fc[7] = pr.p[6];
+                    nf = 8;
+                    kint = 10;
                     if (pr.kind == MC_NODE_CYLINDER) {  // filledCircleDist bases, shapes.go:775-776
                         D3 b1, b2;
                         ortho_basis(vscale(axis, -1), &b1, &b2);
                         put(11, b1);
                         put(14, b2);
+                        for (int k = 0; k < 3; k++) fc[8 + k] = b1.v[k], fc[11 + k] = b2.v[k];
                         ortho_basis(axis, &b1, &b2);
                         put(17, b1);
                         put(20, b2);
+                        for (int k = 0; k < 3; k++) fc[14 + k] = b1.v[k], fc[17 + k] = b2.v[k];
                         nc = 23;
-                        K = 96;
+                        nf = 20;
+                        kint = 40;
                     }
                     break;
                 }
@@ -622,19 +660,33 @@ struct Lowerer {
                     bd.c[9] = pr.p[6];
                     bd.c[10] = pr.p[7];
                     nc = 11;
-                    K = 128;
+                    A = pp(0);
+                    for (int k = 0; k < 3; k++) fc[k] = b1.v[k], fc[3 + k] = b2.v[k];
+                    fc[6] = pr.p[6];
+                    fc[7] = pr.p[7];
+                    nf = 8;
+                    kint = 128;
                     break;
                 }
                 default: fail("a ball's primitive must be a sphere, rect, cylinder, capsule or torus");
             }
-            bd.kind = pr.kind;
+            (void)nc;
             double mag = 0;
-            for (int k = 0; k < nc; k++) {
-                bf.c[k] = (float)bd.c[k];
-                mag = std::max(mag, std::fabs(bd.c[k]));
+            for (int k = 0; k < nf; k++) {
+                bf.c[k] = (float)fc[k];
+                mag = std::max(mag, std::fabs(fc[k]));
             }
             bf.mag = f_up(mag);
-            bf.kerr = (float)K * 5.9604645e-08f;
+            bf.kint = (float)(kint * 0x1p-24);
+            float am = 0;
+            for (int k = 0; k < 3; k++) {
+                bf.a[k] = (float)A.v[k];
+                am = std::max(am, std::fabs(bf.a[k]));
+            }
+            bf.amag = am;
+            bd.kind = pr.kind;
+            bf.kind = pr.kind;
+            bf.n_steps = bd.n_steps;
             bf.w_lo = f_down(bd.w);
             bf.w_hi = f_up(bd.w);
             P->balls.push_back(bd);
