@@ -320,32 +320,83 @@ __device__ double ball_sdf_64(const BallD& b, P3 p) {
     }
 }
 
+// One float64 term w * f(MetaballField(c)) of the reference's sum
+// (metaball.go:238-240).
+__device__ __forceinline__ double ball_term_64(const XStepD* xstep, const MetaD& m, const BallD& b, P3 p) {
+    const P3 q = b.n_steps ? apply_steps(xstep + b.first_step, b.n_steps, p) : p;
+    const double r = -ball_sdf_64(b, q);  // MetaballField
+    double t;
+    if (m.falloff == MC_FALLOFF_POWER) {
+        t = r <= 0 ? INFINITY : go_pow_neg(r, (int)m.param);
+    } else if (r < 0) {
+        t = INFINITY;
+    } else if (r >= m.param) {
+        t = 0;
+    } else {
+        double v = D_SUB(1.0, D_DIV(D_MUL(r, r), m.d2));
+        t = D_MUL(v, v);
+    }
+    return D_MUL(b.w, t);
+}
+
+__device__ __forceinline__ bool meta_in_bounds(const MetaD& m, P3 p) {  // CheckedFuncSolid (solid.go:46-50)
+    return p.x >= m.lo[0] && p.y >= m.lo[1] && p.z >= m.lo[2] && p.x <= m.hi[0] && p.y <= m.hi[1] && p.z <= m.hi[2];
+}
+
 // WeightedMetaballSolid.Contains in float64 (metaball.go:234-242).
 __device__ __noinline__ bool metaball_64(const ProgView& P, const double* ld, P3 p) {
     const MetaD& m = P.metas[(int)ld[0]];
-    if (m.never) return false;
-    if (!(p.x >= m.lo[0] && p.y >= m.lo[1] && p.z >= m.lo[2] && p.x <= m.hi[0] && p.y <= m.hi[1] &&
-          p.z <= m.hi[2]))
-        return false;
+    if (m.never || !meta_in_bounds(m, p)) return false;
     double sum = 0;
-    for (int i = 0; i < m.n_balls; i++) {
-        const BallD& b = P.balls[m.first_ball + i];
-        const P3 q = b.n_steps ? apply_steps(P.xstep + b.first_step, b.n_steps, p) : p;
-        const double r = -ball_sdf_64(b, q);  // MetaballField
-        double t;
-        if (m.falloff == MC_FALLOFF_POWER) {
-            t = r <= 0 ? INFINITY : go_pow_neg(r, (int)m.param);
-        } else if (r < 0) {
-            t = INFINITY;
-        } else if (r >= m.param) {
-            t = 0;
-        } else {
-            double v = D_SUB(1.0, D_DIV(D_MUL(r, r), m.d2));
-            t = D_MUL(v, v);
-        }
-        sum = D_ADD(sum, D_MUL(b.w, t));
-    }
+    for (int i = 0; i < m.n_balls; i++) sum = D_ADD(sum, ball_term_64(P.xstep, m, P.balls[m.first_ball + i], p));
     return sum > m.thr;
+}
+
+// metaball_64 at the leader lane's point, with the active lanes of `mask`
+// computing the terms and the leader adding them in ball order (the
+// reference's sequential sum, so the result is the same bits).  The tables
+// are the leader's (lanes of a batched launch may run different programs).
+// Kernels that call this have at most 8 warps per block.
+constexpr int kCoopBalls = 256;
+__device__ __noinline__ bool metaball_64_coop(const MetaD& m, const BallD* balls, const XStepD* xstep, P3 p,
+                                              unsigned mask, int leader) {
+    __shared__ double terms[8][kCoopBalls];
+    const int lane = threadIdx.x & 31;
+    double* buf = terms[threadIdx.x >> 5];
+    if (m.never || !meta_in_bounds(m, p)) return false;  // the same for every lane of mask
+    const int rank = __popc(mask & ((1u << lane) - 1u)), nact = __popc(mask);
+    double sum = 0;
+    for (int base = 0; base < m.n_balls; base += kCoopBalls) {
+        const int n = min(kCoopBalls, m.n_balls - base);
+        for (int j = rank; j < n; j += nact) buf[j] = ball_term_64(xstep, m, balls[m.first_ball + base + j], p);
+        __syncwarp(mask);
+        if (lane == leader)
+            for (int j = 0; j < n; j++) sum = D_ADD(sum, buf[j]);
+        __syncwarp(mask);
+    }
+    return sum > m.thr;  // meaningful on the leader
+}
+
+// Resolve the lanes whose FP32 filter could not decide (r == 2).  When a few
+// lanes of the warp escalate, the whole warp computes their float64 sums one
+// point at a time; when many do, each lane computes its own.
+__device__ __forceinline__ bool metaball_resolve(const ProgView& P, const double* ld, P3 p, int r) {
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    unsigned need = __ballot_sync(mask, r == 2);
+    if (__popc(need) > 8) return r == 2 ? metaball_64(P, ld, p) : r == 1;
+    bool res = r == 1;
+    while (need) {
+        const int leader = __ffs(need) - 1;
+        need &= need - 1;
+        const MetaD* ml = (const MetaD*)__shfl_sync(mask, (unsigned long long)(P.metas + (int)ld[0]), leader);
+        const BallD* bl = (const BallD*)__shfl_sync(mask, (unsigned long long)P.balls, leader);
+        const XStepD* xl = (const XStepD*)__shfl_sync(mask, (unsigned long long)P.xstep, leader);
+        const P3 pl{__shfl_sync(mask, p.x, leader), __shfl_sync(mask, p.y, leader), __shfl_sync(mask, p.z, leader)};
+        const bool v = metaball_64_coop(*ml, bl, xl, pl, mask, leader);
+        if (lane == leader) res = v;
+    }
+    return res;
 }
 
 __device__ __forceinline__ float dist3_32(float x, float y, float z) { return __fsqrt_rn(x * x + y * y + z * z); }
@@ -563,13 +614,13 @@ template <int MODE>
 __device__ __noinline__ bool leaf64_point(const ProgView& P, int id, P3 p, Counts& cnt, int* err) {
     const double* d = P.leaf_d + (size_t)id * LEAF_D;
     const int kind = P.leaf_kind[id];
-    if (mode_mb(MODE) && kind == LK_METABALL) {
-        if (mode_f32(MODE)) {
+    if constexpr (mode_mb(MODE)) {
+        if (kind == LK_METABALL) {
+            if constexpr (!mode_f32(MODE)) return metaball_64(P, d, p);
             const int r = metaball_32(P, d, p, to_f3(p));
-            if (r != 2) return r;
-            cnt.esc++;
+            if (r == 2) cnt.esc++;
+            return metaball_resolve(P, d, p, r);
         }
-        return metaball_64(P, d, p);
     }
     switch (kind) {
         case LK_SPHERE: return sphere_64(d, p);
