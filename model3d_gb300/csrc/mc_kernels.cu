@@ -399,6 +399,8 @@ __device__ __forceinline__ bool metaball_resolve(const ProgView& P, const double
     return res;
 }
 
+
+
 __device__ __forceinline__ float dist3_32(float x, float y, float z) { return __fsqrt_rn(x * x + y * y + z * z); }
 
 __device__ __forceinline__ void circle_dist_32(const float* b, float qx, float qy, float qz, float pz, float R,
@@ -528,80 +530,227 @@ __device__ __forceinline__ void power_bracket(const MetaF& m, float r, float E, 
     *thi = rlo <= 0.f ? INFINITY : __frcp_ru(powk_rd(rlo, m.k));
 }
 
-// FP32 filter of metaball_64: 1/0 when decided, 2 otherwise.
-__device__ __noinline__ int metaball_32(const ProgView& P, const double* ld, P3 p, F3 pf) {
-    const int id = (int)ld[0];
-    const MetaD& md = P.metas[id];
-    const MetaF& m = P.metas_f[id];
-    if (md.never) return 0;
-    // InBounds: pf = fl(p) with fl monotone, so pf < fl_down(lo) implies p < lo.
+// Bracket [lo, hi] of the weighted term w f(r) for r in [rlo, rhi]; false
+// when 0 * Inf is possible (NaN in the reference's sum).
+__device__ __forceinline__ bool term_bracket(const MetaF& m, bool power, const BallF& b, float r, float E, float rlo,
+                                             float rhi, float* lo, float* hi, float* ab) {
+    float tlo, thi;  // bracket of f(r) for r in [rlo, rhi]
+    if (power) {
+        power_bracket(m, r, E, rlo, rhi, &tlo, &thi);
+    } else {
+        if (rhi < 0.f) {
+            tlo = INFINITY;
+        } else if (rhi >= m.d_lo) {
+            tlo = 0.f;
+        } else {
+            const float v = fmaxf(__fsub_rd(1.f, __fmul_ru(__fmul_ru(rhi, rhi), m.inv_d2_hi)), 0.f);
+            tlo = __fmul_rd(v, v);
+        }
+        if (rlo < 0.f) {
+            thi = INFINITY;
+        } else if (rlo >= m.d_hi) {
+            thi = 0.f;
+        } else {
+            const float v = __fsub_ru(1.f, __fmul_rd(__fmul_rd(rlo, rlo), m.inv_d2_lo));
+            thi = __fmul_ru(v, v);
+        }
+    }
+    if (b.w_lo > 0.f) {
+        *lo = __fmul_rd(b.w_lo, tlo);
+        *hi = __fmul_ru(b.w_hi, thi);
+    } else if (b.w_hi < 0.f) {
+        *lo = __fmul_rd(b.w_lo, thi);
+        *hi = __fmul_ru(b.w_hi, tlo);
+    } else {  // weight 0 (or below the float range): 0 * Inf is NaN
+        if (thi == INFINITY) return false;
+        *lo = __fmul_rd(b.w_lo, thi);
+        *hi = __fmul_ru(b.w_hi, thi);
+    }
+    const float wabs = fmaxf(fabsf(b.w_lo), fabsf(b.w_hi));
+    *ab = __fmul_ru(wabs, power ? thi : fmaxf(thi, 1.f));
+    return true;
+}
+
+// The sum's decision from its bracket: 1/0 when decided, 2 otherwise.
+__device__ __forceinline__ int sum_decision(const MetaF& m, float slo, float shi, float sabs) {
+    if (!(slo == slo) || !(shi == shi)) return 2;
+    if (slo == INFINITY) return 1;   // a certain +Inf term and no possible -Inf term
+    if (shi == -INFINITY) return 0;  // a certain -Inf term and no possible +Inf term
+    const float margin = __fmul_ru(sabs, 9.094947e-13f);  // 2^-40: float64's own roundings
+    if (__fsub_rd(slo, margin) > m.thr_hi) return 1;
+    if (__fadd_ru(shi, margin) <= m.thr_lo) return 0;
+    return 2;
+}
+
+// The InBounds part of the filter: 0 outside, 1 inside (decided exactly).
+__device__ __forceinline__ bool meta_in_bounds_32(const MetaD& md, const MetaF& m, P3 p, F3 pf) {
+    // pf = fl(p) with fl monotone, so pf < fl_down(lo) implies p < lo.
     if (pf.x < m.lo_dn[0] || pf.y < m.lo_dn[1] || pf.z < m.lo_dn[2] || pf.x > m.hi_up[0] || pf.y > m.hi_up[1] ||
         pf.z > m.hi_up[2])
-        return 0;
-    if (!(pf.x > m.lo_up[0] && pf.y > m.lo_up[1] && pf.z > m.lo_up[2] && pf.x < m.hi_dn[0] && pf.y < m.hi_dn[1] &&
-          pf.z < m.hi_dn[2]) &&
-        !(p.x >= md.lo[0] && p.y >= md.lo[1] && p.z >= md.lo[2] && p.x <= md.hi[0] && p.y <= md.hi[1] &&
-          p.z <= md.hi[2]))
-        return 0;
-    if (m.esc_all) return 2;
+        return false;
+    if (pf.x > m.lo_up[0] && pf.y > m.lo_up[1] && pf.z > m.lo_up[2] && pf.x < m.hi_dn[0] && pf.y < m.hi_dn[1] &&
+        pf.z < m.hi_dn[2])
+        return true;
+    return meta_in_bounds(md, p);
+}
+
+// Sum brackets over the balls in `list` (all balls when list is null),
+// starting from [slo, shi] / sabs.  1/0 when decided, 2 otherwise.
+__device__ __forceinline__ int metaball_32_sum(const ProgView& P, const MetaD& md, const MetaF& m, P3 p, F3 pf,
+                                               const uint16_t* list, int nl, float slo, float shi, float sabs) {
     const bool power = md.falloff == MC_FALLOFF_POWER;
-    float slo = 0.f, shi = 0.f, sabs = 0.f;
-    for (int i = 0; i < md.n_balls; i++) {
-        const BallF& b = P.balls_f[md.first_ball + i];
+    const int n = list ? nl : md.n_balls;
+    for (int k = 0; k < n; k++) {
+        const int i = md.first_ball + (list ? list[k] : k);
+        const BallF& b = P.balls_f[i];
         F3 q = pf;
         if (b.n_steps) {
-            const BallD& bd = P.balls[md.first_ball + i];
+            const BallD& bd = P.balls[i];
             q = to_f3(apply_steps(P.xstep + bd.first_step, bd.n_steps, p));
         }
         float r;
         const float E = ball_field_32(b, q, &r);
         const float rlo = __fsub_rd(r, E), rhi = __fadd_ru(r, E);
         if (!(rlo == rlo) || !(rhi == rhi)) return 2;
-        float tlo, thi;  // bracket of f(r) for r in [rlo, rhi]
-        if (power) {
-            power_bracket(m, r, E, rlo, rhi, &tlo, &thi);
-        } else {
-            if (rhi < 0.f) {
-                tlo = INFINITY;
-            } else if (rhi >= m.d_lo) {
-                tlo = 0.f;
-            } else {
-                const float v = fmaxf(__fsub_rd(1.f, __fmul_ru(__fmul_ru(rhi, rhi), m.inv_d2_hi)), 0.f);
-                tlo = __fmul_rd(v, v);
-            }
-            if (rlo < 0.f) {
-                thi = INFINITY;
-            } else if (rlo >= m.d_hi) {
-                thi = 0.f;
-            } else {
-                const float v = __fsub_ru(1.f, __fmul_rd(__fmul_rd(rlo, rlo), m.inv_d2_lo));
-                thi = __fmul_ru(v, v);
-            }
-        }
-        float lo, hi;
-        if (b.w_lo > 0.f) {
-            lo = __fmul_rd(b.w_lo, tlo);
-            hi = __fmul_ru(b.w_hi, thi);
-        } else if (b.w_hi < 0.f) {
-            lo = __fmul_rd(b.w_lo, thi);
-            hi = __fmul_ru(b.w_hi, tlo);
-        } else {  // weight 0 (or below the float range): 0 * Inf is NaN
-            if (thi == INFINITY) return 2;
-            lo = __fmul_rd(b.w_lo, thi);
-            hi = __fmul_ru(b.w_hi, thi);
-        }
+        float lo, hi, ab;
+        if (!term_bracket(m, power, b, r, E, rlo, rhi, &lo, &hi, &ab)) return 2;
         slo = __fadd_rd(slo, lo);
         shi = __fadd_ru(shi, hi);
-        const float wabs = fmaxf(fabsf(b.w_lo), fabsf(b.w_hi));
-        sabs = __fadd_ru(sabs, __fmul_ru(wabs, power ? thi : fmaxf(thi, 1.f)));
+        sabs = __fadd_ru(sabs, ab);
     }
-    if (!(slo == slo) || !(shi == shi)) return 2;
-    if (slo == INFINITY) return 1;   // a certain +Inf term and no possible -Inf term
-    if (shi == -INFINITY) return 0;  // a certain -Inf term and no possible +Inf term
-    const float margin = __fmul_ru(sabs, 9.094947e-13f);  // 2^-40
-    if (__fsub_rd(slo, margin) > m.thr_hi) return 1;
-    if (__fadd_ru(shi, margin) <= m.thr_lo) return 0;
-    return 2;
+    return sum_decision(m, slo, shi, sabs);
+}
+
+// FP32 filter of metaball_64: 1/0 when decided, 2 otherwise.
+__device__ __noinline__ int metaball_32(const ProgView& P, const double* ld, P3 p, F3 pf) {
+    const int id = (int)ld[0];
+    const MetaD& md = P.metas[id];
+    const MetaF& m = P.metas_f[id];
+    if (md.never || !meta_in_bounds_32(md, m, p, pf)) return 0;
+    if (m.esc_all) return 2;
+    return metaball_32_sum(P, md, m, p, pf, nullptr, 0, 0.f, 0.f, 0.f);
+}
+
+// Far-field split for a classification tile.  For every ball without a
+// transform, the field over the tile's box lies within E + h of its float
+// value at the box centre (the SDF is 1-Lipschitz; h = the half-diagonal,
+// widened for float64's own rounding).  The balls whose weighted-term
+// brackets are narrowest, up to a total width of 2^-8 thr, are summed once
+// here as brackets (the cut-off is the largest of 16 powers of two that
+// keeps the total within budget); the others are listed and evaluated per
+// corner.  A corner whose sum the combined bracket cannot decide goes to
+// the full filter.
+constexpr int kNearMax = 128;
+constexpr int kCuts = 16;
+struct MbRegion {
+    float slo, shi, sabs;
+    int nnear;  // -1: no split (too many near balls, or no budget)
+    uint16_t near[kNearMax];
+};
+
+__device__ __forceinline__ float warp_min(float v) {
+    for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_sum_ru(float v) {  // directed sums bound the sum in any order
+    for (int o = 16; o; o >>= 1) v = __fadd_ru(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_sum_rd(float v) {
+    for (int o = 16; o; o >>= 1) v = __fadd_rd(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Bracket of ball i's weighted term over the box (centre c, radius h);
+// false when the ball cannot be bracketed (transformed, NaN, 0 * Inf).
+__device__ __forceinline__ bool region_term(const ProgView& P, const MetaD& md, const MetaF& m, bool power, int i,
+                                            F3 c, float h, float* tl, float* th, float* ta) {
+    const BallF& b = P.balls_f[md.first_ball + i];
+    if (b.n_steps) return false;
+    float r;
+    const float rad = __fadd_ru(ball_field_32(b, c, &r), h);
+    const float rlo = __fsub_rd(r, rad), rhi = __fadd_ru(r, rad);
+    if (!(rlo == rlo) || !(rhi == rhi)) return false;
+    if (!term_bracket(m, power, b, r, rad, rlo, rhi, tl, th, ta)) return false;
+    return __fsub_ru(*th, *tl) < INFINITY;
+}
+
+// All 32 lanes call this.
+__device__ void metaball_region(const ProgView& P, const MetaD& md, const MetaF& m, const float lo[3],
+                                const float hi[3], MbRegion& R) {
+    const int lane = threadIdx.x & 31;
+    const bool power = md.falloff == MC_FALLOFF_POWER;
+    const F3 c{0.5f * (lo[0] + hi[0]), 0.5f * (lo[1] + hi[1]), 0.5f * (lo[2] + hi[2])};
+    const float hx = fmaxf(__fsub_ru(c.x, lo[0]), __fsub_ru(hi[0], c.x));
+    const float hy = fmaxf(__fsub_ru(c.y, lo[1]), __fsub_ru(hi[1], c.y));
+    const float hz = fmaxf(__fsub_ru(c.z, lo[2]), __fsub_ru(hi[2], c.z));
+    const float cmax = fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z));
+    const float h = __fadd_ru(__fmul_ru(__fsqrt_ru(__fadd_ru(__fadd_ru(__fmul_ru(hx, hx), __fmul_ru(hy, hy)),
+                                                          __fmul_ru(hz, hz))), 1.000001f),
+                              __fmul_ru(cmax, 9.3132257e-10f));  // + 2^-30 |c|
+    const float budget = __fmul_rd(m.thr_lo, 0.00390625f);      // 2^-8 thr
+    const float base = __fdiv_rd(budget, (float)md.n_balls);
+    if (!(base > 0.f) || !(budget < INFINITY)) {
+        if (lane == 0) R.nnear = -1;
+        __syncwarp();
+        return;
+    }
+    // Pass 1: total width below each cut-off base * 2^j.
+    float tot[kCuts];
+#pragma unroll
+    for (int j = 0; j < kCuts; j++) tot[j] = 0.f;
+    for (int i = lane; i < md.n_balls; i += 32) {
+        float tl, th, ta;
+        if (!region_term(P, md, m, power, i, c, h, &tl, &th, &ta)) continue;
+        const float w = __fsub_ru(th, tl);
+        float cut = base;
+#pragma unroll
+        for (int j = 0; j < kCuts; j++) {
+            if (w <= cut) tot[j] = __fadd_ru(tot[j], w);
+            cut *= 2.f;
+        }
+    }
+    float tau = 0.f, cut = base;
+#pragma unroll
+    for (int j = 0; j < kCuts; j++) {
+        if (warp_sum_ru(tot[j]) <= budget) tau = cut;
+        cut *= 2.f;
+    }
+    // Pass 2: sum the far brackets, list the near balls.
+    float slo = 0.f, shi = 0.f, sab = 0.f;
+    int nn = 0;
+    bool ok = tau > 0.f;
+    for (int base_i = 0; base_i < md.n_balls; base_i += 32) {
+        const int i = base_i + lane;
+        bool far = false;
+        float tl = 0.f, th = 0.f, ta = 0.f;
+        if (ok && i < md.n_balls && region_term(P, md, m, power, i, c, h, &tl, &th, &ta))
+            far = __fsub_ru(th, tl) <= tau;
+        if (far) {
+            slo = __fadd_rd(slo, tl);
+            shi = __fadd_ru(shi, th);
+            sab = __fadd_ru(sab, ta);
+        }
+        const bool near = i < md.n_balls && !far;
+        const unsigned nm = __ballot_sync(0xffffffffu, near);
+        if (nn + __popc(nm) > kNearMax) ok = false;
+        if (ok && near) R.near[nn + __popc(nm & ((1u << lane) - 1u))] = (uint16_t)i;
+        nn += __popc(nm);
+    }
+    slo = warp_sum_rd(slo);
+    shi = warp_sum_ru(shi);
+    sab = warp_sum_ru(sab);
+    if (lane == 0) {
+        R.slo = slo;
+        R.shi = shi;
+        R.sabs = sab;
+        R.nnear = ok ? nn : -1;
+    }
+    __syncwarp();
 }
 
 // Float64 predicate of one leaf at one point (reference operation order).
@@ -951,6 +1100,44 @@ __device__ uint32_t capsule_rows32(const float* f, const double* d, const RowCtx
     return in;
 }
 
+// Row masks of a metaball leaf over a classification tile (FP32-filtered).
+template <int PREC>
+__device__ __noinline__ uint32_t metaball_rows(const ProgView& P, int id, const RowCtx& rc, Counts& cnt, int* err) {
+    __shared__ MbRegion regions[8];
+    MbRegion& R = regions[threadIdx.x >> 5];
+    const double* d = P.leaf_d + (size_t)id * LEAF_D;
+    const int mid = (int)d[0];
+    const MetaD& md = P.metas[mid];
+    const MetaF& m = P.metas_f[mid];
+    const bool split = !md.never && !m.esc_all && md.n_balls > 8;
+    if (split) {
+        const float lo[3] = {warp_min(__double2float_rd(rc.px)), warp_min(__double2float_rd(rc.ry)),
+                             warp_min(__double2float_rd(rc.rz))};
+        const float hi[3] = {warp_max(__double2float_ru(rc.px)), warp_max(__double2float_ru(rc.ry)),
+                             warp_max(__double2float_ru(rc.rz))};
+        metaball_region(P, md, m, lo, hi, R);
+    }
+    uint32_t mask = 0;
+    for (int r = 0; r < rc.nrows; r++) {
+        const F3 pf{rc.pxf, shf(rc.ryf, r), shf(rc.rzf, r)};
+        const P3 p = row_point(rc, r);
+        int v;
+        if (md.never || !meta_in_bounds_32(md, m, p, pf)) {
+            v = 0;
+        } else if (m.esc_all) {
+            v = 2;
+        } else {
+            v = 2;
+            if (split && R.nnear >= 0) v = metaball_32_sum(P, md, m, p, pf, R.near, R.nnear, R.slo, R.shi, R.sabs);
+            if (v == 2) v = metaball_32_sum(P, md, m, p, pf, nullptr, 0, 0.f, 0.f, 0.f);
+        }
+        if (v == 2) cnt.esc++;
+        mask |= (metaball_resolve(P, d, p, v) ? 1u : 0u) << r;
+    }
+    (void)err;
+    return mask;
+}
+
 template <int PREC>
 __device__ __forceinline__ uint32_t leaf_rows(const ProgView& P, int id, const RowCtx& rc, Counts& cnt, int* err) {
     const int kind = P.leaf_kind[id];
@@ -964,6 +1151,9 @@ __device__ __forceinline__ uint32_t leaf_rows(const ProgView& P, int id, const R
         case LK_CYLINDER: return f32 ? cylinder_rows32(f, d, rc, cnt) : cylinder_rows64(d, rc);
         case LK_CAPSULE: return f32 ? capsule_rows32(f, d, rc, cnt) : capsule_rows64(d, rc);
         default: {  // torus, collider, metaball: point by point
+            if constexpr (mode_mb(PREC) && mode_f32(PREC)) {
+                if (kind == LK_METABALL) return metaball_rows<PREC>(P, id, rc, cnt, err);
+            }
             uint32_t m = 0;
             for (int r = 0; r < rc.nrows; r++) {
                 const F3 pf{rc.pxf, shf(rc.ryf, r), shf(rc.rzf, r)};

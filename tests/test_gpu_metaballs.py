@@ -50,6 +50,12 @@ def test_quartic_blob_64(oracle):
     assert m.stats["escalations"] <= 0.02 * m.stats["leaf_evals"]
 
 
+def test_many_balls(oracle):
+    """200 balls: classification tiles near the middle have more near balls
+    than the far-field split lists, and fall back to the full sum."""
+    _check(oracle, metaball_blob(21, 200), 0.03)
+
+
 @pytest.mark.parametrize("f", [LinearMetaballFalloffFunc, CubicMetaballFalloffFunc,
                                InversePowerMetaballFalloffFunc(7), WyvillMetaballFalloffFunc(0.4),
                                WyvillMetaballFalloffFunc(0.15)])
