@@ -1103,7 +1103,7 @@ __device__ uint32_t capsule_rows32(const float* f, const double* d, const RowCtx
 // Row masks of a metaball leaf over a classification tile (FP32-filtered).
 template <int PREC>
 __device__ __noinline__ uint32_t metaball_rows(const ProgView& P, int id, const RowCtx& rc, Counts& cnt, int* err) {
-    __shared__ MbRegion regions[8];
+    __shared__ MbRegion regions[8];  // one per warp (at most 8 warps per block)
     MbRegion& R = regions[threadIdx.x >> 5];
     const double* d = P.leaf_d + (size_t)id * LEAF_D;
     const int mid = (int)d[0];

@@ -82,6 +82,9 @@ def test_metaballs_in_csg_and_transforms(oracle):
     _check(oracle, SubtractedSolid(JoinedSolid([mb, Sphere(XYZ(0.9, 0.9, 0.9), 0.3)]),
                                    Capsule(XYZ(-1, 0, 0), XYZ(1, 0, 0), 0.15)), 0.015)
     _check(oracle, TransformSolid(Translate(XYZ(0.3, 0.1, -0.2)), mb), 0.015)
+    # two metaball leaves: the search's far-field region serves the first only
+    _check(oracle, JoinedSolid([metaball_blob(8, 12), TransformSolid(Translate(XYZ(0.4, 0, 0)), metaball_blob(9, 12))]),
+           0.015)
 
 
 def test_infinite_and_nan_terms(oracle):
