@@ -2463,6 +2463,12 @@ struct mc_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // triangle read-back overlapping the search kernel
     cudaEvent_t ev[8] = {};
+    // mc_search searches the vertices in kCopyChunks ranges so that the read-
+    // back of each range overlaps the search of the next.
+    static constexpr int kCopyChunks = 4;
+    cudaEvent_t cev[kCopyChunks] = {};
+    int n_chunks = 0;
+    long long chunk_end[kCopyChunks] = {};
     std::string err;
     DevBuf xs, ys, zs, xf, yf, zf, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
     DevBuf pts, pout;
@@ -2605,6 +2611,7 @@ mc_status mc_create(mc_ctx** out, int device) {
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     for (auto& e : c->ev) CK(cudaEventCreate(&e));
+    for (auto& e : c->cev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     CK(cudaMemcpyToSymbolAsync(c_table, &g_table_host, sizeof(CaseTable), 0, cudaMemcpyHostToDevice, c->stream));
     CK(cudaHostAlloc((void**)&c->h_pin, 64 * sizeof(unsigned long long), cudaHostAllocDefault));
     CK(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
@@ -2623,6 +2630,8 @@ void mc_destroy(mc_ctx* ctx) {
                       &ctx->totals, &ctx->pts, &ctx->pout, &ctx->inner, &ctx->xsteps, &ctx->stl})
         b->release();
     for (auto& e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : ctx->cev)
         if (e) cudaEventDestroy(e);
     if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     {
@@ -2797,9 +2806,10 @@ namespace {
 // words is enqueued; the host has waited only for the mesh totals, which
 // are in st->vertices / st->triangles.  search_finish waits for the rest.
 mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters, const mc_opts* opts_in,
-                        mc_stats* stats) {
+                        mc_stats* stats, int copy_chunks = 1) {
     if (!ctx || !solid || iters < 0) return fail(ctx, MC_ERR_ARG, "bad argument");
     ctx->last_V = ctx->last_T = 0;
+    ctx->n_chunks = 0;
     ctx->has_interior = false;
     mc_opts opts = default_opts(opts_in);
     const HostProgram& H = solid->host;
@@ -2945,9 +2955,27 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
         auto ks = MC_PICK(k_search, opts.precision, P.has_metaball);
         if (smem_s > 48 * 1024)
             CK(cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s));
-        int grid_s = (int)std::min<long long>((V + 127) / 128, (long long)ctx->sm_count * 16);
-        ks<<<grid_s, 128, smem_s, sm>>>(g, P, sa);
-        CK(cudaGetLastError());
+        // Vertex ranges (multiples of 32) searched by consecutive launches,
+        // each followed by an event for the caller's read-back.
+        const int nch = copy_chunks > 1 && V >= (1 << 17) ? std::min(copy_chunks, mc_ctx::kCopyChunks) : 1;
+        ctx->n_chunks = nch;
+        long long v0 = 0;
+        for (int c = 0; c < nch; c++) {
+            const long long v1 = c == nch - 1 ? V : (V * (c + 1) / nch) & ~31LL;
+            SearchArgs sc = sa;
+            sc.keys = sa.keys + v0;
+            sc.verts = sa.verts + 3 * v0;
+            if (sa.interior) sc.interior = sa.interior + 3 * v0;
+            sc.nverts = v1 - v0;
+            if (sc.nverts > 0) {
+                int grid_s = (int)std::min<long long>((sc.nverts + 127) / 128, (long long)ctx->sm_count * 16);
+                ks<<<grid_s, 128, smem_s, sm>>>(g, P, sc);
+                CK(cudaGetLastError());
+            }
+            if (nch > 1) CK(cudaEventRecord(ctx->cev[c], sm));
+            ctx->chunk_end[c] = v1;
+            v0 = v1;
+        }
     }
     CK(cudaEventRecord(ctx->ev[4], sm));
     CK(cudaMemcpyAsync(hp + 8, ctx->stats.p, ST_N * 8, cudaMemcpyDeviceToHost, sm));
@@ -3041,6 +3069,7 @@ void* host_alloc(size_t bytes) {
     void* b = std::malloc(bytes + kHostHead);
     if (!b) return nullptr;
     *(size_t*)b = bytes;
+    ((size_t*)b)[1] = 0;  // bytes known to be faulted in
     return (char*)b + kHostHead;
 }
 
@@ -3081,6 +3110,16 @@ void prefault(void* ptr, size_t bytes) {
         if (a < b) ts.emplace_back(touch, a, b);
     }
     for (auto& t : ts) t.join();
+}
+
+// prefault for arrays from host_alloc: a pooled array keeps its pages, so
+// only its first use (or a larger one) touches them.
+void prefault_pooled(void* p, size_t bytes) {
+    if (!p || !bytes) return;
+    size_t* resident = (size_t*)((char*)p - kHostHead) + 1;
+    if (*resident >= bytes) return;
+    prefault(p, bytes);
+    *resident = bytes;
 }
 
 mc_status enqueue_mesh_copy(mc_ctx* ctx, double* vertices, int32_t* triangles) {
@@ -3165,7 +3204,7 @@ mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t it
     if (!out) return fail(ctx, MC_ERR_ARG, "null output");
     std::memset(out, 0, sizeof(*out));
     mc_stats st{};
-    mc_status s = search_launch(ctx, solid, delta, iters, opts, &st);
+    mc_status s = search_launch(ctx, solid, delta, iters, opts, &st, mc_ctx::kCopyChunks);
     if (s != MC_OK) return s;
     const int64_t V = st.vertices, T = st.triangles;
     ctx->last_V = V;
@@ -3179,7 +3218,7 @@ mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t it
     }
     // Emit and search run on the device meanwhile.  The triangles are final
     // once emit ends (event ev[3]), so their read-back overlaps the search.
-    prefault(out->triangles, (size_t)T * 12);
+    prefault_pooled(out->triangles, (size_t)T * 12);
     s = MC_OK;
     if (T) {
         if (cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[3], 0) != cudaSuccess ||
@@ -3187,8 +3226,22 @@ mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t it
                 cudaSuccess)
             s = fail(ctx, MC_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     }
-    prefault(out->vertices, (size_t)V * 24);
-    if (s == MC_OK) s = enqueue_mesh_copy(ctx, out->vertices, nullptr);
+    prefault_pooled(out->vertices, (size_t)V * 24);
+    if (s == MC_OK && ctx->n_chunks > 1) {
+        // Each vertex range follows its own search launch.
+        long long v0 = 0;
+        for (int c = 0; c < ctx->n_chunks && s == MC_OK; c++) {
+            const long long v1 = ctx->chunk_end[c];
+            if (v1 > v0 && (cudaStreamWaitEvent(ctx->copy_stream, ctx->cev[c], 0) != cudaSuccess ||
+                            cudaMemcpyAsync(out->vertices + 3 * v0, ctx->verts.as<double>() + 3 * v0,
+                                            (size_t)(v1 - v0) * 24, cudaMemcpyDeviceToHost,
+                                            ctx->copy_stream) != cudaSuccess))
+                s = fail(ctx, MC_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+            v0 = v1;
+        }
+    } else if (s == MC_OK) {
+        s = enqueue_mesh_copy(ctx, out->vertices, nullptr);
+    }
     mc_status f = search_finish(ctx, &st);
     if (cudaStreamSynchronize(ctx->copy_stream) != cudaSuccess && f == MC_OK)
         f = fail(ctx, MC_ERR_CUDA, "triangle read-back failed");

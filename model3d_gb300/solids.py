@@ -12,6 +12,7 @@ Anything that is not one of these types cannot be lowered and raises
 from __future__ import annotations
 
 import math
+import struct
 from typing import List, Sequence
 
 import numpy as np
@@ -28,6 +29,8 @@ NODE_DTYPE = np.dtype([
     ("min", "<f8", (3,)), ("max", "<f8", (3,)), ("p", "<f8", (12,)),
 ])
 assert NODE_DTYPE.itemsize == 160
+_NODE_PACK = struct.Struct("<4i18d")  # the same record, packed
+_ZEROS = (0.0,) * 12
 
 
 class NotLowerable(TypeError):
@@ -42,6 +45,24 @@ def _circle_axis_bound(axis: int, normal: Coord3D, sign: float) -> float:
     proj = Coord3D(*arr).ProjectOut(normal)
     proj = proj.Scale(1 / (proj.Norm() + 1e-8))
     return sign * (abs(proj.Array()[axis]) + 1e-8)
+
+
+def _circle_axis_offset(normal: Coord3D, sign: float, scale: float) -> Coord3D:
+    """XYZ(circleAxisBound(0..2, normal, sign)).Scale(scale), with the same
+    float64 operations as _circle_axis_bound (ProjectOut = c - n (n . c) with
+    n = normal.Normalize(), coords.go:379-381, :425-428) on plain floats."""
+    x, y, z = normal.X, normal.Y, normal.Z
+    inv = 1 / math.sqrt(x * x + y * y + z * z)
+    nx, ny, nz = x * inv, y * inv, z * inv
+    out = []
+    for axis in range(3):
+        cx, cy, cz = (sign if axis == 0 else 0.0), (sign if axis == 1 else 0.0), (sign if axis == 2 else 0.0)
+        d = nx * cx + ny * cy + nz * cz
+        px, py, pz = cx + (nx * d) * -1, cy + (ny * d) * -1, cz + (nz * d) * -1
+        f = 1 / (math.sqrt(px * px + py * py + pz * pz) + 1e-8)
+        v = (px * f, py * f, pz * f)[axis]
+        out.append((sign * (abs(v) + 1e-8)) * scale)
+    return Coord3D(out[0], out[1], out[2])
 
 
 class Solid:
@@ -93,14 +114,12 @@ class Cylinder(Solid):
     def Min(self):
         minCenter = self.P1.Min(self.P2)
         axis = self.P2.Sub(self.P1)
-        off = Coord3D(*[_circle_axis_bound(i, axis, -1) for i in range(3)]).Scale(self.Radius)
-        return minCenter.Add(off)
+        return minCenter.Add(_circle_axis_offset(axis, -1.0, self.Radius))
 
     def Max(self):
         maxCenter = self.P1.Max(self.P2)
         axis = self.P2.Sub(self.P1)
-        off = Coord3D(*[_circle_axis_bound(i, axis, 1) for i in range(3)]).Scale(self.Radius)
-        return maxCenter.Add(off)
+        return maxCenter.Add(_circle_axis_offset(axis, 1.0, self.Radius))
 
 
 class Capsule(Solid):
@@ -126,13 +145,13 @@ class Torus(Solid):
     def Min(self):
         r = self.InnerRadius
         extra = XYZ(r, r, r)
-        off = Coord3D(*[_circle_axis_bound(i, self.Axis, -1) for i in range(3)]).Scale(self.OuterRadius)
+        off = _circle_axis_offset(self.Axis, -1.0, self.OuterRadius)
         return off.Add(self.Center).Sub(extra)
 
     def Max(self):
         r = self.InnerRadius
         extra = XYZ(r, r, r)
-        off = Coord3D(*[_circle_axis_bound(i, self.Axis, 1) for i in range(3)]).Scale(self.OuterRadius)
+        off = _circle_axis_offset(self.Axis, 1.0, self.OuterRadius)
         return off.Add(self.Center).Add(extra)
 
 
@@ -506,11 +525,10 @@ def serialize(solid: Solid):
 
     def node(kind, s=None, n_children=0, n_steps=0, mesh=0, p=()):
         if s is not None and (not recs or kind in (COLLIDER, TRANSFORM, CHECKED, METABALL)):
-            mn, mx = tuple(s.Min().Array()), tuple(s.Max().Array())
+            mn, mx = s.Min().Array(), s.Max().Array()
         else:
             mn = mx = zero3
-        pp = tuple(p) + (0.0,) * (12 - len(p))
-        recs.append((kind, n_children, n_steps, mesh, mn, mx, pp))
+        recs.append(_NODE_PACK.pack(kind, n_children, n_steps, mesh, *mn, *mx, *p, *_ZEROS[len(p):]))
 
     def emit(s):
         if isinstance(s, Sphere):
@@ -566,4 +584,4 @@ def serialize(solid: Solid):
             raise NotLowerable(f"{type(s).__name__} has no device lowering")
 
     emit(solid)
-    return np.array(recs, dtype=NODE_DTYPE), sets
+    return np.frombuffer(bytearray(b"".join(recs)), dtype=NODE_DTYPE), sets

@@ -321,6 +321,22 @@ def test_marching_cubes_interior(oracle, iters, prec):
         assert Contains(s, inner, precision="fp64").all()
 
 
+def test_interior_points_of_a_chunked_search(oracle):
+    """A mesh large enough (>= 2^17 vertices) that mc_search runs the search
+    in vertex ranges whose read-back overlaps the next range: vertices and
+    interior points still match the oracle's."""
+    from model3d_gb300 import MarchingCubesInterior
+    s = Sphere(XYZ(0.05, -0.02, 0.01), 1.0)
+    ref = oracle.mc_search(*serialize(s), 0.01, 8, interior=True)
+    mesh, inner = MarchingCubesInterior(s, 0.01, 8)
+    assert len(mesh.vertices) >= 1 << 17
+    _same(mesh, ref)
+    want = dict(zip(map(bytes, ref["tris"].reshape(-1, 3).view(np.uint64)),
+                    map(bytes, ref["interior"].reshape(-1, 3).view(np.uint64))))
+    got = [want[bytes(v)] for v in mesh.vertices.view(np.uint64)]
+    assert got == list(map(bytes, inner.view(np.uint64)))
+
+
 def test_marching_cubes_conj(oracle):
     """MarchingCubesConj (mc.go:66-71): search in the transformed space, then
     the inverse transform on the device; equals the oracle's mesh mapped by
