@@ -2302,6 +2302,12 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
         if (status == 2) atomicOr(&Jp->ca.err[ER_EDGE_INDEX], 1);
         const bool work = live && Jp->iters != 0 && status == 0;
         double tpt = 0;
+        // One bisection call site (a second inlined copy of the evaluation
+        // loop costs instruction fetch): the warp's culled program when its
+        // lanes share a job, else every lane's own job's full program.
+        const ProgView* Pp = &Jp->P;
+        const uint32_t* pr = Jp->P.ops;
+        int ln = Jp->P.n_ops;
         if (uniform) {
             const ProgView& P = b.jobs[j0].P;
             if (j0 != prev_job) {
@@ -2314,24 +2320,18 @@ __global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsi
             uint32_t* cur = q + P.fold_cap;
             if (b.cull && __any_sync(0xffffffffu, work))
                 search_cull(P, work, cpt, axis, lo, hi, q, cur, cur + nw, have_prev, prog, len);
-            if (live && status == 0) {
-                const P3 out =
-                    work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, Jp->iters, hi_bit, cnt, Jp->ca.err, &tpt) : cpt;
-                verts[3 * v] = out.x;
-                verts[3 * v + 1] = out.y;
-                verts[3 * v + 2] = out.z;
-            }
+            Pp = &P;
+            pr = prog;
+            ln = len;
         } else {
-            // The batch straddles jobs: every lane runs its own job's full program.
             prev_job = -1;
-            if (live && status == 0) {
-                const P3 out = work ? bisect<PREC>(Jp->P, Jp->P.ops, Jp->P.n_ops, cpt, axis, lo, hi, Jp->iters, hi_bit,
-                                                   cnt, Jp->ca.err, &tpt)
-                                    : cpt;
-                verts[3 * v] = out.x;
-                verts[3 * v + 1] = out.y;
-                verts[3 * v + 2] = out.z;
-            }
+        }
+        if (live && status == 0) {
+            const P3 out = work ? bisect<PREC>(*Pp, pr, ln, cpt, axis, lo, hi, Jp->iters, hi_bit, cnt, Jp->ca.err, &tpt)
+                                : cpt;
+            verts[3 * v] = out.x;
+            verts[3 * v + 1] = out.y;
+            verts[3 * v + 2] = out.z;
         }
         __syncwarp();
     }
