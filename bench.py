@@ -117,7 +117,7 @@ def cpu_sample(nodes, sets, nz, threads):
     dt = time.perf_counter() - t
     corners = (z1 - z0) * m["nx"] * m["ny"]
     return corners / dt, dict(slabs=(z0, z1), corners=corners, seconds=dt,
-                              triangles=len(m["tris"]))
+                              triangles=len(m["tris"]), leaf_evals=m["leaf_evals"])
 
 
 def run_reference(args):
@@ -271,6 +271,8 @@ def run_ours(args):
                               f"{info['slabs'][1]} ({info['corners']} corners, "
                               f"{info['seconds']:.1f} s)")}
         s0 = sts[0]
+        alu = alu_roofline(s0, serialize(solid)[0], phases["ms_classify"] + phases["ms_search"], pk[0],
+                           info if cpu else None)
         out = {
             "metric": METRIC, "value": value, "unit": "corners/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -292,6 +294,7 @@ def run_ours(args):
             "roofline": roof,
             "tiles": {"tile_y": tuned[0], "tile_z": tuned[1], "chosen_by": "mc_autotune"},
             "measured_peaks_this_gpu": {"fp32_tflops": pk[0], "fp64_tflops": pk[1], "l2_read_gbs": pk[2]},
+            "alu_roofline": alu,
             "other_configs": others,
             "clocks": clk.summary(),
             "wall_s_timed_region": wall,
@@ -514,6 +517,35 @@ def roofline(kernel, ms, st, peaks, kind):
     return {"kernel": name, "bound": "hbm", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": NCU_TRAFFIC.get(name),
             "algorithmic_bytes": int(alg), "ms": ms, "peak_kind": kind}
+
+
+# Float operations of one leaf predicate (precomputed constants; compares
+# count as operations): Sphere 9 + 1, Rect 6, Cylinder 21 + 2, Capsule 21 + 2,
+# Torus about 36.
+LEAF_FLOPS = {1: 10, 2: 6, 3: 23, 4: 23, 5: 36}
+
+
+def alu_roofline(st, nodes, ms, fp32_tflops, ref=None):
+    """Float operations of the leaf evaluations the classification and search
+    kernels performed (their own counter, times the mean operation count of
+    the solid's leaf kinds) over those kernels' event time, against the
+    measured FP32 peak (dense FMA loop).  With ref (the oracle's leaf
+    evaluations per corner on a sample of the same grid) it adds the
+    operations the reference's short-circuit evaluation performs for the
+    whole grid, over the same time: tile culling skips most of them."""
+    kinds = [int(k) for k in nodes["kind"] if int(k) in LEAF_FLOPS]
+    per_leaf = sum(LEAF_FLOPS[k] for k in kinds) / max(1, len(kinds))
+    flops = st["leaf_evals"] * per_leaf
+    achieved = flops / (ms / 1000.0) / 1e12
+    out = {"bound": "fp32_alu", "kernels": ["k_classify", "k_search"], "achieved": achieved,
+           "peak": fp32_tflops, "unit": "TFLOP/s", "frac": achieved / fp32_tflops,
+           "leaf_evals": int(st["leaf_evals"]), "flops_per_leaf_eval": per_leaf, "ms": ms,
+           "peak_kind": "measured on this GPU (mc_measure_peaks)"}
+    if ref:
+        ref_flops = ref["leaf_evals"] / ref["corners"] * st["corners"] * per_leaf
+        out["reference_work"] = {"leaf_evals_per_corner": ref["leaf_evals"] / ref["corners"],
+                                 "flops": ref_flops, "tflops_equivalent": ref_flops / (ms / 1000.0) / 1e12}
+    return out
 
 
 def main():
