@@ -112,19 +112,19 @@ enum {
 
 /*
  * One record of the prefix-order serialisation of a Solid tree: a node, then
- * (for MC_NODE_TRANSFORM) its n_steps transform-step records, then its
+ * (for MC_NODE_TRANSFORM and MC_NODE_BALL) its n_steps transform-step records, then its
  * children, each serialised the same way.
  *
  * min/max are the node's Min()/Max() exactly as the host language computed
  * them; the library uses the root's bounds for the spacer and the bounds of
- * TRANSFORM / CHECKED / COLLIDER nodes for their containment checks, so that
+ * TRANSFORM / CHECKED / COLLIDER / METABALL nodes for their containment checks, so that
  * the grid is bit-identical to the caller's own newSquareSpacer.  The bounds
  * of other non-root nodes are not read and may be left zero.
  */
 typedef struct mc_node {
     int32_t kind;
     int32_t n_children;
-    int32_t n_steps;  /* MC_NODE_TRANSFORM: number of MC_XF_* records that follow */
+    int32_t n_steps;  /* MC_NODE_TRANSFORM / MC_NODE_BALL: number of MC_XF_* records that follow */
     int32_t mesh;     /* MC_NODE_COLLIDER: index into the mc_tri_set array */
     double min[3];
     double max[3];
@@ -223,6 +223,27 @@ mc_status mc_solid_bounds(const mc_solid* solid, double min[3], double max[3]);
  * full count.  MC_ERR_GRID if the loop would not terminate. */
 mc_status mc_spacer_axis(double lo, double hi, double delta, double* out, int64_t cap,
                          int64_t* n);
+
+/* Host-only: lower a node array as mc_solid_create does, without a GPU or a
+ * context, and describe the program.  Returns the lowering's status
+ * (MC_ERR_NOT_LOWERABLE, MC_ERR_BAD_PROGRAM, MC_ERR_LIMIT, ...) with its
+ * message in err (err_cap bytes, may be 0).  No counterpart in the
+ * reference: a binding can refuse an unlowerable solid before any device
+ * work. */
+typedef struct mc_program_info {
+    int64_t n_ops;        /* postfix program words */
+    int64_t n_leaves;     /* leaf predicates: primitives, colliders, metaballs */
+    int64_t n_metaballs;  /* MC_NODE_METABALL leaves */
+    int64_t n_balls;      /* their balls */
+    int64_t n_boxes;      /* TRANSFORM / CHECKED box checks */
+    int64_t n_colliders;  /* collider trees */
+    int64_t max_stack;    /* deepest bit stack */
+    double threshold;     /* f(radiusThreshold) of the first metaball, as the library computed it */
+    double root_min[3];
+    double root_max[3];
+} mc_program_info;
+mc_status mc_program_check(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets, size_t n_sets,
+                           mc_program_info* info, char* err, size_t err_cap);
 
 /* MarchingCubesSearch(s, delta, iters) (model3d/mc.go:45-49); iters == 0 is
  * MarchingCubes (model3d/mc.go:14-37).  The result is copied into host arrays

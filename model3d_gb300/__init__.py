@@ -24,7 +24,7 @@ from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesC2F
                  MarchingCubesFilter, MarchingCubesSearchFilter,
                  MarchingCubesInterior, MarchingCubesSearch, MarchingCubesSearchBatch,
                  MarchingCubesSearchSTL, MCError,
-                 Mesh, autotune, canonical, case_table, default_context, measure_peaks,
+                 Mesh, autotune, canonical, case_table, check_program, default_context, measure_peaks,
                  spacer_axis)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

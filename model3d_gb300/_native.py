@@ -36,7 +36,14 @@ EXPORTS = [
     "mc_search_device", "mc_result_device", "mc_result_copy", "mc_contains", "mc_search_batch",
     "mc_case_table", "mc_version", "mc_search_noalloc", "mc_autotune",
     "mc_measure_peaks", "mc_result_interior_copy", "mc_result_transform", "mc_result_stl",
+    "mc_program_check",
 ]
+
+
+class MCProgramInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in (
+        "n_ops", "n_leaves", "n_metaballs", "n_balls", "n_boxes", "n_colliders", "max_stack")] + [
+        ("threshold", ctypes.c_double), ("root_min", ctypes.c_double * 3), ("root_max", ctypes.c_double * 3)]
 
 
 class MCStats(ctypes.Structure):
@@ -120,6 +127,8 @@ def lib():
                                       ctypes.POINTER(MCOpts), ctypes.POINTER(MCMesh), vp]
         L.mc_case_table.argtypes = [vp, vp]
         L.mc_measure_peaks.argtypes = [vp, ctypes.POINTER(dbl), ctypes.POINTER(dbl), ctypes.POINTER(dbl)]
+        L.mc_program_check.argtypes = [vp, ctypes.c_size_t, vp, ctypes.c_size_t, ctypes.POINTER(MCProgramInfo),
+                                       ctypes.c_char_p, ctypes.c_size_t]
         L.mc_autotune.argtypes = [vp, vp, dbl, i32, ctypes.POINTER(MCOpts), ctypes.POINTER(MCOpts),
                                   ctypes.POINTER(dbl)]
         L.mc_search_noalloc.argtypes = [vp, ctypes.c_size_t, dbl, i32, ctypes.POINTER(MCOpts), vp,

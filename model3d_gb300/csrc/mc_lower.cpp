@@ -1183,3 +1183,41 @@ int build_case_table(uint8_t counts[256], uint8_t tris[256][5][6]) {
 }
 
 }  // namespace mcgpu
+
+extern "C" mc_status mc_program_check(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets,
+                                      size_t n_sets, mc_program_info* info, char* err, size_t err_cap) {
+    using namespace mcgpu;
+    auto message = [&](const char* m) {
+        if (err && err_cap) {
+            std::strncpy(err, m, err_cap - 1);
+            err[err_cap - 1] = 0;
+        }
+    };
+    message("");
+    HostProgram P;
+    try {
+        lower_scene(nodes, n_nodes, sets, n_sets, &P);
+    } catch (const LowerError& e) {
+        message(e.what());
+        return e.status;
+    } catch (const std::exception& e) {
+        message(e.what());
+        return MC_ERR_BAD_PROGRAM;
+    }
+    if (info) {
+        *info = mc_program_info{};
+        info->n_ops = (int64_t)P.ops.size();
+        info->n_leaves = (int64_t)P.leaf_kind.size();
+        info->n_metaballs = (int64_t)P.metas.size();
+        info->n_balls = (int64_t)P.balls.size();
+        info->n_boxes = (int64_t)P.xbox.size();
+        info->n_colliders = (int64_t)P.trees.size();
+        info->max_stack = P.max_stack;
+        info->threshold = P.metas.empty() ? std::numeric_limits<double>::quiet_NaN() : P.metas[0].thr;
+        for (int i = 0; i < 3; i++) {
+            info->root_min[i] = P.root_min[i];
+            info->root_max[i] = P.root_max[i];
+        }
+    }
+    return MC_OK;
+}

@@ -80,6 +80,37 @@ def default_context(device: int = 0) -> Context:
     return ctxs[device]
 
 
+def _tri_sets(sets):
+    """The mc_tri_set array of serialize()'s triangle sets, and the arrays it
+    points into (keep them alive for the call)."""
+    arr = (N.MCTriSet * max(1, len(sets)))()
+    keep = []
+    for i, s in enumerate(sets):
+        t = np.ascontiguousarray(s.tris, dtype=np.float64)
+        keep.append(t)
+        arr[i].tris = t.ctypes.data
+        arr[i].n = len(t)
+        arr[i].grouped = int(s.grouped)
+    return arr, keep
+
+
+def check_program(solid: Solid) -> dict:
+    """Lower `solid` on the host as DeviceSolid would (mc_program_check), with
+    no GPU, and describe the program; raises MCError when it cannot be lowered."""
+    nodes, sets = serialize(solid)
+    arr, keep = _tri_sets(sets)
+    info = N.MCProgramInfo()
+    err = ctypes.create_string_buffer(256)
+    st = N.lib().mc_program_check(nodes.ctypes.data, len(nodes), ctypes.addressof(arr), len(sets),
+                                  ctypes.byref(info), err, len(err))
+    if st != N.MC_OK:
+        raise MCError(st, err.value.decode())
+    out = {n: getattr(info, n) for n, _ in N.MCProgramInfo._fields_[:7]}
+    out["threshold"] = info.threshold
+    out["root_min"], out["root_max"] = list(info.root_min), list(info.root_max)
+    return out
+
+
 class DeviceSolid:
     """A Solid lowered to the device (mc_solid): CSG bytecode and collider
     trees resident in HBM.  Reuse it across calls to avoid re-lowering."""
@@ -89,14 +120,7 @@ class DeviceSolid:
         nodes, sets = serialize(solid)
         self.nodes = nodes
         self._sets = sets
-        arr = (N.MCTriSet * max(1, len(sets)))()
-        keep = []
-        for i, s in enumerate(sets):
-            t = np.ascontiguousarray(s.tris, dtype=np.float64)
-            keep.append(t)
-            arr[i].tris = t.ctypes.data
-            arr[i].n = len(t)
-            arr[i].grouped = int(s.grouped)
+        arr, keep = _tri_sets(sets)
         p = ctypes.c_void_p()
         _check(N.lib().mc_solid_create(self.ctx.ptr, nodes.ctypes.data, len(nodes),
                                        ctypes.addressof(arr), len(sets), ctypes.byref(p)),

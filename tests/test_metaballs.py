@@ -161,3 +161,59 @@ def test_serialised_records(oracle):
     assert nodes[2]["p"][0] == 1.0 and nodes[2]["n_steps"] == 2 and nodes[6]["p"][0] == -0.5
     assert list(nodes[1]["min"]) == mb.Min().Array()
     oracle.bounds(nodes, [])  # parses
+
+
+def _records(s):
+    nodes, _ = serialize(s)
+    return nodes.copy()
+
+
+def test_library_lowering_on_the_host():
+    """mc_program_check lowers without a GPU: the library's own restatement of
+    math.Pow gives the same threshold bits as the Python mirror's, the root
+    bounds are the serialised ones, and the program has one leaf per metaball."""
+    from model3d_gb300 import check_program
+    for name, s in _solids().items():
+        info = check_program(s)
+        assert info["n_metaballs"] == 1 and info["n_leaves"] == 1, name
+        assert info["n_balls"] == len(s.balls)
+        assert info["threshold"] == s.falloff(s.radiusThreshold), name
+        assert info["root_min"] == s.Min().Array() and info["root_max"] == s.Max().Array()
+    for k in range(1, 9):
+        for rt in (0.05, 0.1, 0.37, 1.0, 3.3):
+            s = MetaballSolid(InversePowerMetaballFalloffFunc(k), rt, Sphere(XYZ(0, 0, 0), 0.3))
+            assert check_program(s)["threshold"] == go_pow_int(rt, -k)
+    info = check_program(JoinedSolid([metaball_blob(1, 5), Sphere(XYZ(2, 0, 0), 0.2)]))
+    assert info["n_metaballs"] == 1 and info["n_leaves"] == 2
+
+
+def test_library_lowering_errors():
+    """Malformed or unlowerable metaball records return statuses on the host."""
+    import ctypes
+    from model3d_gb300 import _native as N
+    L = N.lib()
+    base = _records(MetaballSolid(None, 0.1, Sphere(XYZ(0, 0, 0), 0.3), Capsule(XYZ(0, 0, 0), XYZ(0.2, 0, 0), 0.1)))
+
+    def status(nodes):
+        err = ctypes.create_string_buffer(256)
+        return L.mc_program_check(nodes.ctypes.data, len(nodes), None, 0, None, err, 256), err.value.decode()
+
+    assert status(base)[0] == N.MC_OK
+    bad = base.copy()
+    bad[0]["p"][1] = 3  # unknown falloff kind
+    assert status(bad)[0] == N.MC_ERR_NOT_LOWERABLE
+    bad = base.copy()
+    bad[0]["p"][2] = 2.5  # non-integer power
+    assert status(bad)[0] == N.MC_ERR_NOT_LOWERABLE
+    bad = base.copy()
+    bad[0]["p"][1], bad[0]["p"][2] = 2, -1.0  # Wyvill needs d > 0
+    assert status(bad)[0] == N.MC_ERR_BAD_PROGRAM
+    bad = base.copy()
+    bad[1]["kind"] = 1  # a ball record replaced by a primitive
+    assert status(bad)[0] == N.MC_ERR_BAD_PROGRAM
+    bad = base.copy()
+    bad[2]["kind"] = 16  # a ball's primitive replaced by a combinator
+    assert status(bad)[0] == N.MC_ERR_BAD_PROGRAM
+    assert status(base[:3])[0] == N.MC_ERR_BAD_PROGRAM  # truncated
+    many = _records(MetaballSolid(None, 0.1, *[Sphere(XYZ(i * 0.01, 0, 0), 0.1) for i in range(4097)]))
+    assert status(many)[0] == N.MC_ERR_LIMIT
