@@ -117,6 +117,38 @@ def test_sphere_volume(oracle):
         assert abs(vol - 4 / 3 * math.pi * s.Radius ** 3) <= 1e-2
 
 
+def test_search_vertices_lie_on_the_surface(oracle):
+    """The SDF tests' solid (sdf_test.go:189-196, the torus of
+    TestMeshSDFVertices / TestMeshSDFConsistency at delta 0.02, iters 8): every
+    searched vertex lies within the last bisection step of the true surface,
+    |SDF| <= delta * 2^-8 (a crossing is bracketed on its edge to 2^-iters of
+    the edge, and the SDF is 1-Lipschitz); a sphere and a capsule likewise."""
+    ax = XYZ(1, 2, -0.5).Normalize()
+    torus = Torus(XYZ(0, 0, 0), ax, 0.7, 0.2)
+    a = np.array(ax.Array())
+
+    def torus_sdf(v):
+        h = v @ a
+        ring = np.linalg.norm(v - h[:, None] * a, axis=1)
+        return 0.2 - np.sqrt((ring - 0.7) ** 2 + h ** 2)
+
+    def sphere_sdf(v):
+        return 0.55 - np.linalg.norm(v - np.array([0.1, -0.2, 0.05]), axis=1)
+
+    p1, p2 = np.array([-0.3, 0.1, 0.0]), np.array([0.4, -0.2, 0.3])
+
+    def capsule_sdf(v):
+        d = p2 - p1
+        t = np.clip((v - p1) @ d / (d @ d), 0, 1)
+        return 0.25 - np.linalg.norm(v - (p1 + t[:, None] * d), axis=1)
+
+    for s, sdf in ((torus, torus_sdf), (Sphere(XYZ(0.1, -0.2, 0.05), 0.55), sphere_sdf),
+                   (Capsule(XYZ(*p1), XYZ(*p2), 0.25), capsule_sdf)):
+        m = oracle.mc_search(*serialize(s), 0.02, 8)
+        v = m["tris"].reshape(-1, 3)
+        assert np.abs(sdf(v)).max() <= 0.02 / 256 * 1.001
+
+
 def test_search_mesh_is_closed(oracle):
     for seed in range(3):
         s = csg_tree(seed, 6, 2)
