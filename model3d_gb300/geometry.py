@@ -85,10 +85,17 @@ class Coord3D:
         return math.sqrt(d1 * d1 + d2 * d2 + d3 * d3)
 
     def Min(self, c: "Coord3D") -> "Coord3D":
-        return Coord3D(go_min(self.X, c.X), go_min(self.Y, c.Y), go_min(self.Z, c.Z))
+        # A strict comparison decides math.Min; ties (+0/-0) and NaN go to go_min.
+        a, b = self, c
+        return Coord3D(a.X if a.X < b.X else (b.X if b.X < a.X else go_min(a.X, b.X)),
+                       a.Y if a.Y < b.Y else (b.Y if b.Y < a.Y else go_min(a.Y, b.Y)),
+                       a.Z if a.Z < b.Z else (b.Z if b.Z < a.Z else go_min(a.Z, b.Z)))
 
     def Max(self, c: "Coord3D") -> "Coord3D":
-        return Coord3D(go_max(self.X, c.X), go_max(self.Y, c.Y), go_max(self.Z, c.Z))
+        a, b = self, c
+        return Coord3D(a.X if a.X > b.X else (b.X if b.X > a.X else go_max(a.X, b.X)),
+                       a.Y if a.Y > b.Y else (b.Y if b.Y > a.Y else go_max(a.Y, b.Y)),
+                       a.Z if a.Z > b.Z else (b.Z if b.Z > a.Z else go_max(a.Z, b.Z)))
 
     def Sum(self) -> float:
         return self.X + self.Y + self.Z
