@@ -126,3 +126,59 @@ def test_empty_threshold(oracle):
     """radiusThreshold <= 0 makes the threshold +Inf: nothing is contained."""
     m = MarchingCubesSearch(DeviceSolid(MetaballSolid(None, 0.0, CAPS[0])), 0.05, 8)
     assert m.NumTriangles() == 0
+
+
+def _random_metaball(seed):
+    """A metaball solid mixing every primitive kind and wrapper, negative and
+    non-float weights, and one of the lowerable falloffs."""
+    from model3d_gb300.workloads import SplitMix64
+    rng = SplitMix64(seed)
+    balls, weights = [], []
+    for i in range(6 + seed % 7):
+        c = XYZ(rng.uniform(-0.5, 0.5), rng.uniform(-0.5, 0.5), rng.uniform(-0.5, 0.5))
+        r = rng.uniform(0.05, 0.2)
+        k = rng.next_u64() % 5
+        axis = rng.unit_vector()
+        if k == 0:
+            b = Sphere(c, r)
+        elif k == 1:
+            h = XYZ(rng.uniform(0.03, 0.15), rng.uniform(0.03, 0.15), rng.uniform(0.03, 0.15))
+            b = Rect(c.Sub(h), c.Add(h))
+        elif k == 2:
+            b = Capsule(c.Sub(axis.Scale(0.1)), c.Add(axis.Scale(0.1)), r)
+        elif k == 3:
+            b = Cylinder(c.Sub(axis.Scale(0.1)), c.Add(axis.Scale(0.1)), r)
+        else:
+            b = Torus(c, axis, 0.15, r * 0.5)
+        w = rng.next_u64() % 4
+        if w == 0:
+            b = TranslateMetaball(RotateMetaball(b, rng.unit_vector(), rng.uniform(0, 3)), XYZ(0.05, -0.02, 0.01))
+        elif w == 1:
+            b = VecScaleMetaball(ScaleMetaball(b, rng.uniform(0.7, 1.3)), XYZ(1.1, 0.9, rng.uniform(0.8, 1.2)))
+        balls.append(b)
+        weights.append(-rng.uniform(0.1, 0.5) if i % 4 == 3 else rng.uniform(0.4, 1.6))
+    f = [None, CubicMetaballFalloffFunc, LinearMetaballFalloffFunc, WyvillMetaballFalloffFunc(0.3)][seed % 4]
+    return WeightedMetaballSolid(f, 0.08 if f is None or f is CubicMetaballFalloffFunc else 0.12, balls, weights)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_filter_is_sound_on_random_metaballs(oracle, seed):
+    """FP32-filtered Contains equals the float64 kernel at every point on and
+    a few float ulps around the threshold surface of random metaball solids
+    (the filter never decides a point the float64 sum would decide the other
+    way), and both equal the oracle on a subset."""
+    s = _random_metaball(seed)
+    ds = DeviceSolid(s)
+    mesh = MarchingCubesSearch(ds, 0.02, 8, precision="fp64")
+    if mesh.NumTriangles() == 0:
+        pytest.skip("empty solid")
+    v = np.unique(mesh.vertices, axis=0)
+    sp = np.spacing(v.astype(np.float32)).astype(float)
+    pts = np.ascontiguousarray(np.concatenate(
+        [v, np.nextafter(v, np.inf), np.nextafter(v, -np.inf), v + sp, v - sp, v + 3 * sp, v - 3 * sp]))
+    a = Contains(s, pts, precision="fp32")
+    b = Contains(s, pts, precision="fp64")
+    assert (a == b).all(), f"{np.count_nonzero(a != b)} of {len(pts)} points differ"
+    sub = pts[::7]
+    ref, _ = oracle.contains(*serialize(s), np.ascontiguousarray(sub))
+    assert (b[::7] == ref).all()
