@@ -2,7 +2,7 @@
 
 The oracle is the CPU restatement of the reference MarchingCubesSearch path
 in oracle/mc_oracle.cpp.  Only tests/, __graft_entry__.smoke() and bench.py's
-CPU-baseline leg load it, as the checker; the product never does.
+CPU-baseline leg load it, to check results against; the product never does.
 """
 from __future__ import annotations
 
