@@ -281,3 +281,21 @@ def test_invalid_bounds_panic(oracle):
     with pytest.raises(oracle.OracleError) as e:
         oracle.mc_search(nodes, sets, 0.1, 8)
     assert e.value.status == 1
+
+
+def test_coord_min_max_follow_go_math():
+    """Coord3D.Min/Max take a strict comparison first; on ties (+0 / -0), NaN
+    and infinities they must still give math.Min / math.Max's answers
+    (coords.go:440-448)."""
+    from model3d_gb300.geometry import Coord3D, go_max, go_min
+    vals = [0.0, -0.0, 1.0, -1.0, math.inf, -math.inf, math.nan, 2.5, -3.0, 5e-324]
+
+    def same(a, b):
+        return (math.isnan(a) and math.isnan(b)) or (a == b and math.copysign(1, a) == math.copysign(1, b))
+
+    for x in vals:
+        for y in vals:
+            a, b = Coord3D(x, y, x), Coord3D(y, x, y)
+            m, M = a.Min(b), a.Max(b)
+            for got, want in ((m.X, go_min(x, y)), (m.Y, go_min(y, x)), (M.X, go_max(x, y)), (M.Y, go_max(y, x))):
+                assert same(got, want), (x, y, got, want)
