@@ -343,22 +343,43 @@ def _device_rate(L, N, ctx, ds, delta, iters, prec, flush, torch, reps=3):
 def other_configs(ctx, torch, flush, single_rate, count=16):
     """The other benchmark configurations, device time (CUDA events, best of 3
     after a warm-up): unit sphere (delta 0.01), the 1,048,820-triangle
-    displaced icosphere collider on a ~256^3 grid, and 512 CSG solids in one
-    batched launch (graph replay) next to the same solids one call at a time."""
-    import ctypes
-    from model3d_gb300 import (DeviceSolid, MarchingCubesSearchBatch, MeshToCollider,
-                               NewColliderSolid, Sphere, XYZ)
-    from model3d_gb300 import _native as N
-    from model3d_gb300.workloads import csg_batch, displaced_icosphere
-    L = N.lib()
+    displaced icosphere collider on a ~256^3 grid, 512 CSG solids in one
+    batched launch (graph replay) next to the same solids one call at a
+    time, a 64-ball metaball, and batched colliders.  A configuration that
+    fails is reported under its name with the error, without losing the
+    others or the headline line."""
     out = {}
+    lines = [("sphere_r1_delta0.01", lambda: sphere_line(ctx, torch, flush)),
+             ("collider_icosphere_1048820_tris_256cubed", lambda: collider_line(ctx, torch, flush)),
+             ("batch_512_csg", lambda: batch_line(ctx, torch, flush, single_rate)),
+             ("metaball_blob64_quartic_delta0.005", lambda: metaball_line(ctx, torch, flush)),
+             ("batch_colliders", lambda: collider_batch_line(ctx, count))]
+    for name, f in lines:
+        try:
+            out.update(f())
+        except Exception as e:  # noqa: BLE001 - reported in the JSON line
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    return out
+
+
+def sphere_line(ctx, torch, flush):
+    from model3d_gb300 import DeviceSolid, Sphere, XYZ
+    from model3d_gb300 import _native as N
+    L = N.lib()
     sph = DeviceSolid(Sphere(XYZ(0, 0, 0), 1.0), ctx)
     a = _device_rate(L, N, ctx, sph, 0.01, 8, N.MC_PREC_FP32_FILTERED, flush, torch)
     b = _device_rate(L, N, ctx, sph, 0.01, 8, N.MC_PREC_FP64, flush, torch)
-    out["sphere_r1_delta0.01"] = {"corners": a["corners"], "triangles": a["triangles"],
-                                  "fp32_corners_per_s": a["corners"] / (a["ms_total"] / 1e3),
-                                  "fp64_corners_per_s": b["corners"] / (b["ms_total"] / 1e3),
-                                  "ms_fp32": a["ms_total"], "ms_fp64": b["ms_total"]}
+    return {"sphere_r1_delta0.01": {"corners": a["corners"], "triangles": a["triangles"],
+                                    "fp32_corners_per_s": a["corners"] / (a["ms_total"] / 1e3),
+                                    "fp64_corners_per_s": b["corners"] / (b["ms_total"] / 1e3),
+                                    "ms_fp32": a["ms_total"], "ms_fp64": b["ms_total"]}}
+
+
+def collider_line(ctx, torch, flush):
+    from model3d_gb300 import DeviceSolid, MeshToCollider, NewColliderSolid
+    from model3d_gb300 import _native as N
+    from model3d_gb300.workloads import displaced_icosphere
+    L = N.lib()
     tris = displaced_icosphere(229)
     col = NewColliderSolid(MeshToCollider(tris))
     mn, mx = col.Min(), col.Max()
@@ -369,13 +390,20 @@ def other_configs(ctx, torch, flush, single_rate, count=16):
     a = _device_rate(L, N, ctx, cds, d, 8, N.MC_PREC_FP32_FILTERED, flush, torch, reps=2)
     b = _device_rate(L, N, ctx, cds, d, 8, N.MC_PREC_FP64, flush, torch, reps=1)
     tests = a["bvh_nodes"] + a["bvh_tris"]
-    out["collider_icosphere_1048820_tris_256cubed"] = {
+    return {"collider_icosphere_1048820_tris_256cubed": {
         "grid": [a["nx"], a["ny"], a["nz"]], "triangles_in": len(tris), "triangles_out": a["triangles"],
         "fp32_corners_per_s": a["corners"] / (a["ms_total"] / 1e3),
         "fp64_corners_per_s": b["corners"] / (b["ms_total"] / 1e3),
         "ms_fp32": a["ms_total"], "ms_fp64": b["ms_total"],
         "escalation_rate": a["escalations"] / max(1, tests), "bvh_box_tests": a["bvh_nodes"],
-        "triangle_tests": a["bvh_tris"], "host_lowering_s": lower_s}
+        "triangle_tests": a["bvh_tris"], "host_lowering_s": lower_s}}
+
+
+def batch_line(ctx, torch, flush, single_rate):
+    from model3d_gb300 import DeviceSolid, MarchingCubesSearchBatch
+    from model3d_gb300 import _native as N
+    from model3d_gb300.workloads import csg_batch
+    L = N.lib()
     items = csg_batch(2024, count=512)
     jobs = [(DeviceSolid(s, ctx), dd, 8) for s, dd in items]
     res = {}
@@ -395,7 +423,7 @@ def other_configs(ctx, torch, flush, single_rate, count=16):
     br = _device_rate(L, N, ctx, bds, bd, bit, N.MC_PREC_FP32_FILTERED, flush, torch, reps=3)
     big_rate = br["corners"] / (br["ms_total"] / 1e3)
     corners = res["fp32"][1]
-    out["batch_512_csg"] = {
+    return {"batch_512_csg": {
         "jobs": len(jobs), "corners": corners, "triangles": res["fp32"][2],
         "fp32_corners_per_s": corners / (res["fp32"][0] / 1e3),
         "fp32_meshes_per_s": len(jobs) / (res["fp32"][0] / 1e3),
@@ -406,10 +434,7 @@ def other_configs(ctx, torch, flush, single_rate, count=16):
         "fraction_of_single_large_solid_rate": (corners / (res["fp32"][0] / 1e3)) / single_rate,
         "largest_job_alone": {"corners": br["corners"], "triangles": br["triangles"],
                               "fp32_corners_per_s": big_rate},
-        "fraction_of_largest_job_alone_rate": (corners / (res["fp32"][0] / 1e3)) / big_rate}
-    out.update(metaball_line(ctx, torch, flush))
-    out.update(collider_batch_line(ctx, count))
-    return out
+        "fraction_of_largest_job_alone_rate": (corners / (res["fp32"][0] / 1e3)) / big_rate}}
 
 
 def metaball_line(ctx, torch, flush):
