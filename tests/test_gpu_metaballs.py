@@ -182,3 +182,26 @@ def test_filter_is_sound_on_random_metaballs(oracle, seed):
     sub = pts[::7]
     ref, _ = oracle.contains(*serialize(s), np.ascontiguousarray(sub))
     assert (b[::7] == ref).all()
+
+
+def test_power_and_parameter_extremes(oracle):
+    """Powers past the fast bracket's k <= 64, and Wyvill radii whose d^2
+    leaves the float range (every corner then takes the float64 sum)."""
+    s1 = Sphere(XYZ(0, 0, 0), 0.3)
+    s2 = Capsule(XYZ(0.1, -0.2, 0.05), XYZ(0.35, 0.1, -0.1), 0.12)
+    _check(oracle, MetaballSolid(InversePowerMetaballFalloffFunc(20), 0.1, s1, s2), 0.02)
+    _check(oracle, MetaballSolid(InversePowerMetaballFalloffFunc(100), 0.1, s1, s2), 0.02)
+    # d^2 = 9e-32: every corner in the box takes the float64 sum.  Inside a
+    # ball the Wyvill falloff is +Inf, so the solid is the balls' union.
+    _check(oracle, WeightedMetaballSolid(WyvillMetaballFalloffFunc(3e-16), 1e-16, [s1, s2], [1.0, 0.5]), 0.02)
+
+
+def test_metaball_with_collider_and_intersection(oracle):
+    """Metaball leaves next to a collider leaf (both rare kinds in one
+    program) and under an intersection."""
+    from model3d_gb300 import IntersectedSolid, MeshToCollider, NewColliderSolid
+    from model3d_gb300.workloads import displaced_icosphere
+    col = NewColliderSolid(MeshToCollider(displaced_icosphere(6) * 0.4 + 0.5))
+    mb = metaball_blob(13, 10)
+    _check(oracle, JoinedSolid([mb, col]), 0.02)
+    _check(oracle, IntersectedSolid([mb, Rect(XYZ(-0.5, -0.6, -0.4), XYZ(0.4, 0.3, 0.5))]), 0.015)
