@@ -675,6 +675,7 @@ struct ClassifyArgs {
     int cull;
     int ty, tz;  // tile height / depth (rows per tile = ty * tz)
     int ntx, nty, ntz;
+    int nxs;  // x segments per column (0 or 1: one item walks the whole column)
 };
 
 __device__ __forceinline__ bool cull_overlap_f(const float* c, const float lo[3], const float hi[3]) {
@@ -700,8 +701,9 @@ __device__ __forceinline__ uint32_t transpose32(uint32_t m, int lane) {
 // Per tile the warp ballots which leaves' culling boxes meet the tile (float
 // boxes rounded outward, tile box rounded outward) and re-folds the program
 // only when that set changed since the previous tile of the column.
-// One work item of the classification: the column of 32 x ty x tz corner
-// tiles at (ty, tz) = (item % nty, item / nty), walked along x.  Per tile the
+// One work item of the classification: segment item % nxs of the column of
+// 32 x ty x tz corner tiles at (ty, tz) = (c % nty, c / nty), c = item / nxs,
+// walked along x.  Per tile the
 // warp ballots which leaves' culling boxes meet the tile (float boxes rounded
 // outward, tile box rounded outward) and re-folds the program only when that
 // set changed since the previous tile of the column.
@@ -712,6 +714,10 @@ __device__ __forceinline__ void classify_column(const GridView& g, const ProgVie
     const int lane = threadIdx.x & 31;
     const int nw = (P.n_leaves + 31) >> 5;
     const int rows = a.ty * a.tz;
+    const int nxs = a.nxs > 1 ? a.nxs : 1;
+    const int seg = item % nxs;
+    item /= nxs;
+    const int tx_begin = seg * a.ntx / nxs, tx_end = (seg + 1) * a.ntx / nxs;
     const int ty = item % a.nty, tz = item / a.nty;
     const int y0 = ty * a.ty, z0 = tz * a.tz;
     const int y1 = min(y0 + a.ty - 1, g.ny - 1), z1 = min(z0 + a.tz - 1, g.nz - 1);
@@ -720,7 +726,7 @@ __device__ __forceinline__ void classify_column(const GridView& g, const ProgVie
     bool have_prev = false;
     int len = P.n_ops;
     const uint32_t* prog = P.ops;
-    for (int tx = 0; tx < a.ntx; tx++) {
+    for (int tx = tx_begin; tx < tx_end; tx++) {
         const int x0 = tx * 32, x1 = min(x0 + 31, g.nx - 1);
         if (a.cull) {
             const float lo[3] = {__double2float_rd(g.xs[x0]), ylo, zlo};
@@ -832,7 +838,7 @@ __global__ void __launch_bounds__(256, 3) k_classify(GridView g, ProgView P, Cla
     uint32_t* prev = cur + nw;
     Counts cnt;
     unsigned long long nconst = 0;
-    const int nitems = a.nty * a.ntz;
+    const int nitems = a.nty * a.ntz * (a.nxs > 1 ? a.nxs : 1);
     for (;;) {
         int item = 0;
         if (lane == 0) item = (int)atomicAdd(a.work, 1u);
@@ -1949,6 +1955,17 @@ void pick_tiles(const mc_opts* user, const HostProgram& H, int tuned_ty, int tun
     }
 }
 
+// Classification work items: each tile column splits along x into segments
+// until there are about eight items per resident warp, so that the last
+// items -- surface columns cost many times constant ones -- end together.  A
+// segment keeps at least four tiles, since its first tile folds the program
+// afresh.
+int pick_xsegments(long long columns, int ntx, long long warps) {
+    if (columns <= 0 || ntx < 8) return 1;
+    const long long want = (8 * warps + columns - 1) / columns;
+    return (int)std::max<long long>(1, std::min<long long>(want, ntx / 4));
+}
+
 mc_opts default_opts(const mc_opts* o) {
     mc_opts r{};
     r.precision = MC_PREC_FP32_FILTERED;
@@ -2300,7 +2317,9 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     if (smem_c > 48 * 1024) CK(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kc, 256, smem_c));
-    long long items = (long long)ca.nty * ca.ntz;
+    const long long cols = (long long)ca.nty * ca.ntz;
+    ca.nxs = pick_xsegments(cols, ca.ntx, 8LL * ctx->sm_count * std::max(occ, 1));
+    long long items = cols * ca.nxs;
     int grid_c = (int)std::max<long long>(1, std::min<long long>((items + 7) / 8, (long long)ctx->sm_count * std::max(occ, 1)));
     kc<<<grid_c, 256, smem_c, sm>>>(g, P, ca);
     CK(cudaGetLastError());
@@ -3299,7 +3318,9 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     ca.ntz = (nz + ca.tz - 1) / ca.tz;
     const size_t smem_c = classify_smem(P);
     if (smem_c > 48 * 1024) return MC_ERR_LIMIT;
-    long long items = (long long)ca.nty * ca.ntz;
+    const long long cols = (long long)ca.nty * ca.ntz;
+    ca.nxs = pick_xsegments(cols, ca.ntx, 8LL * sms * 4);
+    long long items = cols * ca.nxs;
     auto kc = MC_PICK(k_classify, opts.precision, P.has_metaball);
     kc<<<(int)std::max<long long>(1, std::min<long long>((items + 7) / 8, (long long)sms * 4)), 256, smem_c, sm>>>(
         g, P, ca);
