@@ -1934,36 +1934,51 @@ constexpr int kTileY = 8, kTileZ = 4;  // default corner-tile rows (32 x 8 x 4 c
 // Classification tile shape: the caller's, else one row per tile for solids
 // with colliders (a collider row costs a ray query per corner, so the grid
 // needs many small work items to fill the GPU), else the context's tuned or
-// the default shape.
-void pick_tiles(const mc_opts* user, const HostProgram& H, int tuned_ty, int tuned_tz, int ny, int nz, int* ty,
-                int* tz) {
+// the default shape.  `warps` is the launch's resident warps when the columns
+// split along x (pick_xsegments), 0 when they do not.
+void pick_tiles(const mc_opts* user, const HostProgram& H, int tuned_ty, int tuned_tz, int nx, int ny, int nz,
+                long long warps, int* ty, int* tz) {
     const int uy = user ? user->tile_y : 0, uz = user ? user->tile_z : 0;
     const bool fixed = uy > 0 || uz > 0;
     const bool small = !fixed && H.has_collider;
     *ty = uy > 0 ? uy : (small ? 1 : (tuned_ty > 0 ? tuned_ty : kTileY));
     *tz = uz > 0 ? uz : (small ? 1 : (tuned_tz > 0 ? tuned_tz : kTileZ));
     if (!fixed && !small && !H.metas.empty()) {
-        // Metaball corners are costly, so a grid must split into enough tile
-        // columns for every warp: at most sqrt(ny nz) / 25 rows per tile
-        // (measured best: 4 x 2 on 226^3, 4 x 4 on 450^3).
-        static const int cand[5][2] = {{4, 4}, {4, 2}, {2, 2}, {2, 1}, {1, 1}};
-        const double rmax = std::sqrt((double)ny * (double)nz) / 25;
-        int k = 0;
-        while (k < 4 && cand[k][0] * cand[k][1] > rmax) k++;
+        // Metaball corners are costly, so the grid must split into enough
+        // tiles for every warp.  With columns split along x: the largest
+        // shape that gives eight tiles per resident warp (8 x 4 on 450^3,
+        // measured best there; 4 x 2 on 226^3).  Without: at most
+        // sqrt(ny nz) / 25 rows per tile (measured best: 4 x 2 on 226^3,
+        // 4 x 4 on 450^3).
+        static const int cand[6][2] = {{8, 4}, {4, 4}, {4, 2}, {2, 2}, {2, 1}, {1, 1}};
+        int k = warps > 0 ? 0 : 1;
+        if (warps > 0) {
+            const long long ntx = (nx + 31) / 32;
+            auto tiles = [&](int j) {
+                return ntx * ((ny + cand[j][0] - 1) / cand[j][0]) * ((nz + cand[j][1] - 1) / cand[j][1]);
+            };
+            while (k < 5 && tiles(k) < 8 * warps) k++;
+        } else {
+            const double rmax = std::sqrt((double)ny * (double)nz) / 25;
+            while (k < 5 && cand[k][0] * cand[k][1] > rmax) k++;
+        }
         *ty = cand[k][0];
         *tz = cand[k][1];
     }
 }
 
 // Classification work items: each tile column splits along x into segments
-// until there are about eight items per resident warp, so that the last
-// items -- surface columns cost many times constant ones -- end together.  A
-// segment keeps at least four tiles, since its first tile folds the program
-// afresh.
-int pick_xsegments(long long columns, int ntx, long long warps) {
-    if (columns <= 0 || ntx < 8) return 1;
-    const long long want = (8 * warps + columns - 1) / columns;
-    return (int)std::max<long long>(1, std::min<long long>(want, ntx / 4));
+// until there are `per_warp` items per resident warp, so that the last items
+// -- surface columns cost many times constant ones -- end together.  A
+// segment keeps at least `min_tiles` tiles, since its first tile folds the
+// program afresh.  Measured on a 580 x 613 x 606 CSG grid: 16 items per warp
+// in segments of three or more tiles; on a 64-ball metaball grid, where a
+// tile costs far more than a fold, 32 items per warp down to single tiles.
+int pick_xsegments(long long columns, int ntx, long long warps, bool metaball) {
+    if (columns <= 0) return 1;
+    const int per_warp = metaball ? 32 : 16, min_tiles = metaball ? 1 : 3;
+    const long long want = (per_warp * warps + columns - 1) / columns;
+    return (int)std::max<long long>(1, std::min<long long>(want, ntx / min_tiles));
 }
 
 mc_opts default_opts(const mc_opts* o) {
@@ -2306,19 +2321,20 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     ca.xf = ctx->xf.as<float>();
     ca.yf = ctx->yf.as<float>();
     ca.zf = ctx->zf.as<float>();
-    pick_tiles(opts_in, H, ctx->tuned_ty, ctx->tuned_tz, ny, nz, &ca.ty, &ca.tz);
-    ca.ntx = (nx + 31) / 32;
-    ca.nty = (ny + ca.ty - 1) / ca.ty;
-    ca.ntz = (nz + ca.tz - 1) / ca.tz;
-    long long ntiles = (long long)ca.ntx * ca.nty * ca.ntz;
-    st.tiles = ntiles;
     const size_t smem_c = classify_smem(P);
     auto kc = MC_PICK(k_classify, opts.precision, P.has_metaball);
     if (smem_c > 48 * 1024) CK(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kc, 256, smem_c));
+    const long long warps_c = 8LL * ctx->sm_count * std::max(occ, 1);
+    pick_tiles(opts_in, H, ctx->tuned_ty, ctx->tuned_tz, nx, ny, nz, warps_c, &ca.ty, &ca.tz);
+    ca.ntx = (nx + 31) / 32;
+    ca.nty = (ny + ca.ty - 1) / ca.ty;
+    ca.ntz = (nz + ca.tz - 1) / ca.tz;
+    long long ntiles = (long long)ca.ntx * ca.nty * ca.ntz;
+    st.tiles = ntiles;
     const long long cols = (long long)ca.nty * ca.ntz;
-    ca.nxs = pick_xsegments(cols, ca.ntx, 8LL * ctx->sm_count * std::max(occ, 1));
+    ca.nxs = pick_xsegments(cols, ca.ntx, warps_c, P.has_metaball);
     long long items = cols * ca.nxs;
     int grid_c = (int)std::max<long long>(1, std::min<long long>((items + 7) / 8, (long long)ctx->sm_count * std::max(occ, 1)));
     kc<<<grid_c, 256, smem_c, sm>>>(g, P, ca);
@@ -2862,7 +2878,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             J.P = jobs[i].solid->view;
             J.ca.prec = pl->prec;
             J.ca.cull = opts.cull;
-            pick_tiles(opts_in, jobs[i].solid->host, ctx->tuned_ty, ctx->tuned_tz, ny, nz, &J.ca.ty, &J.ca.tz);
+            pick_tiles(opts_in, jobs[i].solid->host, ctx->tuned_ty, ctx->tuned_tz, nx, ny, nz, 0, &J.ca.ty, &J.ca.tz);
             J.ca.ntx = (nx + 31) / 32;
             J.ca.nty = (ny + J.ca.ty - 1) / J.ca.ty;
             J.ca.ntz = (nz + J.ca.tz - 1) / J.ca.tz;
@@ -3312,14 +3328,14 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     ca.xf = (const float*)up[12].dst;
     ca.yf = (const float*)up[13].dst;
     ca.zf = (const float*)up[14].dst;
-    pick_tiles(&opts, H, 0, 0, ny, nz, &ca.ty, &ca.tz);
+    pick_tiles(&opts, H, 0, 0, nx, ny, nz, 8LL * sms * 4, &ca.ty, &ca.tz);
     ca.ntx = (nx + 31) / 32;
     ca.nty = (ny + ca.ty - 1) / ca.ty;
     ca.ntz = (nz + ca.tz - 1) / ca.tz;
     const size_t smem_c = classify_smem(P);
     if (smem_c > 48 * 1024) return MC_ERR_LIMIT;
     const long long cols = (long long)ca.nty * ca.ntz;
-    ca.nxs = pick_xsegments(cols, ca.ntx, 8LL * sms * 4);
+    ca.nxs = pick_xsegments(cols, ca.ntx, 8LL * sms * 4, P.has_metaball);
     long long items = cols * ca.nxs;
     auto kc = MC_PICK(k_classify, opts.precision, P.has_metaball);
     kc<<<(int)std::max<long long>(1, std::min<long long>((items + 7) / 8, (long long)sms * 4)), 256, smem_c, sm>>>(
