@@ -1054,34 +1054,74 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t* blocksum, 
 }
 
 // Per-chunk exclusive offsets (vertex, triangle) as two u32 arrays; one
-// block per kChunksPerBlock chunks, eight 256-wide scans with a carry.
+// block per kChunksPerBlock chunks.  Thread t takes the eight consecutive
+// chunks base + 8t .. base + 8t + 7 (two 16-byte loads and stores per array
+// when all eight exist and the arrays are 16-byte aligned), then a warp
+// shuffle scan and one pass over the eight warp totals: one barrier a block.
 __global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* packed, const unsigned long long* blockoff,
                                                      long long nchunks, uint32_t* prefv, uint32_t* preft) {
-    __shared__ uint32_t sv[256], st[256];
-    const int t = threadIdx.x;
-    const long long base = (long long)blockIdx.x * kChunksPerBlock;
-    unsigned long long cv = blockoff[2 * blockIdx.x], ct = blockoff[2 * blockIdx.x + 1];
-    for (int k = 0; k < kChunksPerBlock / 256; k++) {
-        const long long i = base + k * 256 + t;
-        const uint32_t p = i < nchunks ? packed[i] : 0;
-        const uint32_t v = (p & 63u) + ((p >> 6) & 63u) + ((p >> 12) & 63u), w = p >> 18;
-        sv[t] = v;
-        st[t] = w;
-        __syncthreads();
-        for (int o = 1; o < 256; o <<= 1) {
-            const uint32_t av = t >= o ? sv[t - o] : 0, aw = t >= o ? st[t - o] : 0;
-            __syncthreads();
-            sv[t] += av;
-            st[t] += aw;
-            __syncthreads();
+    __shared__ uint32_t wsv[8], wst[8];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const long long i0 = (long long)blockIdx.x * kChunksPerBlock + 8 * t;
+    const bool vec = i0 + 8 <= nchunks &&
+                     ((reinterpret_cast<uintptr_t>(packed) | reinterpret_cast<uintptr_t>(prefv) |
+                       reinterpret_cast<uintptr_t>(preft)) & 15u) == 0;
+    uint32_t p[8];
+    if (vec) {
+        const uint4 a = *reinterpret_cast<const uint4*>(packed + i0);
+        const uint4 b = *reinterpret_cast<const uint4*>(packed + i0 + 4);
+        p[0] = a.x, p[1] = a.y, p[2] = a.z, p[3] = a.w, p[4] = b.x, p[5] = b.y, p[6] = b.z, p[7] = b.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) p[k] = i0 + k < nchunks ? packed[i0 + k] : 0u;
+    }
+    uint32_t ev[8], et[8], sv = 0, st = 0;  // exclusive within the thread
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        ev[k] = sv;
+        et[k] = st;
+        sv += (p[k] & 63u) + ((p[k] >> 6) & 63u) + ((p[k] >> 12) & 63u);
+        st += p[k] >> 18;
+    }
+    uint32_t iv = sv, it = st;  // inclusive within the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t av = __shfl_up_sync(0xffffffffu, iv, o), at = __shfl_up_sync(0xffffffffu, it, o);
+        if (lane >= o) {
+            iv += av;
+            it += at;
         }
-        if (i < nchunks) {
-            prefv[i] = (uint32_t)(cv + sv[t] - v);
-            preft[i] = (uint32_t)(ct + st[t] - w);
-        }
-        cv += sv[255];
-        ct += st[255];
-        __syncthreads();
+    }
+    if (lane == 31) {
+        wsv[w] = iv;
+        wst[w] = it;
+    }
+    __syncthreads();
+    uint32_t bv = 0, bt = 0;
+    for (int k = 0; k < w; k++) {
+        bv += wsv[k];
+        bt += wst[k];
+    }
+    const unsigned long long cv = blockoff[2 * blockIdx.x] + bv + (iv - sv);
+    const unsigned long long ct = blockoff[2 * blockIdx.x + 1] + bt + (it - st);
+    uint32_t ov[8], ot[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        ov[k] = (uint32_t)(cv + ev[k]);
+        ot[k] = (uint32_t)(ct + et[k]);
+    }
+    if (vec) {
+        *reinterpret_cast<uint4*>(prefv + i0) = make_uint4(ov[0], ov[1], ov[2], ov[3]);
+        *reinterpret_cast<uint4*>(prefv + i0 + 4) = make_uint4(ov[4], ov[5], ov[6], ov[7]);
+        *reinterpret_cast<uint4*>(preft + i0) = make_uint4(ot[0], ot[1], ot[2], ot[3]);
+        *reinterpret_cast<uint4*>(preft + i0 + 4) = make_uint4(ot[4], ot[5], ot[6], ot[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (i0 + k < nchunks) {
+                prefv[i0 + k] = ov[k];
+                preft[i0 + k] = ot[k];
+            }
     }
 }
 
