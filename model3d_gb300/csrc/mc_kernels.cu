@@ -1058,8 +1058,11 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t* blocksum, 
 // chunks base + 8t .. base + 8t + 7 (two 16-byte loads and stores per array
 // when all eight exist and the arrays are 16-byte aligned), then a warp
 // shuffle scan and one pass over the eight warp totals: one barrier a block.
+// With `list`, the indices of the chunks with a nonzero count are appended
+// to it (one atomic per warp on *n_list; order between warps is arbitrary).
 __global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* packed, const unsigned long long* blockoff,
-                                                     long long nchunks, uint32_t* prefv, uint32_t* preft) {
+                                                     long long nchunks, uint32_t* prefv, uint32_t* preft,
+                                                     uint32_t* list = nullptr, unsigned long long* n_list = nullptr) {
     __shared__ uint32_t wsv[8], wst[8];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const long long i0 = (long long)blockIdx.x * kChunksPerBlock + 8 * t;
@@ -1074,6 +1077,25 @@ __global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* packed, con
     } else {
 #pragma unroll
         for (int k = 0; k < 8; k++) p[k] = i0 + k < nchunks ? packed[i0 + k] : 0u;
+    }
+    if (list) {
+        uint32_t f = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) f |= (p[k] != 0u ? 1u : 0u) << k;
+        const uint32_t cnt = __popc(f);
+        uint32_t inc = cnt;  // inclusive within the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t a = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += a;
+        }
+        unsigned long long wbase = 0;
+        if (lane == 31 && inc) wbase = atomicAdd(n_list, (unsigned long long)inc);
+        wbase = __shfl_sync(0xffffffffu, wbase, 31);
+        unsigned long long pos = wbase + (inc - cnt);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if ((f >> k) & 1u) list[pos++] = (uint32_t)(i0 + k);
     }
     uint32_t ev[8], et[8], sv = 0, st = 0;  // exclusive within the thread
 #pragma unroll
@@ -1231,6 +1253,14 @@ __device__ __forceinline__ void emit_chunk(const GridView& g, const EmitArgs& a,
 __global__ void __launch_bounds__(256) k_emit(GridView g, EmitArgs a) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < a.nchunks) emit_chunk(g, a, i, 0u);
+}
+
+// The same over the list of non-empty chunks from k_scan_chunks: about one
+// chunk in twenty has a crossed edge, so every lane of a warp now emits
+// instead of a few.  Outputs go where the prefix arrays say, in any order.
+__global__ void __launch_bounds__(256) k_emit_list(GridView g, EmitArgs a, const uint32_t* list, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) emit_chunk(g, a, (long long)list[i], 0u);
 }
 
 // ------------------------------------------------------------ k_search
@@ -1930,10 +1960,11 @@ struct mc_ctx {
     long long chunk_end[kCopyChunks] = {};
     std::string err;
     DevBuf xs, ys, zs, xf, yf, zf, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
+    DevBuf nonempty;  // indices of the chunks with crossed edges (k_scan_chunks -> k_emit_list)
     DevBuf pts, pout;
     DevBuf inner, xsteps, stl;  // interior points of the last search; steps of mc_result_transform; STL bytes
     bool has_interior = false;
-    unsigned long long* h_pin = nullptr;  // pinned: totals[2], stats[ST_N], errs (as ints) ...
+    unsigned long long* h_pin = nullptr;  // pinned: [0, 2) totals, [2, 4) errs (as ints), [4] non-empty chunks, [8, 8 + ST_N) stats
     // Device buffers of destroyed solids, reused by the next mc_solid_create
     // (stream order makes reuse safe without a synchronisation).  Solids may
     // be destroyed from another thread than the context's, hence the lock.
@@ -2125,7 +2156,7 @@ void mc_destroy(mc_ctx* ctx) {
     ctx->plan.reset();
     for (DevBuf* b : {&ctx->xs, &ctx->ys, &ctx->zs, &ctx->xf, &ctx->yf, &ctx->zf, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
                       &ctx->prefv, &ctx->preft, &ctx->keys, &ctx->verts, &ctx->tris, &ctx->stats, &ctx->errs,
-                      &ctx->totals, &ctx->pts, &ctx->pout, &ctx->inner, &ctx->xsteps, &ctx->stl})
+                      &ctx->totals, &ctx->nonempty, &ctx->pts, &ctx->pout, &ctx->inner, &ctx->xsteps, &ctx->stl})
         b->release();
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -2340,7 +2371,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     CK(ctx->zs.ensure(nz * 8));
     CK(ctx->stats.ensure(ST_N * 8));
     CK(ctx->errs.ensure(ER_N * 4));
-    CK(ctx->totals.ensure(16));
+    CK(ctx->totals.ensure(24));  // vertices, triangles, non-empty chunks
     CK(cudaMemcpyAsync(ctx->xs.p, X.data(), nx * 8, cudaMemcpyHostToDevice, sm));
     CK(cudaMemcpyAsync(ctx->ys.p, Y.data(), ny * 8, cudaMemcpyHostToDevice, sm));
     CK(cudaMemcpyAsync(ctx->zs.p, Z.data(), nz * 8, cudaMemcpyHostToDevice, sm));
@@ -2353,7 +2384,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     CK(cudaMemcpyAsync(ctx->zf.p, ZF.data(), nz * 4, cudaMemcpyHostToDevice, sm));
     CK(cudaMemsetAsync(ctx->stats.p, 0, ST_N * 8, sm));
     CK(cudaMemsetAsync(ctx->errs.p, 0, ER_N * 4, sm));
-    CK(cudaMemsetAsync(ctx->totals.p, 0, 16, sm));
+    CK(cudaMemsetAsync(ctx->totals.p, 0, 24, sm));
     g.xs = ctx->xs.as<double>();
     g.ys = ctx->ys.as<double>();
     g.zs = ctx->zs.as<double>();
@@ -2396,13 +2427,13 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
 
     long long nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)g.CX * (ny - 1) * (nz - 1) : 0;
     const int nblk = (int)((nchunks + kChunksPerBlock - 1) / kChunksPerBlock);
-    const int egrid = (int)((nchunks + 255) / 256);
     if (nchunks > 0) {
         CK(ctx->packed.ensure(nchunks * 4));
         CK(ctx->blocksum.ensure((size_t)nblk * 8));
         CK(ctx->blockoff.ensure((size_t)nblk * 16));
         CK(ctx->prefv.ensure(nchunks * 4));
         CK(ctx->preft.ensure(nchunks * 4));
+        CK(ctx->nonempty.ensure(nchunks * 4));
         CountArgs cn{ctx->bits.as<uint32_t>(), ctx->packed.as<uint32_t>(), ctx->blocksum.as<uint32_t>(), nchunks};
         k_count<<<nblk, 256, 0, sm>>>(g, cn);
         CK(cudaGetLastError());
@@ -2410,13 +2441,15 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
                                           ctx->totals.as<unsigned long long>());
         CK(cudaGetLastError());
         k_scan_chunks<<<nblk, 256, 0, sm>>>(ctx->packed.as<uint32_t>(), ctx->blockoff.as<unsigned long long>(),
-                                            nchunks, ctx->prefv.as<uint32_t>(), ctx->preft.as<uint32_t>());
+                                            nchunks, ctx->prefv.as<uint32_t>(), ctx->preft.as<uint32_t>(),
+                                            ctx->nonempty.as<uint32_t>(), ctx->totals.as<unsigned long long>() + 2);
         CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ctx->ev[6], sm));
     unsigned long long* hp = ctx->h_pin;
     CK(cudaMemcpyAsync(hp, ctx->totals.p, 16, cudaMemcpyDeviceToHost, sm));
     CK(cudaMemcpyAsync(hp + 2, ctx->errs.p, ER_N * 4, cudaMemcpyDeviceToHost, sm));
+    CK(cudaMemcpyAsync(hp + 4, ctx->totals.as<unsigned long long>() + 2, 8, cudaMemcpyDeviceToHost, sm));
     CK(cudaStreamSynchronize(sm));
     const int* herr = (const int*)(hp + 2);
     if (herr[ER_BORDER]) return fail(ctx, MC_ERR_BOUNDS_INSIDE, "solid is true outside of bounds");
@@ -2432,7 +2465,8 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     if (nchunks > 0 && (V > 0 || T > 0)) {
         EmitArgs ea{ctx->bits.as<uint32_t>(), ctx->packed.as<uint32_t>(), ctx->prefv.as<uint32_t>(),
                     ctx->preft.as<uint32_t>(), ctx->keys.as<unsigned long long>(), ctx->tris.as<int32_t>(), nchunks};
-        k_emit<<<egrid, 256, 0, sm>>>(g, ea);
+        const long long n_ne = std::min<long long>((long long)hp[4], nchunks);
+        if (n_ne > 0) k_emit_list<<<(int)((n_ne + 255) / 256), 256, 0, sm>>>(g, ea, ctx->nonempty.as<uint32_t>(), n_ne);
         CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ctx->ev[3], sm));
