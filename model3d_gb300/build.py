@@ -52,7 +52,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v" if verbose else "-O3",
          "-c", cu, "-o", cu_o],
-        ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-Wall",
+        ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-Wall", "-pthread",
          "-c", cpp, "-o", cpp_o],
     ]
 
@@ -67,7 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if verbose:
         sys.stderr.write("".join(logs))
     tmp = OUT + ".tmp"
-    run([nvcc, ARCH, "-shared", "-cudart", "static", cu_o, cpp_o, "-o", tmp])
+    run([nvcc, ARCH, "-shared", "-cudart", "static", cu_o, cpp_o, "-lpthread", "-o", tmp])
     os.replace(tmp, OUT)
     return OUT
 

@@ -18,6 +18,8 @@
 #include <limits>
 #include <map>
 #include <stdexcept>
+#include <system_error>
+#include <thread>
 
 namespace mcgpu {
 namespace {
@@ -168,10 +170,9 @@ struct Tri {
     D3 mn, mx;
 };
 
-struct Flagged {
+struct GItem {
+    D3 mn, mx;
     int idx;
-    D3 mn, mx, md;
-    bool flag;
 };
 
 double bounds_area(D3 mn, D3 mx) {  // bvh.go:289-292
@@ -179,63 +180,105 @@ double bounds_area(D3 mn, D3 mx) {  // bvh.go:289-292
     return 2 * (d.v[0] * (d.v[1] + d.v[2]) + d.v[1] * d.v[2]);
 }
 
-double multi_area(Flagged* const* b, size_t n) {  // bvh.go:257-287
-    D3 mn = b[0]->mn, mx = b[0]->mx;
+double multi_area(const GItem* b, size_t n) {  // bvh.go:257-287
+    D3 mn = b[0].mn, mx = b[0].mx;
     for (size_t i = 1; i < n; i++)
         for (int a = 0; a < 3; a++) {
-            if (b[i]->mn.v[a] < mn.v[a]) mn.v[a] = b[i]->mn.v[a];
-            if (b[i]->mx.v[a] > mx.v[a]) mx.v[a] = b[i]->mx.v[a];
+            if (b[i].mn.v[a] < mn.v[a]) mn.v[a] = b[i].mn.v[a];
+            if (b[i].mx.v[a] > mx.v[a]) mx.v[a] = b[i].mx.v[a];
         }
     return bounds_area(mn, mx);
 }
 
-// groupBounders (model3d/bvh.go:135-217); ties in the sorts keep input order.
-void group_rec(std::vector<Flagged*>* s, int* out) {
-    size_t n = s[0].size();
-    if (n <= 2) {
-        for (size_t i = 0; i < n; i++) out[i] = s[0][i]->idx;
-        return;
-    }
-    size_t mid = n / 2;
-    int axis = 0;
-    double best = multi_area(s[0].data(), mid) + multi_area(s[0].data() + mid, n - mid);
-    for (int a = 1; a < 3; a++) {
-        double v = multi_area(s[a].data(), mid) + multi_area(s[a].data() + mid, n - mid);
-        if (v < best) {
-            best = v;
-            axis = a;
+// groupBounders (model3d/bvh.go:135-217).  s[a] holds every item sorted by
+// its midpoint along axis a (ties keep input order); a call on the range
+// [lo, lo + n) picks the split axis, then stably partitions the two other
+// axes' ranges into the lower and upper halves, so that each half's range
+// stays sorted along every axis.  No allocation per call.  The two halves
+// touch disjoint ranges of s, tmp and out and disjoint items of `lower`, so
+// the upper levels run them on two threads; the result does not depend on it.
+struct Grouper {
+    std::vector<GItem> s[3];
+    std::vector<uint8_t> lower;  // by item index: in the lower half of the split being made
+    std::vector<GItem> tmp;      // partition scratch, indexed like s
+
+    void rec(size_t lo, size_t n, int* out, int spawn_depth) {
+        if (n <= 2) {
+            for (size_t i = 0; i < n; i++) out[i] = s[0][lo + i].idx;
+            return;
         }
-    }
-    for (size_t i = 0; i < n; i++) s[axis][i]->flag = i < mid;
-    std::vector<Flagged*> lo[3], hi[3];
-    for (int a = 0; a < 3; a++) {
-        if (a == axis) {
-            lo[a].assign(s[a].begin(), s[a].begin() + mid);
-            hi[a].assign(s[a].begin() + mid, s[a].end());
-        } else {
-            lo[a].reserve(mid);
-            hi[a].reserve(n - mid);
-            for (Flagged* f : s[a]) (f->flag ? lo[a] : hi[a]).push_back(f);
+        const size_t mid = n / 2;
+        int axis = 0;
+        double best = multi_area(&s[0][lo], mid) + multi_area(&s[0][lo + mid], n - mid);
+        for (int a = 1; a < 3; a++) {
+            double v = multi_area(&s[a][lo], mid) + multi_area(&s[a][lo + mid], n - mid);
+            if (v < best) {
+                best = v;
+                axis = a;
+            }
         }
-        std::vector<Flagged*>().swap(s[a]);
+        for (size_t i = 0; i < n; i++) lower[s[axis][lo + i].idx] = i < mid;
+        for (int a = 0; a < 3; a++) {
+            if (a == axis) continue;
+            GItem* v = &s[a][lo];
+            GItem* w = &tmp[lo];
+            size_t k = 0, m = 0;
+            for (size_t i = 0; i < n; i++) {
+                if (lower[v[i].idx]) v[k++] = v[i];
+                else w[m++] = v[i];
+            }
+            std::copy(w, w + m, v + k);
+        }
+        std::thread upper;
+        if (spawn_depth > 0 && n >= kParallelGroup) {
+            try {
+                upper = std::thread([=] { rec(lo + mid, n - mid, out + mid, spawn_depth - 1); });
+            } catch (const std::system_error&) {
+                // no thread to be had: the caller's thread does both halves
+            }
+        }
+        rec(lo, mid, out, upper.joinable() ? spawn_depth - 1 : 0);
+        if (upper.joinable()) upper.join();
+        else rec(lo + mid, n - mid, out + mid, 0);
     }
-    group_rec(lo, out);
-    group_rec(hi, out + mid);
-}
+    static constexpr size_t kParallelGroup = 1 << 16;
+};
 
 std::vector<int> group_triangles(const std::vector<Tri>& t) {  // GroupTriangles, bvh.go:118-133
-    std::vector<Flagged> f(t.size());
-    for (size_t i = 0; i < t.size(); i++)
-        f[i] = {(int)i, t[i].mn, t[i].mx, vscale(vadd(t[i].mn, t[i].mx), 0.5), false};
-    std::vector<Flagged*> s[3];
-    for (int a = 0; a < 3; a++) {
-        s[a].resize(f.size());
-        for (size_t i = 0; i < f.size(); i++) s[a][i] = &f[i];
-        std::stable_sort(s[a].begin(), s[a].end(),
-                         [a](const Flagged* x, const Flagged* y) { return x->md.v[a] < y->md.v[a]; });
+    const size_t n = t.size();
+    std::vector<int> out(n);
+    if (n == 0) return out;
+    Grouper g;
+    // The three axes' orders are independent: one thread each for large sets.
+    auto sort_axis = [&](int a) {
+        std::vector<std::pair<double, int>> key(n);
+        for (size_t i = 0; i < n; i++) key[i] = {vscale(vadd(t[i].mn, t[i].mx), 0.5).v[a], (int)i};
+        std::stable_sort(key.begin(), key.end(),
+                         [](const std::pair<double, int>& x, const std::pair<double, int>& y) { return x.first < y.first; });
+        g.s[a].reserve(n);
+        for (size_t i = 0; i < n; i++) {
+            const Tri& tr = t[key[i].second];
+            g.s[a].push_back(GItem{tr.mn, tr.mx, key[i].second});
+        }
+    };
+    std::thread th[2];
+    for (int a = 1; a < 3 && n >= Grouper::kParallelGroup; a++) {
+        try {
+            th[a - 1] = std::thread(sort_axis, a);
+        } catch (const std::system_error&) {
+        }
     }
-    std::vector<int> out(t.size());
-    if (!t.empty()) group_rec(s, out.data());
+    sort_axis(0);
+    for (int a = 1; a < 3; a++) {
+        if (th[a - 1].joinable()) th[a - 1].join();
+        else sort_axis(a);
+    }
+    g.lower.assign(n, 0);
+    g.tmp.resize(n);
+    const unsigned hw = std::thread::hardware_concurrency();
+    int depth = 0;  // 2^depth threads at the deepest split level, up to the host's threads
+    while (depth < 5 && (2u << depth) <= std::max(1u, hw)) depth++;
+    g.rec(0, n, out.data(), depth);
     return out;
 }
 
@@ -248,7 +291,7 @@ struct BNode {
 
 struct TreeBuilder {
     const std::vector<Tri>& tris;
-    std::vector<BNode> nodes;
+    std::vector<BNode> nodes;  // reserve n - 1 before build(): one node per pair merged
     // Returns a child reference: node index, or -(tri+1).
     int build(const int* order, size_t n) {  // GroupedTrianglesToCollider, collisions.go:169-181
         if (n == 1) return -(order[0] + 1);
@@ -262,7 +305,8 @@ struct TreeBuilder {
         j.mx = vmax3(j.mx, bounds_max(c2));
         for (int c : {c1, c2}) {
             if (c >= 0 && veq(nodes[c].mn, j.mn) && veq(nodes[c].mx, j.mx)) {
-                std::vector<int> cc = nodes[c].ch;
+                // Absorbed: nothing refers to node c afterwards, so its list moves.
+                std::vector<int> cc = std::move(nodes[c].ch);
                 j.ch.insert(j.ch.end(), cc.begin(), cc.end());
             } else {
                 j.ch.push_back(c);
@@ -375,6 +419,11 @@ void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, in
         *c1 = std::min(n - 1, (int)std::floor((hi - org) * inv + 0.05));
     };
     const size_t ncell = (size_t)ga * gb;
+    // Each cell lists its boxes by (maxt, triangle), a strict order (a box
+    // enters a cell once).  Filling the cells from the boxes in that order
+    // leaves every cell sorted without a sort per cell.
+    std::sort(boxes.begin(), boxes.end(),
+              [](const Box& x, const Box& y) { return x.maxt < y.maxt || (x.maxt == y.maxt && x.tri < y.tri); });
     std::vector<int64_t> cnt(ncell + 1, 0);
     for (const Box& b : boxes) {
         int a0, a1, b0, b1;
@@ -396,9 +445,6 @@ void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, in
         for (int y = b0; y <= b1; y++)
             for (int x = a0; x <= a1; x++) P->ents[base + fill[(size_t)y * ga + x]++] = RayEnt{b.maxt, b.tri};
     }
-    for (size_t c = 0; c < ncell; c++)
-        std::sort(P->ents.begin() + base + cnt[c], P->ents.begin() + base + cnt[c + 1],
-                  [](const RayEnt& x, const RayEnt& y) { return x.maxt < y.maxt || (x.maxt == y.maxt && x.tri < y.tri); });
     tree->cell_base = (int32_t)P->cell_start.size();
     tree->n_cells = (int32_t)ncell;
     for (size_t c = 0; c <= ncell; c++) P->cell_start.push_back((int32_t)(base + cnt[c]));
@@ -730,6 +776,8 @@ struct Lowerer {
         }
         TreeD tree{};
         int tri_base = (int)P->tris.size();
+        P->tris.reserve(P->tris.size() + order.size());
+        P->tris_f.reserve(P->tris_f.size() + order.size());
         // Triangle records in grouped order (traversal locality).
         std::vector<int> pos_of(ts.n);
         for (size_t i = 0; i < order.size(); i++) pos_of[order[i]] = (int)i;
@@ -766,6 +814,7 @@ struct Lowerer {
         P->tri_parent.resize(P->tris.size(), -1);
         if (ts.n > 1) {
             TreeBuilder tb{t, {}};
+            tb.nodes.reserve(order.size() - 1);
             int root = tb.build(order.data(), order.size());
             int node_base = (int)P->nodes.size();
             // Breadth-first order keeps the upper levels together.
