@@ -241,6 +241,8 @@ typedef struct mc_program_info {
     double threshold;     /* f(radiusThreshold) of the first metaball, as the library computed it */
     double root_min[3];
     double root_max[3];
+    uint64_t digest;      /* FNV-1a over the 64-bit words of every array of the lowered program, in a
+                             fixed order: changes exactly when the bytes uploaded to the device change */
 } mc_program_info;
 mc_status mc_program_check(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets, size_t n_sets,
                            mc_program_info* info, char* err, size_t err_cap);

@@ -43,7 +43,8 @@ EXPORTS = [
 class MCProgramInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int64) for n in (
         "n_ops", "n_leaves", "n_metaballs", "n_balls", "n_boxes", "n_colliders", "max_stack")] + [
-        ("threshold", ctypes.c_double), ("root_min", ctypes.c_double * 3), ("root_max", ctypes.c_double * 3)]
+        ("threshold", ctypes.c_double), ("root_min", ctypes.c_double * 3), ("root_max", ctypes.c_double * 3),
+        ("digest", ctypes.c_uint64)]
 
 
 class MCStats(ctypes.Structure):

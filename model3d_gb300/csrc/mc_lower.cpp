@@ -1233,6 +1233,68 @@ int build_case_table(uint8_t counts[256], uint8_t tris[256][5][6]) {
 
 }  // namespace mcgpu
 
+namespace {
+
+// FNV-1a (64-bit offset basis and prime) over little-endian 64-bit words;
+// a tail shorter than a word is zero-padded.  The length goes in first, so
+// adjacent arrays cannot trade bytes.
+struct Digest {
+    uint64_t h = 1469598103934665603ull;
+    void word(uint64_t w) { h = (h ^ w) * 1099511628211ull; }
+    void bytes(const void* p, size_t n) {
+        word(n);
+        const unsigned char* b = (const unsigned char*)p;
+        size_t i = 0;
+        for (; i + 8 <= n; i += 8) {
+            uint64_t w;
+            std::memcpy(&w, b + i, 8);
+            word(w);
+        }
+        if (i < n) {
+            uint64_t w = 0;
+            std::memcpy(&w, b + i, n - i);
+            word(w);
+        }
+    }
+    template <class T>
+    void vec(const std::vector<T>& v) { bytes(v.data(), v.size() * sizeof(T)); }
+};
+
+uint64_t program_digest(const mcgpu::HostProgram& P) {
+    Digest d;
+    d.vec(P.ops);
+    d.vec(P.ops_allfalse);
+    d.word((uint64_t)(int64_t)P.n_ops_allfalse);
+    d.word((uint64_t)(int64_t)P.fold_cap);
+    d.vec(P.leaf_kind);
+    d.vec(P.leaf_d);
+    d.vec(P.leaf_f);
+    d.vec(P.cull);
+    d.vec(P.cull_f);
+    d.vec(P.xbox);
+    d.vec(P.xstep);
+    d.vec(P.trees);
+    d.vec(P.nodes);
+    d.vec(P.nodes_f);
+    d.vec(P.tri_parent);
+    d.vec(P.cell_start);
+    d.vec(P.ents);
+    d.vec(P.tris);
+    d.vec(P.tris_f);
+    d.vec(P.metas);
+    d.vec(P.metas_f);
+    d.vec(P.balls);
+    d.vec(P.balls_f);
+    d.bytes(P.root_min, sizeof P.root_min);
+    d.bytes(P.root_max, sizeof P.root_max);
+    d.word((uint64_t)(int64_t)P.max_stack);
+    d.word((uint64_t)(int64_t)P.max_xdepth);
+    d.word((uint64_t)P.has_collider | (uint64_t)P.has_transform << 1);
+    return d.h;
+}
+
+}  // namespace
+
 extern "C" mc_status mc_program_check(const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets,
                                       size_t n_sets, mc_program_info* info, char* err, size_t err_cap) {
     using namespace mcgpu;
@@ -1267,6 +1329,7 @@ extern "C" mc_status mc_program_check(const mc_node* nodes, size_t n_nodes, cons
             info->root_min[i] = P.root_min[i];
             info->root_max[i] = P.root_max[i];
         }
+        info->digest = program_digest(P);
     }
     return MC_OK;
 }

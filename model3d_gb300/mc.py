@@ -108,6 +108,7 @@ def check_program(solid: Solid) -> dict:
     out = {n: getattr(info, n) for n, _ in N.MCProgramInfo._fields_[:7]}
     out["threshold"] = info.threshold
     out["root_min"], out["root_max"] = list(info.root_min), list(info.root_max)
+    out["digest"] = "%016x" % info.digest
     return out
 
 

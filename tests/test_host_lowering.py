@@ -151,3 +151,30 @@ def test_user_defined_solids_are_not_lowerable():
         check_program(Custom())
     with pytest.raises(NotLowerable):
         check_program(JoinedSolid([Sphere(XYZ(0, 0, 0), 1), Custom()]))
+
+
+def test_lowering_matches_golden_digests():
+    """Every array of the lowered program is byte-identical to the lowering
+    that the GPU parity tests passed with (tests/golden/lowering.json, made by
+    tests/golden/make_lowering_golden.py)."""
+    import json
+    import os
+    import sys
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, here)
+    import make_lowering_golden as G
+    gold = json.load(open(os.path.join(here, "lowering.json")))
+    assert G.digests() == gold
+
+
+def test_digest_follows_every_byte():
+    """One ulp in one parameter, or one triangle moved, changes the digest."""
+    import math
+    a = check_program(Sphere(XYZ(0, 0, 0), 1.0))["digest"]
+    assert check_program(Sphere(XYZ(0, 0, 0), 1.0))["digest"] == a
+    assert check_program(Sphere(XYZ(0, 0, 0), math.nextafter(1.0, 2.0)))["digest"] != a
+    tris = icosphere_triangles(4)
+    d0 = check_program(NewColliderSolid(MeshToCollider(tris)))["digest"]
+    moved = tris.copy()
+    moved[7, 4] = math.nextafter(moved[7, 4], 9.0)
+    assert check_program(NewColliderSolid(MeshToCollider(moved)))["digest"] != d0
