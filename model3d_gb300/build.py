@@ -67,7 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if verbose:
         sys.stderr.write("".join(logs))
     tmp = OUT + ".tmp"
-    run([nvcc, ARCH, "-shared", "-cudart", "static", cu_o, cpp_o, "-lpthread", "-o", tmp])
+    run([nvcc, ARCH, "-shared", "-cudart", "static", cu_o, cpp_o, "-o", tmp])
     os.replace(tmp, OUT)
     return OUT
 
