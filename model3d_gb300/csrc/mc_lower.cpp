@@ -319,6 +319,32 @@ struct TreeBuilder {
     D3 bounds_max(int c) { return c >= 0 ? nodes[c].mx : tris[-c - 1].mx; }
 };
 
+// f(lo, hi) over contiguous chunks of [0, n) on up to 16 host threads, at
+// least min_per_thread items a chunk; the caller's thread takes the first
+// chunk, and runs any chunk whose thread cannot be created.  Chunks must
+// touch disjoint data.
+template <class F>
+void parallel_chunks(size_t n, size_t min_per_thread, F&& f) {
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t T = std::min<size_t>({hw, 16, n / std::max<size_t>(min_per_thread, 1)});
+    if (T <= 1) {
+        f((size_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(T);
+    for (size_t k = 1; k < T; k++) {
+        const size_t lo = n * k / T, hi = n * (k + 1) / T;
+        try {
+            th.emplace_back([&f, lo, hi] { f(lo, hi); });
+        } catch (const std::system_error&) {
+            f(lo, hi);
+        }
+    }
+    f((size_t)0, n / T);
+    for (std::thread& x : th) x.join();
+}
+
 // ---------------------------------------------------------------- ray grid
 
 // Cells and entries of one tree's ray grid (layout and exactness argument at
@@ -340,52 +366,69 @@ void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, in
         float maxt;
         int tri;
     };
+    // Per triangle (position i of the grouped order), on host threads: 0 never
+    // hit, 1 a box, 2 tested by every ray, 3 tested by every ray but its
+    // extent still counts towards the cell size.  Then boxes, `all` and the
+    // extents are collected in triangle order.
+    const size_t n = order.size();
+    std::vector<Box> cand(n);
+    std::vector<uint8_t> kind(n, 0);
+    std::vector<double> extent(n, 0.0);
+    parallel_chunks(n, 16384, [&](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; i++) {
+            if (!P->tris[tri_base + i].valid) continue;  // parallel or det == 0: never hit
+            const Tri& tr = t[order[i]];
+            const D3 v1 = vsub(tr.p[1], tr.p[0]), v2 = vsub(tr.p[2], tr.p[0]);
+            const double det = std::fabs(vdot(vcross(kRay, v2), v1));
+            const double k1 = vnorm(v1) * vnorm(v2) * dlen / det;
+            double k2 = 0;
+            for (int e = 0; e < 3; e++) {
+                const D3 ev = vsub(tr.p[(e + 1) % 3], tr.p[e]);
+                const D3 perp = vsub(ev, vscale(dh, vdot(ev, dh)));
+                const double nv = vnorm(ev), np = vnorm(perp);
+                if (nv > 0) k2 = std::max(k2, nv / np);
+            }
+            if (!(7 * eps * k1 <= 1e-3) || !std::isfinite(k2)) {
+                kind[i] = 2;
+                continue;
+            }
+            const double pad = (R + 1) * (4e-6 + 1e3 * eps * (k1 + k2));
+            Box b{DBL_MAX, -DBL_MAX, DBL_MAX, -DBL_MAX, 0.f, tri_base + (int)i};
+            double mt = -DBL_MAX;
+            for (int k = 0; k < 3; k++) {
+                const D3& v = tr.p[k];
+                const double a = v.v[1] - RAYGRID_KY * v.v[0], bb = v.v[2] - RAYGRID_KZ * v.v[0];
+                b.alo = std::min(b.alo, a);
+                b.ahi = std::max(b.ahi, a);
+                b.blo = std::min(b.blo, bb);
+                b.bhi = std::max(b.bhi, bb);
+                mt = std::max(mt, v.v[0] * RAYGRID_INV_DX);
+            }
+            extent[i] = std::max(b.ahi - b.alo, b.bhi - b.blo);
+            b.alo -= pad;
+            b.ahi += pad;
+            b.blo -= pad;
+            b.bhi += pad;
+            b.maxt = f_up(mt + pad * (1 + RAYGRID_INV_DX));
+            if (!std::isfinite(b.alo + b.ahi + b.blo + b.bhi)) {
+                kind[i] = 3;
+                continue;
+            }
+            cand[i] = b;
+            kind[i] = 1;
+        }
+    });
     std::vector<Box> boxes;
-    boxes.reserve(order.size());
+    boxes.reserve(n);
     std::vector<int> all;
     std::vector<double> sizes;
-    sizes.reserve(order.size());
-    for (size_t i = 0; i < order.size(); i++) {
-        if (!P->tris[tri_base + i].valid) continue;  // parallel or det == 0: never hit
-        const Tri& tr = t[order[i]];
-        const D3 v1 = vsub(tr.p[1], tr.p[0]), v2 = vsub(tr.p[2], tr.p[0]);
-        const double det = std::fabs(vdot(vcross(kRay, v2), v1));
-        const double k1 = vnorm(v1) * vnorm(v2) * dlen / det;
-        double k2 = 0;
-        for (int e = 0; e < 3; e++) {
-            const D3 ev = vsub(tr.p[(e + 1) % 3], tr.p[e]);
-            const D3 perp = vsub(ev, vscale(dh, vdot(ev, dh)));
-            const double n = vnorm(ev), np = vnorm(perp);
-            if (n > 0) k2 = std::max(k2, n / np);
-        }
-        if (!(7 * eps * k1 <= 1e-3) || !std::isfinite(k2)) {
-            all.push_back(tri_base + (int)i);
-            continue;
-        }
-        const double pad = (R + 1) * (4e-6 + 1e3 * eps * (k1 + k2));
-        Box b{DBL_MAX, -DBL_MAX, DBL_MAX, -DBL_MAX, 0.f, tri_base + (int)i};
-        double mt = -DBL_MAX;
-        for (int k = 0; k < 3; k++) {
-            const D3& v = tr.p[k];
-            const double a = v.v[1] - RAYGRID_KY * v.v[0], bb = v.v[2] - RAYGRID_KZ * v.v[0];
-            b.alo = std::min(b.alo, a);
-            b.ahi = std::max(b.ahi, a);
-            b.blo = std::min(b.blo, bb);
-            b.bhi = std::max(b.bhi, bb);
-            mt = std::max(mt, v.v[0] * RAYGRID_INV_DX);
-        }
-        sizes.push_back(std::max(b.ahi - b.alo, b.bhi - b.blo));
-        b.alo -= pad;
-        b.ahi += pad;
-        b.blo -= pad;
-        b.bhi += pad;
-        b.maxt = f_up(mt + pad * (1 + RAYGRID_INV_DX));
-        if (!std::isfinite(b.alo + b.ahi + b.blo + b.bhi)) {
-            all.push_back(tri_base + (int)i);
-            continue;
-        }
-        boxes.push_back(b);
+    sizes.reserve(n);
+    for (size_t i = 0; i < n; i++) {
+        if (kind[i] == 1 || kind[i] == 3) sizes.push_back(extent[i]);
+        if (kind[i] == 1) boxes.push_back(cand[i]);
+        if (kind[i] == 2 || kind[i] == 3) all.push_back(tri_base + (int)i);
     }
+    std::vector<Box>().swap(cand);
     double amin = 0, amax = 0, bmin = 0, bmax = 0;
     if (!boxes.empty()) {
         amin = bmin = DBL_MAX;
@@ -424,27 +467,38 @@ void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, in
     // leaves every cell sorted without a sort per cell.
     std::sort(boxes.begin(), boxes.end(),
               [](const Box& x, const Box& y) { return x.maxt < y.maxt || (x.maxt == y.maxt && x.tri < y.tri); });
+    // Counting and filling run on bands of cell rows: a band's cells belong to
+    // one thread, which walks every box in the sorted order.
+    const size_t band_rows = boxes.size() >= 65536 ? 1 : (size_t)gb;
     std::vector<int64_t> cnt(ncell + 1, 0);
-    for (const Box& b : boxes) {
-        int a0, a1, b0, b1;
-        cell_range(b.alo, b.ahi, amin_f, ga, &a0, &a1);
-        cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
-        for (int y = b0; y <= b1; y++)
-            for (int x = a0; x <= a1; x++) cnt[(size_t)y * ga + x + 1]++;
-    }
+    parallel_chunks((size_t)gb, band_rows, [&](size_t y_lo, size_t y_hi) {
+        for (const Box& b : boxes) {
+            int a0, a1, b0, b1;
+            cell_range(b.alo, b.ahi, amin_f, ga, &a0, &a1);
+            cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
+            b0 = std::max(b0, (int)y_lo);
+            b1 = std::min(b1, (int)y_hi - 1);
+            for (int y = b0; y <= b1; y++)
+                for (int x = a0; x <= a1; x++) cnt[(size_t)y * ga + x + 1]++;
+        }
+    });
     for (size_t c = 0; c < ncell; c++) cnt[c + 1] += cnt[c];
     const int64_t base = (int64_t)P->ents.size();
     if (base + cnt[ncell] + (int64_t)all.size() >= ((int64_t)1 << 31))
         throw LowerError(MC_ERR_LIMIT, "collider ray grid exceeds 2^31 entries");
     P->ents.resize(base + cnt[ncell]);
     std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
-    for (const Box& b : boxes) {
-        int a0, a1, b0, b1;
-        cell_range(b.alo, b.ahi, amin_f, ga, &a0, &a1);
-        cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
-        for (int y = b0; y <= b1; y++)
-            for (int x = a0; x <= a1; x++) P->ents[base + fill[(size_t)y * ga + x]++] = RayEnt{b.maxt, b.tri};
-    }
+    parallel_chunks((size_t)gb, band_rows, [&](size_t y_lo, size_t y_hi) {
+        for (const Box& b : boxes) {
+            int a0, a1, b0, b1;
+            cell_range(b.alo, b.ahi, amin_f, ga, &a0, &a1);
+            cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
+            b0 = std::max(b0, (int)y_lo);
+            b1 = std::min(b1, (int)y_hi - 1);
+            for (int y = b0; y <= b1; y++)
+                for (int x = a0; x <= a1; x++) P->ents[base + fill[(size_t)y * ga + x]++] = RayEnt{b.maxt, b.tri};
+        }
+    });
     tree->cell_base = (int32_t)P->cell_start.size();
     tree->n_cells = (int32_t)ncell;
     for (size_t c = 0; c <= ncell; c++) P->cell_start.push_back((int32_t)(base + cnt[c]));
@@ -776,41 +830,43 @@ struct Lowerer {
         }
         TreeD tree{};
         int tri_base = (int)P->tris.size();
-        P->tris.reserve(P->tris.size() + order.size());
-        P->tris_f.reserve(P->tris_f.size() + order.size());
-        // Triangle records in grouped order (traversal locality).
         std::vector<int> pos_of(ts.n);
         for (size_t i = 0; i < order.size(); i++) pos_of[order[i]] = (int)i;
+        // Triangle records in grouped order (traversal locality), on host threads.
+        P->tris.resize(tri_base + order.size());
+        P->tris_f.resize(tri_base + order.size());
         D3 dn = vnormalize(kRay);
-        for (size_t i = 0; i < order.size(); i++) {
-            const Tri& tr = t[order[i]];
-            TriD d{};
-            TriF f{};
-            D3 v1 = vsub(tr.p[1], tr.p[0]);
-            D3 v2 = vsub(tr.p[2], tr.p[0]);
-            D3 nrm = vnormalize(vcross(v1, v2));      // Triangle.Normal, primitives.go:27-33
-            double dd = vdot(nrm, dn);                 // primitives.go:208
-            bool parallel = dd < 1e-8 && dd > -1e-8;
-            D3 c1 = vcross(kRay, v2);                  // primitives.go:219
-            double det = vdot(c1, v1);                 // primitives.go:220
-            double inv = 1 / det;                      // primitives.go:227
-            for (int k = 0; k < 3; k++) {
-                d.t0[k] = tr.p[0].v[k];
-                d.v1[k] = v1.v[k];
-                d.v2[k] = v2.v[k];
-                d.c1[k] = c1.v[k];
-                f.t0[k] = (float)d.t0[k];
-                f.v1[k] = (float)d.v1[k];
-                f.v2[k] = (float)d.v2[k];
-                f.c1[k] = (float)d.c1[k];
+        parallel_chunks(order.size(), 16384, [&](size_t lo, size_t hi) {
+            for (size_t i = lo; i < hi; i++) {
+                const Tri& tr = t[order[i]];
+                TriD d{};
+                TriF f{};
+                D3 v1 = vsub(tr.p[1], tr.p[0]);
+                D3 v2 = vsub(tr.p[2], tr.p[0]);
+                D3 nrm = vnormalize(vcross(v1, v2));      // Triangle.Normal, primitives.go:27-33
+                double dd = vdot(nrm, dn);                 // primitives.go:208
+                bool parallel = dd < 1e-8 && dd > -1e-8;
+                D3 c1 = vcross(kRay, v2);                  // primitives.go:219
+                double det = vdot(c1, v1);                 // primitives.go:220
+                double inv = 1 / det;                      // primitives.go:227
+                for (int k = 0; k < 3; k++) {
+                    d.t0[k] = tr.p[0].v[k];
+                    d.v1[k] = v1.v[k];
+                    d.v2[k] = v2.v[k];
+                    d.c1[k] = c1.v[k];
+                    f.t0[k] = (float)d.t0[k];
+                    f.v1[k] = (float)d.v1[k];
+                    f.v2[k] = (float)d.v2[k];
+                    f.c1[k] = (float)d.c1[k];
+                }
+                d.inv_det = inv;
+                d.valid = (!parallel && det != 0) ? 1 : 0;
+                f.inv_det = (float)inv;
+                f.valid = d.valid;
+                P->tris[tri_base + i] = d;
+                P->tris_f[tri_base + i] = f;
             }
-            d.inv_det = inv;
-            d.valid = (!parallel && det != 0) ? 1 : 0;
-            f.inv_det = (float)inv;
-            f.valid = d.valid;
-            P->tris.push_back(d);
-            P->tris_f.push_back(f);
-        }
+        });
         P->tri_parent.resize(P->tris.size(), -1);
         if (ts.n > 1) {
             TreeBuilder tb{t, {}};
