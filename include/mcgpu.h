@@ -160,7 +160,8 @@ typedef struct mc_opts {
     int32_t tile_z;     /* corner-tile depth in z (0: tuned default) */
     int32_t interior;   /* 1: also record each vertex's interior point (MarchingCubesInterior,
                            model3d/mc.go:55-60) for mc_result_interior_copy; mc_search_device
-                           and mc_search only (ignored by the batch and allocation-free calls) */
+                           and mc_search only (ignored by the batch call; the allocation-free
+                           call returns MC_ERR_ARG) */
     int32_t reserved[3];
 } mc_opts;
 
@@ -335,18 +336,26 @@ mc_status mc_case_table(uint8_t counts[256], uint8_t tris[256][5][6]);
  * those calls can synchronise the whole device.  No counterpart in the
  * reference (it is a GPU-memory concern the Go code does not have).
  *
- * Same result as mc_search for CSG solids (no MC_NODE_COLLIDER nodes; those
- * return MC_ERR_BAD_PROGRAM).  Every intermediate array lives in one
- * file-scope device array of MC_NOALLOC_SCRATCH_BYTES, which every GPU that
- * loads the library holds until the process exits; the call makes no
+ * Same result as mc_search for CSG and metaball solids.  Solids with a
+ * MC_NODE_COLLIDER node return MC_ERR_BAD_PROGRAM (a collider's tree and ray
+ * grid are built from triangle sets this call does not take), and
+ * opts->interior set returns MC_ERR_ARG.  Every intermediate array lives in
+ * one file-scope device array of MC_NOALLOC_SCRATCH_BYTES, which every GPU
+ * that loads the library holds until the process exits; the call makes no
  * cudaMalloc / cudaFree.  Inputs: the node array (host memory), delta,
  * iters, opts (may be NULL), the stream to run on (NULL: the legacy default
  * stream) on the current device.  Outputs: device buffers vertices
  * (vertex_cap x 3 float64) and triangles (triangle_cap x 3 int32), written in
  * the same layout as mc_search_device; *n_vertices / *n_triangles receive the
  * mesh size, also when the status is MC_ERR_LIMIT because a buffer is too
- * small (the caller can retry with larger buffers).  A grid or program that
- * does not fit the scratch array returns MC_ERR_LIMIT.
+ * small (the caller can retry with larger buffers).  MC_ERR_LIMIT also means
+ * that the grid, the program or the vertex keys do not fit the scratch array
+ * (roughly beyond 400^3 corners), or that the folded program needs more
+ * shared memory per block than the device offers.  When it returns
+ * MC_ERR_LIMIT, no work of the call is left running on the GPU.
+ *
+ * The call uploads the program from host memory and waits on the stream
+ * twice before it returns: once for the mesh size, once for the error words.
  *
  * The first call on a device looks up the scratch array's device address
  * (cudaGetSymbolAddress) and uploads the case table; make that first call

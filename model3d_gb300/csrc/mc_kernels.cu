@@ -3293,6 +3293,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
                                        int64_t vertex_cap, int32_t* triangles, int64_t triangle_cap,
                                        int64_t* n_vertices, int64_t* n_triangles) {
     if (!nodes || n_nodes == 0 || iters < 0 || vertex_cap < 0 || triangle_cap < 0) return MC_ERR_ARG;
+    if (opts_in && opts_in->interior) return MC_ERR_ARG;  // interior points need an array of their own
     if (n_vertices) *n_vertices = 0;
     if (n_triangles) *n_triangles = 0;
     int dev = 0;
@@ -3419,12 +3420,23 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     ca.ntx = (nx + 31) / 32;
     ca.nty = (ny + ca.ty - 1) / ca.ty;
     ca.ntz = (nz + ca.tz - 1) / ca.tz;
-    const size_t smem_c = classify_smem(P);
-    if (smem_c > 48 * 1024) return MC_ERR_LIMIT;
+    // Shared memory of the folded program: checked and raised for both kernels
+    // before anything is launched (setting the attribute allocates nothing).
+    auto kc = MC_PICK(k_classify, opts.precision, P.has_metaball);
+    auto ks = MC_PICK(k_search, opts.precision, P.has_metaball);
+    const size_t smem_c = classify_smem(P), smem_s = search_smem(P);
+    int smem_optin = 48 * 1024;
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (smem_c > (size_t)smem_optin || smem_s > (size_t)smem_optin) return MC_ERR_LIMIT;
+    if (smem_c > 48 * 1024 &&
+        cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c) != cudaSuccess)
+        return MC_ERR_CUDA;
+    if (smem_s > 48 * 1024 &&
+        cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s) != cudaSuccess)
+        return MC_ERR_CUDA;
     const long long cols = (long long)ca.nty * ca.ntz;
     ca.nxs = pick_xsegments(cols, ca.ntx, 8LL * sms * 4, P.has_metaball);
     long long items = cols * ca.nxs;
-    auto kc = MC_PICK(k_classify, opts.precision, P.has_metaball);
     kc<<<(int)std::max<long long>(1, std::min<long long>((items + 7) / 8, (long long)sms * 4)), 256, smem_c, sm>>>(
         g, P, ca);
     if (nchunks > 0) {
@@ -3462,9 +3474,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         sa.cull = opts.cull;
         sa.err = errs;
         sa.stats = stats;
-        if (search_smem(P) > 48 * 1024) return MC_ERR_LIMIT;
-        auto ks = MC_PICK(k_search, opts.precision, P.has_metaball);
-        ks<<<search_blocks(V, sms), 128, search_smem(P), sm>>>(g, P, sa);
+        ks<<<search_blocks(V, sms), 128, smem_s, sm>>>(g, P, sa);
     }
     if (cudaGetLastError() != cudaSuccess) return MC_ERR_CUDA;
     if (cudaMemcpyAsync(h + 2, errs, ER_N * 4, cudaMemcpyDeviceToHost, sm) != cudaSuccess ||
