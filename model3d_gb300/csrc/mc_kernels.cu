@@ -36,6 +36,15 @@
 #include "mc_lower.h"
 #include "mc_predicates.cuh"
 
+// Resident blocks per SM the classification (256 threads) and search (128
+// threads) kernels are compiled for; they set the register budget per thread.
+#ifndef MC_CLASSIFY_MIN_BLOCKS
+#define MC_CLASSIFY_MIN_BLOCKS 3
+#endif
+#ifndef MC_SEARCH_MIN_BLOCKS
+#define MC_SEARCH_MIN_BLOCKS 4
+#endif
+
 namespace mcgpu {
 
 // ------------------------------------------------------------ counters
@@ -828,7 +837,7 @@ __device__ __forceinline__ void classify_column(const GridView& g, const ProgVie
 
 // One warp per work item, items handed out by an atomic counter.
 template <int PREC>
-__global__ void __launch_bounds__(256, 3) k_classify(GridView g, ProgView P, ClassifyArgs a) {
+__global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify(GridView g, ProgView P, ClassifyArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (P.n_leaves + 31) >> 5;
@@ -1018,38 +1027,100 @@ __global__ void __launch_bounds__(256) k_count(GridView g, CountArgs a) {
     }
 }
 
-// Exclusive scan of the per-block sums by one CTA; totals at out[2*nb..].
-__global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t* blocksum, unsigned long long* blockoff,
-                                                      int nb, unsigned long long* totals) {
-    __shared__ unsigned long long sv[1024], st[1024];
-    int t = threadIdx.x, T = blockDim.x;
-    int per = (nb + T - 1) / T;
-    int b0 = t * per, b1 = min(nb, b0 + per);
-    unsigned long long v = 0, w = 0;
-    for (int b = b0; b < b1; b++) {
-        v += blocksum[2 * b];
-        w += blocksum[2 * b + 1];
+// Exclusive scan of the per-block (vertex, triangle) sums of k_count.
+// Group g = one CTA scans blocks [1024 g, 1024 g + 1024) into offsets local
+// to the group (blockoff[2b], [2b+1]; a group's sums fit in 32 bits: at most
+// 1024 x 2048 chunks x 160 triangles) and publishes the group's sums.  The
+// CTA that finishes last (a ticket counter: no CTA waits for another) scans
+// the group sums into group offsets at blockoff[2 nb + 2 g] and writes the
+// totals; k_scan_chunks adds the two.  The ticket (*ticket, zero on entry)
+// is reset to zero by the last CTA.
+constexpr int kScanGroup = 1024;
+
+__device__ __forceinline__ void block_scan_u64(unsigned long long& v, unsigned long long& w,
+                                               unsigned long long* sv, unsigned long long* sw) {
+    // Inclusive scan of (v, w) over a 1024-thread block; sv / sw: 32 words each.
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long a = __shfl_up_sync(0xffffffffu, v, o), b = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) {
+            v += a;
+            w += b;
+        }
     }
-    sv[t] = v;
-    st[t] = w;
+    if (lane == 31) {
+        sv[wid] = v;
+        sw[wid] = w;
+    }
     __syncthreads();
-    for (int o = 1; o < T; o <<= 1) {  // Hillis-Steele inclusive scan
-        unsigned long long av = t >= o ? sv[t - o] : 0, aw = t >= o ? st[t - o] : 0;
+    if (wid == 0) {
+        unsigned long long a = sv[lane], b = sw[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long c = __shfl_up_sync(0xffffffffu, a, o), d = __shfl_up_sync(0xffffffffu, b, o);
+            if (lane >= o) {
+                a += c;
+                b += d;
+            }
+        }
+        sv[lane] = a;
+        sw[lane] = b;
+    }
+    __syncthreads();
+    if (wid > 0) {
+        v += sv[wid - 1];
+        w += sw[wid - 1];
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(const uint32_t* blocksum, unsigned long long* blockoff,
+                                                      int nb, unsigned long long* totals, unsigned int* ticket) {
+    __shared__ unsigned long long sv[32], sw[32], carry[2];
+    __shared__ bool last;
+    const int t = threadIdx.x, b = blockIdx.x * kScanGroup + t;
+    unsigned long long* grp = blockoff + 2 * (size_t)nb;
+    const unsigned long long v0 = b < nb ? blocksum[2 * b] : 0, w0 = b < nb ? blocksum[2 * b + 1] : 0;
+    unsigned long long v = v0, w = w0;
+    block_scan_u64(v, w, sv, sw);
+    if (b < nb) {
+        blockoff[2 * b] = v - v0;
+        blockoff[2 * b + 1] = w - w0;
+    }
+    if (t == kScanGroup - 1) {
+        grp[2 * blockIdx.x] = v;  // the group's sums, replaced by its offsets below
+        grp[2 * blockIdx.x + 1] = w;
+    }
+    __threadfence();
+    __syncthreads();
+    if (t == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int ng = gridDim.x;
+    if (t == 0) carry[0] = carry[1] = 0;
+    __syncthreads();
+    for (int g0 = 0; g0 < ng; g0 += kScanGroup) {
+        const int g = g0 + t;
+        const unsigned long long a0 = g < ng ? __ldcg(&grp[2 * g]) : 0, c0 = g < ng ? __ldcg(&grp[2 * g + 1]) : 0;
+        unsigned long long a = a0, c = c0;
+        block_scan_u64(a, c, sv, sw);
+        const unsigned long long ca = carry[0], cc = carry[1];
+        if (g < ng) {
+            grp[2 * g] = ca + a - a0;
+            grp[2 * g + 1] = cc + c - c0;
+        }
         __syncthreads();
-        sv[t] += av;
-        st[t] += aw;
+        if (t == kScanGroup - 1) {
+            carry[0] = ca + a;
+            carry[1] = cc + c;
+        }
         __syncthreads();
     }
-    unsigned long long ov = sv[t] - v, ow = st[t] - w;
-    for (int b = b0; b < b1; b++) {
-        blockoff[2 * b] = ov;
-        blockoff[2 * b + 1] = ow;
-        ov += blocksum[2 * b];
-        ow += blocksum[2 * b + 1];
-    }
-    if (t == T - 1) {
-        totals[0] = sv[t];
-        totals[1] = st[t];
+    if (t == 0) {
+        totals[0] = carry[0];
+        totals[1] = carry[1];
+        *ticket = 0u;
     }
 }
 
@@ -1124,8 +1195,9 @@ __global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* packed, con
         bv += wsv[k];
         bt += wst[k];
     }
-    const unsigned long long cv = blockoff[2 * blockIdx.x] + bv + (iv - sv);
-    const unsigned long long ct = blockoff[2 * blockIdx.x + 1] + bt + (it - st);
+    const unsigned long long* grp = blockoff + 2 * (size_t)gridDim.x + 2 * (blockIdx.x / kScanGroup);
+    const unsigned long long cv = grp[0] + blockoff[2 * blockIdx.x] + bv + (iv - sv);
+    const unsigned long long ct = grp[1] + blockoff[2 * blockIdx.x + 1] + bt + (it - st);
     uint32_t ov[8], ot[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -1504,7 +1576,7 @@ __device__ __forceinline__ void search_cull(const ProgView& P, bool work, const 
 }
 
 template <int PREC>
-__global__ void __launch_bounds__(128, 4) k_search(GridView g, ProgView P, SearchArgs a) {
+__global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search(GridView g, ProgView P, SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (P.n_leaves + 31) >> 5;
@@ -1683,7 +1755,7 @@ struct BatchArgs {
 };
 
 template <int PREC>
-__global__ void __launch_bounds__(256, 3) k_classify_batch(BatchArgs b) {
+__global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify_batch(BatchArgs b) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t* base = (uint32_t*)smem + (size_t)warp * b.fold_words;
@@ -1750,8 +1822,27 @@ __global__ void __launch_bounds__(256) k_emit_batch(BatchArgs b, const uint32_t*
     emit_chunk(J.g, ea, i - c0, (uint32_t)b.vbase[j]);
 }
 
+// Emission over the non-empty chunks that k_scan_chunks listed (global chunk
+// indices; about one chunk in twenty), so that every lane emits instead of a
+// few.  The list's length is read from device memory (b.totals[2]), so the
+// captured graph replays with any list; grid-stride over the list.
+__global__ void __launch_bounds__(256) k_emit_batch_list(BatchArgs b, const uint32_t* packed, const uint32_t* prefv,
+                                                          const uint32_t* preft, unsigned long long* keys,
+                                                          int32_t* tris, const uint32_t* list) {
+    const long long n = (long long)b.totals[2];
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long i = list[k];
+        const int j = find_slot(b.chunk_offs, b.njobs, i);
+        const JobD& J = b.jobs[j];
+        const long long c0 = b.chunk_offs[j];
+        EmitArgs ea{J.ca.bits, packed + c0, prefv + c0, preft + c0, keys, tris, J.nchunks};
+        emit_chunk(J.g, ea, i - c0, (uint32_t)b.vbase[j]);
+    }
+}
+
 template <int PREC>
-__global__ void __launch_bounds__(128, 4) k_search_batch(BatchArgs b, const unsigned long long* keys, double* verts) {
+__global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(BatchArgs b, const unsigned long long* keys, double* verts) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t* q = (uint32_t*)smem + (size_t)warp * b.fold_words;
@@ -1927,19 +2018,20 @@ struct BatchPlan {
     std::vector<mcgpu::JobD> hjobs;
     std::vector<long long> hchunk_offs;
     long long nitems = 0, nchunks = 0;
-    int nblk = 0, fold_words = 0, grid_c = 1, grid_s = 1, prec = 1;
+    int nblk = 0, fold_words = 0, grid_c = 1, grid_s = 1, grid_e = 1, prec = 1;
     bool has_metaball = false;
+    bool use_list = false;  // emit over the list of non-empty chunks
     size_t smem_c = 0, smem_s = 0;
     long long cap_V = -1, cap_T = -1;
     cudaGraphExec_t exec = nullptr;
     DevBuf jobs, sched_off, sched_job, chunk_offs, vbase, tbase, grid, bits, errs, packed, blocksum, blockoff, prefv,
-        preft, keys, verts, tris, totals, stats;
+        preft, keys, verts, tris, totals, stats, nonempty;
     unsigned long long* h_stage = nullptr;  // pinned staging for the outputs
     size_t h_stage_bytes = 0;
     ~BatchPlan() {
         if (exec) cudaGraphExecDestroy(exec);
         for (DevBuf* b : {&jobs, &sched_off, &sched_job, &chunk_offs, &vbase, &tbase, &grid, &bits, &errs, &packed,
-                          &blocksum, &blockoff, &prefv, &preft, &keys, &verts, &tris, &totals, &stats})
+                          &blocksum, &blockoff, &prefv, &preft, &keys, &verts, &tris, &totals, &stats, &nonempty})
             b->release();
         if (h_stage) cudaFreeHost(h_stage);
     }
@@ -2371,7 +2463,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     CK(ctx->zs.ensure(nz * 8));
     CK(ctx->stats.ensure(ST_N * 8));
     CK(ctx->errs.ensure(ER_N * 4));
-    CK(ctx->totals.ensure(24));  // vertices, triangles, non-empty chunks
+    CK(ctx->totals.ensure(32));  // vertices, triangles, non-empty chunks, scan ticket
     CK(cudaMemcpyAsync(ctx->xs.p, X.data(), nx * 8, cudaMemcpyHostToDevice, sm));
     CK(cudaMemcpyAsync(ctx->ys.p, Y.data(), ny * 8, cudaMemcpyHostToDevice, sm));
     CK(cudaMemcpyAsync(ctx->zs.p, Z.data(), nz * 8, cudaMemcpyHostToDevice, sm));
@@ -2384,7 +2476,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     CK(cudaMemcpyAsync(ctx->zf.p, ZF.data(), nz * 4, cudaMemcpyHostToDevice, sm));
     CK(cudaMemsetAsync(ctx->stats.p, 0, ST_N * 8, sm));
     CK(cudaMemsetAsync(ctx->errs.p, 0, ER_N * 4, sm));
-    CK(cudaMemsetAsync(ctx->totals.p, 0, 24, sm));
+    CK(cudaMemsetAsync(ctx->totals.p, 0, 32, sm));
     g.xs = ctx->xs.as<double>();
     g.ys = ctx->ys.as<double>();
     g.zs = ctx->zs.as<double>();
@@ -2427,18 +2519,20 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
 
     long long nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)g.CX * (ny - 1) * (nz - 1) : 0;
     const int nblk = (int)((nchunks + kChunksPerBlock - 1) / kChunksPerBlock);
+    const int ngrp = (nblk + kScanGroup - 1) / kScanGroup;
     if (nchunks > 0) {
         CK(ctx->packed.ensure(nchunks * 4));
         CK(ctx->blocksum.ensure((size_t)nblk * 8));
-        CK(ctx->blockoff.ensure((size_t)nblk * 16));
+        CK(ctx->blockoff.ensure((size_t)(nblk + ngrp) * 16));
         CK(ctx->prefv.ensure(nchunks * 4));
         CK(ctx->preft.ensure(nchunks * 4));
         CK(ctx->nonempty.ensure(nchunks * 4));
         CountArgs cn{ctx->bits.as<uint32_t>(), ctx->packed.as<uint32_t>(), ctx->blocksum.as<uint32_t>(), nchunks};
         k_count<<<nblk, 256, 0, sm>>>(g, cn);
         CK(cudaGetLastError());
-        k_scan_blocks<<<1, 1024, 0, sm>>>(ctx->blocksum.as<uint32_t>(), ctx->blockoff.as<unsigned long long>(), nblk,
-                                          ctx->totals.as<unsigned long long>());
+        k_scan_blocks<<<ngrp, kScanGroup, 0, sm>>>(ctx->blocksum.as<uint32_t>(), ctx->blockoff.as<unsigned long long>(),
+                                                   nblk, ctx->totals.as<unsigned long long>(),
+                                                   (unsigned int*)(ctx->totals.as<unsigned long long>() + 3));
         CK(cudaGetLastError());
         k_scan_chunks<<<nblk, 256, 0, sm>>>(ctx->packed.as<uint32_t>(), ctx->blockoff.as<unsigned long long>(),
                                             nchunks, ctx->prefv.as<uint32_t>(), ctx->preft.as<uint32_t>(),
@@ -3003,7 +3097,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         CK(pl->bits.ensure(std::max<size_t>(nbits_total, 1) * 4));
         CK(pl->errs.ensure(std::max(nd, 1) * ER_N * 4));
         CK(pl->stats.ensure(ST_N * 8));
-        CK(pl->totals.ensure(16));
+        CK(pl->totals.ensure(32));  // vertices, triangles, non-empty chunks, scan ticket
         CK(pl->vbase.ensure((nd + 1) * 8));
         CK(pl->tbase.ensure((nd + 1) * 8));
         unsigned char* gbase = (unsigned char*)pl->grid.p;
@@ -3048,9 +3142,12 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         if (pl->nchunks > 0) {
             CK(pl->packed.ensure(pl->nchunks * 4));
             CK(pl->blocksum.ensure((size_t)pl->nblk * 8));
-            CK(pl->blockoff.ensure((size_t)pl->nblk * 16));
+            CK(pl->blockoff.ensure((size_t)(pl->nblk + (pl->nblk + kScanGroup - 1) / kScanGroup) * 16));
             CK(pl->prefv.ensure(pl->nchunks * 4));
             CK(pl->preft.ensure(pl->nchunks * 4));
+            // The list of non-empty chunks holds u32 chunk indices.
+            pl->use_list = pl->nchunks < (1LL << 32);
+            if (pl->use_list) CK(pl->nonempty.ensure(pl->nchunks * 4));
         }
         CK(cudaMemcpyAsync(pl->grid.p, gd.data(), gd_bytes, cudaMemcpyHostToDevice, sm));
         CK(cudaMemcpyAsync(gbase + gf_off, gf.data(), gf.size() * 4, cudaMemcpyHostToDevice, sm));
@@ -3091,21 +3188,28 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
     auto front = [&]() -> cudaError_t {
         cudaMemsetAsync(pl->stats.p, 0, ST_N * 8, sm);
         cudaMemsetAsync(pl->errs.p, 0, std::max(nd, 1) * ER_N * 4, sm);
-        cudaMemsetAsync(pl->totals.p, 0, 16, sm);
+        cudaMemsetAsync(pl->totals.p, 0, 32, sm);
         cudaMemsetAsync(pl->bits.p, 0, pl->bits.cap, sm);
         if (nd > 0) kcb<<<pl->grid_c, 256, pl->smem_c, sm>>>(ba);
         if (pl->nchunks > 0) {
             k_count_batch<<<pl->nblk, 256, 0, sm>>>(ba, pl->packed.as<uint32_t>(), pl->blocksum.as<uint32_t>());
-            k_scan_blocks<<<1, 1024, 0, sm>>>(pl->blocksum.as<uint32_t>(), pl->blockoff.as<unsigned long long>(),
-                                              pl->nblk, ba.totals);
+            k_scan_blocks<<<(pl->nblk + kScanGroup - 1) / kScanGroup, kScanGroup, 0, sm>>>(
+                pl->blocksum.as<uint32_t>(), pl->blockoff.as<unsigned long long>(), pl->nblk, ba.totals,
+                (unsigned int*)(ba.totals + 3));
             k_scan_chunks<<<pl->nblk, 256, 0, sm>>>(pl->packed.as<uint32_t>(), pl->blockoff.as<unsigned long long>(),
-                                                    pl->nchunks, pl->prefv.as<uint32_t>(), pl->preft.as<uint32_t>());
+                                                    pl->nchunks, pl->prefv.as<uint32_t>(), pl->preft.as<uint32_t>(),
+                                                    pl->use_list ? pl->nonempty.as<uint32_t>() : nullptr,
+                                                    pl->use_list ? ba.totals + 2 : nullptr);
         }
         k_job_bases<<<(nd + 256) / 256, 256, 0, sm>>>(ba, pl->prefv.as<uint32_t>(), pl->preft.as<uint32_t>());
         return cudaGetLastError();
     };
     auto back = [&]() -> cudaError_t {
-        if (pl->nchunks > 0)
+        if (pl->nchunks > 0 && pl->use_list)
+            k_emit_batch_list<<<pl->grid_e, 256, 0, sm>>>(ba, pl->packed.as<uint32_t>(), pl->prefv.as<uint32_t>(),
+                                                          pl->preft.as<uint32_t>(), pl->keys.as<unsigned long long>(),
+                                                          pl->tris.as<int32_t>(), pl->nonempty.as<uint32_t>());
+        else if (pl->nchunks > 0)
             k_emit_batch<<<(int)((pl->nchunks + 255) / 256), 256, 0, sm>>>(ba, pl->packed.as<uint32_t>(),
                                                                              pl->prefv.as<uint32_t>(),
                                                    pl->preft.as<uint32_t>(), pl->keys.as<unsigned long long>(),
@@ -3114,9 +3218,9 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         return cudaGetLastError();
     };
     std::vector<int> herr(std::max(nd, 1) * ER_N);
-    std::vector<unsigned long long> hvb(nd + 1), htb(nd + 1), htot(2), hstats(ST_N);
+    std::vector<unsigned long long> hvb(nd + 1), htb(nd + 1), htot(3), hstats(ST_N);
     auto readback = [&]() -> cudaError_t {
-        cudaMemcpyAsync(htot.data(), pl->totals.p, 16, cudaMemcpyDeviceToHost, sm);
+        cudaMemcpyAsync(htot.data(), pl->totals.p, 24, cudaMemcpyDeviceToHost, sm);
         cudaMemcpyAsync(herr.data(), pl->errs.p, herr.size() * 4, cudaMemcpyDeviceToHost, sm);
         cudaMemcpyAsync(hvb.data(), pl->vbase.p, (nd + 1) * 8, cudaMemcpyDeviceToHost, sm);
         cudaMemcpyAsync(htb.data(), pl->tbase.p, (nd + 1) * 8, cudaMemcpyDeviceToHost, sm);
@@ -3146,6 +3250,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         CK(pl->verts.ensure(std::max<long long>(V, 1) * 24));
         CK(pl->tris.ensure(std::max<long long>(T, 1) * 12));
         pl->grid_s = std::max(ctx->sm_count * 16, search_blocks(V, ctx->sm_count));
+        pl->grid_e = (int)std::max<long long>(1, std::min<long long>(((long long)htot[2] + 255) / 256, 1LL << 30));
         CK(back());
         CK(cudaEventRecord(ctx->ev[4], sm));
         CK(readback());
@@ -3345,7 +3450,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     for (auto& p : up) p.dst = cv.take(p.bytes);
     int* errs = (int*)cv.take(ER_N * 4);
     unsigned long long* stats = (unsigned long long*)cv.take(ST_N * 8);
-    unsigned long long* totals = (unsigned long long*)cv.take(16);
+    unsigned long long* totals = (unsigned long long*)cv.take(32);  // V, T, (unused), scan ticket
     GridView g{};
     g.nx = nx;
     g.ny = ny;
@@ -3359,7 +3464,8 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     const int egrid = (int)((nchunks + 255) / 256);
     uint32_t* packed = (uint32_t*)cv.take(nchunks * 4);
     uint32_t* blocksum = (uint32_t*)cv.take((size_t)nblk * 8);
-    unsigned long long* blockoff = (unsigned long long*)cv.take((size_t)nblk * 16);
+    const int ngrp = (nblk + kScanGroup - 1) / kScanGroup;
+    unsigned long long* blockoff = (unsigned long long*)cv.take((size_t)(nblk + ngrp) * 16);
     uint32_t* prefv = (uint32_t*)cv.take(nchunks * 4);
     uint32_t* preft = (uint32_t*)cv.take(nchunks * 4);
     if (!cv.ok) return MC_ERR_LIMIT;  // grid or program larger than the scratch array
@@ -3377,7 +3483,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
             return MC_ERR_CUDA;
     }
     if (cudaMemsetAsync(errs, 0, ER_N * 4, sm) != cudaSuccess || cudaMemsetAsync(stats, 0, ST_N * 8, sm) != cudaSuccess ||
-        cudaMemsetAsync(totals, 0, 16, sm) != cudaSuccess || cudaMemsetAsync(bits, 0, nbits * 4, sm) != cudaSuccess)
+        cudaMemsetAsync(totals, 0, 32, sm) != cudaSuccess || cudaMemsetAsync(bits, 0, nbits * 4, sm) != cudaSuccess)
         return MC_ERR_CUDA;
     g.xs = (const double*)up[8].dst;
     g.ys = (const double*)up[9].dst;
@@ -3441,7 +3547,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         g, P, ca);
     if (nchunks > 0) {
         k_count<<<nblk, 256, 0, sm>>>(g, CountArgs{bits, packed, blocksum, nchunks});
-        k_scan_blocks<<<1, 1024, 0, sm>>>(blocksum, blockoff, nblk, totals);
+        k_scan_blocks<<<ngrp, kScanGroup, 0, sm>>>(blocksum, blockoff, nblk, totals, (unsigned int*)(totals + 3));
         k_scan_chunks<<<nblk, 256, 0, sm>>>(packed, blockoff, nchunks, prefv, preft);
     }
     if (cudaGetLastError() != cudaSuccess) return MC_ERR_CUDA;
