@@ -162,7 +162,16 @@ typedef struct mc_opts {
                            model3d/mc.go:55-60) for mc_result_interior_copy; mc_search_device
                            and mc_search only (ignored by the batch call; the allocation-free
                            call returns MC_ERR_ARG) */
-    int32_t reserved[3];
+    int32_t z_begin;    /* z-slab of one solid: cube layers [z_begin, z_end) of the solid's */
+    int32_t z_end;      /* grid, on corner planes z_begin..z_end (z_end == 0: the whole grid).
+                           The spacer, LookupEdgePoint and the border check stay those of the
+                           whole grid, so the slabs of a partition, meshed separately, give the
+                           whole mesh once the vertices that two neighbouring slabs share (the
+                           x and y edges of their common corner plane, equal bit for bit) are
+                           merged.  mc_search_device / mc_search only (the batch and the
+                           allocation-free calls return MC_ERR_ARG).  No counterpart in the
+                           reference: its z-slab ring runs inside one call (mc.go:614-645). */
+    int32_t reserved;
 } mc_opts;
 
 typedef struct mc_stats {

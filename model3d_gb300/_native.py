@@ -69,7 +69,8 @@ class MCMesh(ctypes.Structure):
 class MCOpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("cull", ctypes.c_int32),
                 ("tile_y", ctypes.c_int32), ("tile_z", ctypes.c_int32),
-                ("interior", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("interior", ctypes.c_int32), ("z_begin", ctypes.c_int32), ("z_end", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class MCTriSet(ctypes.Structure):

@@ -41,8 +41,11 @@
 #ifndef MC_CLASSIFY_MIN_BLOCKS
 #define MC_CLASSIFY_MIN_BLOCKS 3
 #endif
+#ifndef MC_CLASSIFY_WIDE_MIN_BLOCKS
+#define MC_CLASSIFY_WIDE_MIN_BLOCKS 2
+#endif
 #ifndef MC_SEARCH_MIN_BLOCKS
-#define MC_SEARCH_MIN_BLOCKS 4
+#define MC_SEARCH_MIN_BLOCKS 5
 #endif
 
 namespace mcgpu {
@@ -660,7 +663,16 @@ struct GridView {
     const double* xs;
     const double* ys;
     const double* zs;
+    const int32_t* lk[3];  // LookupEdgePoint codes per axis (edge_lookup_table), 2 per value
     int nx, ny, nz;
+    // A z-slab of a larger grid: local corner plane 0 is plane z0 of the
+    // grid (zs and lk[2] point at it); zb0 / zb1 say whether the first / last
+    // local plane is a border plane of the grid (1 / 1 for a whole grid).
+    int z0, zb0, zb1;
+    // Chunk layers: nz - 1 (one per cube layer), plus an edge-only layer on
+    // the last corner plane when that plane is not a grid border (a slab's
+    // top plane): its x and y edges can be crossed and are vertices there.
+    int nzc;
     int W;   // 32-bit words per row, including one zero padding word
     int CX;  // 32-cube chunks per row: ceil((nx-1)/32)
 };
@@ -801,7 +813,7 @@ __device__ __forceinline__ void classify_column(const GridView& g, const ProgVie
             if (rin) {
                 const int y = y0 + lane % a.ty, z = z0 + lane / a.ty;
                 a.bits[((size_t)z * g.ny + y) * g.W + tx] = m;
-                const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                const bool edge_row = (z == 0 && g.zb0) || (z == g.nz - 1 && g.zb1) || y == 0 || y == g.ny - 1;
                 if (m && (edge_row || (m & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
             }
             continue;
@@ -811,7 +823,7 @@ __device__ __forceinline__ void classify_column(const GridView& g, const ProgVie
             const int y = y0 + lane % a.ty, z = z0 + lane / a.ty;
             if (lane < rows && y < g.ny && z < g.nz) {
                 a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
-                const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                const bool edge_row = (z == 0 && g.zb0) || (z == g.nz - 1 && g.zb1) || y == 0 || y == g.ny - 1;
                 if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
             }
             continue;
@@ -828,7 +840,7 @@ __device__ __forceinline__ void classify_column(const GridView& g, const ProgVie
             if (lane == 0) {
                 a.bits[((size_t)z * g.ny + y) * g.W + tx] = word;
                 // solid is true outside of bounds (mc.go:687-689)
-                const bool edge_row = z == 0 || z == g.nz - 1 || y == 0 || y == g.ny - 1;
+                const bool edge_row = (z == 0 && g.zb0) || (z == g.nz - 1 && g.zb1) || y == 0 || y == g.ny - 1;
                 if (word && (edge_row || (word & edge_mask))) atomicOr(&a.err[ER_BORDER], 1);
             }
         }
@@ -837,7 +849,7 @@ __device__ __forceinline__ void classify_column(const GridView& g, const ProgVie
 
 // One warp per work item, items handed out by an atomic counter.
 template <int PREC>
-__global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify(GridView g, ProgView P, ClassifyArgs a) {
+__device__ __forceinline__ void classify_items(const GridView& g, const ProgView& P, const ClassifyArgs& a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (P.n_leaves + 31) >> 5;
@@ -859,6 +871,22 @@ __global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify(GridVi
     if (lane == 0 && nconst) atomicAdd(&a.stats[ST_TILES_CONST], nconst);
 }
 
+template <int PREC>
+__global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify(GridView g, ProgView P, ClassifyArgs a) {
+    classify_items<PREC>(g, P, a);
+}
+
+// The same with a larger register budget (fewer resident blocks): faster for
+// CSG programs, whose tiles spill at the tighter budget (headline tree:
+// 0.427 -> 0.401 ms).  A collider row costs a ray query per corner and a
+// metaball corner a sum over the balls; both want the resident warps
+// (1M-triangle collider 2.53 -> 2.97 ms, 64-ball metaball 9.2 -> 11.7 ms).
+template <int PREC>
+__global__ void __launch_bounds__(256, MC_CLASSIFY_WIDE_MIN_BLOCKS) k_classify_wide(GridView g, ProgView P,
+                                                                                   ClassifyArgs a) {
+    classify_items<PREC>(g, P, a);
+}
+
 // ------------------------------------------------------------ case table
 
 struct CaseTable {
@@ -877,11 +905,15 @@ __device__ __forceinline__ uint32_t valid_mask(const GridView& g, int c) {
 struct Rows {
     uint32_t r[4], n[4];  // rows (y,z), (y+1,z), (y,z+1), (y+1,z+1): word c and c+1
 };
+// On the edge-only layer (z == nz - 1) the rows above are absent: they read
+// as copies of the rows at z, so no z edge is crossed there (the callers also
+// emit no cube of that layer).
 __device__ __forceinline__ Rows load_rows(const GridView& g, const uint32_t* bits, int c, int y, int z) {
     Rows R;
     const size_t W = g.W;
-    size_t b00 = ((size_t)z * g.ny + y) * W + c;
-    size_t off[4] = {b00, b00 + W, b00 + (size_t)g.ny * W, b00 + (size_t)g.ny * W + W};
+    const size_t b00 = ((size_t)z * g.ny + y) * W + c;
+    const size_t up = z + 1 < g.nz ? (size_t)g.ny * W : 0;
+    const size_t off[4] = {b00, b00 + W, b00 + up, b00 + up + W};
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         R.r[k] = __ldg(bits + off[k]);
@@ -951,7 +983,7 @@ __device__ __forceinline__ void block_sum2(uint32_t& a, uint32_t& b) {
 constexpr int kChunkTY = 16, kChunkTZ = 16;
 
 __device__ __forceinline__ int chunk_index(const GridView& g, int c, int y, int z) {
-    const int nyc = g.ny - 1, nzc = g.nz - 1;
+    const int nyc = g.ny - 1, nzc = g.nzc;
     const int zb = z / kChunkTZ, yb = y / kChunkTY;
     const int hz = min(kChunkTZ, nzc - zb * kChunkTZ), hy = min(kChunkTY, nyc - yb * kChunkTY);
     return zb * kChunkTZ * nyc * g.CX + yb * kChunkTY * hz * g.CX + c * hy * hz + (z - zb * kChunkTZ) * hy +
@@ -959,7 +991,7 @@ __device__ __forceinline__ int chunk_index(const GridView& g, int c, int y, int 
 }
 
 __device__ __forceinline__ void chunk_coords(const GridView& g, int i, int* c, int* y, int* z) {
-    const int nyc = g.ny - 1, nzc = g.nz - 1;
+    const int nyc = g.ny - 1, nzc = g.nzc;
     const int zslab = kChunkTZ * nyc * g.CX;
     const int zb = i / zslab;
     int r = i - zb * zslab;
@@ -993,7 +1025,7 @@ __device__ __forceinline__ uint32_t count_chunk(const GridView& g, const uint32_
         all &= cp[k];
         anyb |= cp[k];
     }
-    uint32_t act = anyb & ~all & vm;
+    uint32_t act = z + 1 < g.nz ? anyb & ~all & vm : 0u;
     nt = 0;
     while (act) {
         const int b = __ffs(act) - 1;
@@ -1267,7 +1299,7 @@ __device__ __forceinline__ void emit_chunk(const GridView& g, const EmitArgs& a,
     // only the chunks inside the cube index space are read.
     auto base = [&](int dy, int dz, int w, uint32_t* bx, uint32_t* by, uint32_t* bz) {
         *bx = *by = *bz = 0;
-        if (y + dy > g.ny - 2 || z + dz > g.nz - 2 || c + w >= g.CX) return;
+        if (y + dy > g.ny - 2 || z + dz > g.nzc - 1 || c + w >= g.CX) return;
         const int ci = chunk_index(g, c + w, y + dy, z + dz);
         const uint32_t pv = a.prefv[ci], pn = a.packed[ci];
         *bx = pv;
@@ -1338,7 +1370,6 @@ __global__ void __launch_bounds__(256) k_emit_list(GridView g, EmitArgs a, const
 // ------------------------------------------------------------ k_search
 
 struct SearchArgs {
-    double inv_dl;  // 1 / (xs[1] - xs[0])
     const uint32_t* bits;  // the classification's corner bits
     const unsigned long long* keys;
     double* verts;  // V x 3
@@ -1368,86 +1399,28 @@ __device__ __forceinline__ double warp_max(double v) {
     return v;
 }
 
-// LookupEdgePoint (mc.go:647-660): the first axis i whose |fmod(c_i - o_i,
-// dl)| lies in (dl/4, 3dl/4), with idx = int((c_i - o_i) / dl).  Both the
-// band test and the truncation are decided from q = (c_i - o_i) * (1/dl)
-// when its fractional part is more than 1e-7 from the band edges: for
-// 0 <= q < 2^24 the error of q is below 3 * 2^-53 * 2^24 < 1e-8, and inside
-// the band the exact quotient is at least 1/4 from an integer, so the
-// correctly rounded quotient truncates to floor(q).  Otherwise the
-// reference's exact fmod and IEEE division decide.
+// LookupEdgePoint (mc.go:647-660) of the vertex on edge (ax; x, y, z): the
+// first axis i whose coordinate lies in the reference's band, read from the
+// host-built tables (edge_lookup_table): g.lk[i][2k] for a grid value k,
+// g.lk[i][2k+1] for the midpoint of edge k.  No float64 operation remains.
 // Returns 0 (found), 1 ("vertex not on edge") or 2 (index out of range).
-__device__ __forceinline__ int lookup_edge(const GridView& g, const P3& c, double inv_dl, int* axis, double* lo,
-                                           double* hi, long long* idx_out) {
-    const double org[3] = {g.xs[0], g.ys[0], g.zs[0]};
-    const double* vals[3] = {g.xs, g.ys, g.zs};
-    const int nvals[3] = {g.nx, g.ny, g.nz};
-    const double dl = D_SUB(g.xs[1], g.xs[0]);
+__device__ __forceinline__ int lookup_edge(const GridView& g, int ax, const int k[3], int* axis, int* idx_out) {
+#pragma unroll
     for (int i = 0; i < 3; i++) {
-        const double ci = comp(c, i);
-        int band = -1;  // -1 undecided, 0 outside, 1 inside
-        long long idx = 0;
-        // FP32 stage: |qf - q_exact| <= u(|c| + |o|)/dl + 3u qf < 2e-3 when
-        // the coordinates are below 2^12 delta (checked), so a fractional
-        // part farther than 2e-3 from 1/4, 3/4 and the integers decides.
-        {
-            const float cf = (float)ci, of = (float)org[i], idl = (float)inv_dl;
-            const float qf = (cf - of) * idl;
-            const float bnd = (fabsf(cf) + fabsf(of)) * idl;
-            if (qf >= 0.f && qf < 4096.f && bnd < 4096.f) {
-                const float nf = floorf(qf), fr = qf - nf;
-                if (fr > 0.252f && fr < 0.748f) {
-                    band = 1;
-                    idx = (long long)nf;
-                } else if (fr < 0.248f || fr > 0.752f) {
-                    band = 0;
-                }
-            }
-        }
-        if (band >= 0) {
-            if (band) {
-                if (idx < 0 || idx + 1 >= nvals[i]) return 2;
-                *axis = i;
-                *lo = vals[i][idx];
-                *hi = vals[i][idx + 1];
-                *idx_out = idx;
-                return 0;
-            }
-            continue;
-        }
-        const double av = D_SUB(ci, org[i]);
-        const double q = D_MUL(av, inv_dl);
-        if (av >= 0 && q < 16777216.0) {
-            const double n = floor(q);
-            const double fr = D_SUB(q, n);
-            if (fr > 0.2500001 && fr < 0.7499999) {
-                band = 1;
-                idx = (long long)n;
-            } else if (fr < 0.2499999 || fr > 0.7500001) {
-                band = 0;
-            }
-        }
-        if (band < 0) {
-            const double m = fabs(fmod(av, dl));
-            band = (m > D_MUL(dl, 0.25) && m < D_MUL(D_MUL(3.0, dl), 0.25)) ? 1 : 0;  // delta/4, 3*delta/4
-            if (band) idx = __double2ll_rz(D_DIV(av, dl));
-        }
-        if (band) {
-            if (idx < 0 || idx + 1 >= nvals[i]) return 2;
-            *axis = i;
-            *lo = vals[i][idx];
-            *hi = vals[i][idx + 1];
-            *idx_out = idx;
-            return 0;
-        }
+        const int code = g.lk[i][2 * k[i] + (i == ax ? 1 : 0)];
+        if (code == -1) continue;
+        if (code < 0) return 2;
+        *axis = i;
+        *idx_out = code;
+        return 0;
     }
     return 1;
 }
 
 // Vertex setup: edge key -> midpoint (corners[a].Mid(corners[b]),
-// mc.go:401-407) and, when iters != 0, LookupEdgePoint.  Returns the status.
+// mc.go:401-407) and, when lookup is set, LookupEdgePoint.  Returns the status.
 __device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* bits, unsigned long long key, bool lookup,
-                                            double inv_dl, P3* cpt, int* axis, double* lo, double* hi, int* hi_bit) {
+                                            P3* cpt, int* axis, double* lo, double* hi, int* hi_bit) {
     const int ax = (int)(key >> 60);
     const int z = (int)((key >> 40) & 0xfffff), y = (int)((key >> 20) & 0xfffff), x = (int)(key & 0xfffff);
     const P3 c0{g.xs[x], g.ys[y], g.zs[z]};
@@ -1465,16 +1438,22 @@ __device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* b
     *axis = 0;
     *hi_bit = -1;
     if (!lookup) return 0;
-    long long idx = -1;
-    const int st = lookup_edge(g, *cpt, inv_dl, axis, lo, hi, &idx);
+    const int k[3] = {x, y, z};
+    int idx = -1;
+    const int st = lookup_edge(g, ax, k, axis, &idx);
+    if (st != 0) return st;
+    // Table indices are the whole grid's (a slab's zs starts at plane z0).
+    const double* vals = *axis == 0 ? g.xs : (*axis == 1 ? g.ys : g.zs - g.z0);
+    *lo = vals[idx];
+    *hi = vals[idx + 1];
     // The first Contains of the bisection is at `hi`; when LookupEdgePoint
     // found this vertex's own edge that is grid corner (index + 1 along the
     // axis), whose bit the classification already wrote.
-    if (st == 0 && bits && *axis == ax && idx == (ax == 0 ? x : (ax == 1 ? y : z))) {
+    if (bits && *axis == ax && idx == k[ax] + (ax == 2 ? g.z0 : 0)) {
         const int cx = x + (ax == 0), cy = y + (ax == 1), cz = z + (ax == 2);
         *hi_bit = (int)((bits[((size_t)cz * g.ny + cy) * g.W + (cx >> 5)] >> (cx & 31)) & 1u);
     }
-    return st;
+    return 0;
 }
 
 // mcSearchPoint (mc.go:223-258) against a (folded) program; only the axis
@@ -1603,7 +1582,7 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search(GridView g
         P3 cpt{0, 0, 0};
         int hi_bit = -1;
         const bool lookup = a.iters != 0 || a.interior != nullptr;  // mc.go:182-185
-        int status = live ? vertex_setup(g, a.bits, a.keys[v], lookup, a.inv_dl, &cpt, &axis, &lo, &hi, &hi_bit) : 0;
+        int status = live ? vertex_setup(g, a.bits, a.keys[v], lookup, &cpt, &axis, &lo, &hi, &hi_bit) : 0;
         if (status == 1) atomicOr(&a.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&a.err[ER_EDGE_INDEX], 1);
         const bool work = live && lookup && status == 0;
@@ -1706,7 +1685,6 @@ struct JobD {
     long long nchunks;
     int iters;
     int pad;
-    double inv_dl;
 };
 
 // Last index k in [0, n) with off[k] <= x (off ascending, off[0] <= x).
@@ -1876,7 +1854,7 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(Batc
         P3 cpt{0, 0, 0};
         int hi_bit = -1;
         const int status =
-            live ? vertex_setup(Jp->g, Jp->ca.bits, keys[v], Jp->iters != 0, Jp->inv_dl, &cpt, &axis, &lo, &hi, &hi_bit)
+            live ? vertex_setup(Jp->g, Jp->ca.bits, keys[v], Jp->iters != 0, &cpt, &axis, &lo, &hi, &hi_bit)
                  : 0;
         if (status == 1) atomicOr(&Jp->ca.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&Jp->ca.err[ER_EDGE_INDEX], 1);
@@ -2051,7 +2029,7 @@ struct mc_ctx {
     int n_chunks = 0;
     long long chunk_end[kCopyChunks] = {};
     std::string err;
-    DevBuf xs, ys, zs, xf, yf, zf, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
+    DevBuf grid, bits, packed, blocksum, blockoff, prefv, preft, keys, verts, tris, stats, errs, totals;
     DevBuf nonempty;  // indices of the chunks with crossed edges (k_scan_chunks -> k_emit_list)
     DevBuf pts, pout;
     DevBuf inner, xsteps, stl;  // interior points of the last search; steps of mc_result_transform; STL bytes
@@ -2156,6 +2134,8 @@ mc_opts default_opts(const mc_opts* o) {
         r.tile_y = o->tile_y;
         r.tile_z = o->tile_z;
         r.interior = o->interior;
+        r.z_begin = o->z_begin;
+        r.z_end = o->z_end;
     }
     return r;
 }
@@ -2246,7 +2226,7 @@ void mc_destroy(mc_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     ctx->plan.reset();
-    for (DevBuf* b : {&ctx->xs, &ctx->ys, &ctx->zs, &ctx->xf, &ctx->yf, &ctx->zf, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
+    for (DevBuf* b : {&ctx->grid, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
                       &ctx->prefv, &ctx->preft, &ctx->keys, &ctx->verts, &ctx->tris, &ctx->stats, &ctx->errs,
                       &ctx->totals, &ctx->nonempty, &ctx->pts, &ctx->pout, &ctx->inner, &ctx->xsteps, &ctx->stl})
         b->release();
@@ -2441,7 +2421,13 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
         spacer_axis(H.root_min[1], H.root_max[1], delta, &Y, kMaxAxis + 1) ||
         spacer_axis(H.root_min[2], H.root_max[2], delta, &Z, kMaxAxis + 1))
         return fail(ctx, MC_ERR_GRID, "spacer does not terminate or exceeds the axis limit");
-    const int nx = (int)X.size(), ny = (int)Y.size(), nz = (int)Z.size();
+    const int nx = (int)X.size(), ny = (int)Y.size(), nzg = (int)Z.size();
+    // A z-slab: cube layers [z_begin, z_end) on corner planes z_begin..z_end.
+    const bool slab = opts.z_begin != 0 || opts.z_end != 0;
+    if (slab && !(opts.z_begin >= 0 && opts.z_end > opts.z_begin && opts.z_end <= nzg - 1))
+        return fail(ctx, MC_ERR_ARG, "z slab outside the grid's cube layers");
+    const int zb = slab ? opts.z_begin : 0;
+    const int nz = slab ? opts.z_end - opts.z_begin + 1 : nzg;
     if ((int64_t)nx * ny * nz > kMaxCorners) return fail(ctx, MC_ERR_GRID, "grid exceeds the corner limit");
     mc_stats st{};
     st.nx = nx;
@@ -2458,28 +2444,46 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     g.W = (nx + 31) / 32 + 1;
     g.CX = nx >= 2 ? (nx - 1 + 31) / 32 : 0;
     CK(cudaEventRecord(ctx->ev[0], sm));
-    CK(ctx->xs.ensure(nx * 8));
-    CK(ctx->ys.ensure(ny * 8));
-    CK(ctx->zs.ensure(nz * 8));
+    // The spacer (float64 and its float roundings) and the LookupEdgePoint
+    // tables, staged on the host and uploaded with one copy.
+    const size_t o_d = 0, o_f = align256((size_t)(nx + ny + nzg) * 8),
+                 o_l = o_f + align256((size_t)(nx + ny + nzg) * 4), grid_bytes = o_l + (size_t)(nx + ny + nzg) * 8;
+    std::vector<unsigned char> stage(grid_bytes, 0);
+    {
+        double* d = (double*)(stage.data() + o_d);
+        float* f = (float*)(stage.data() + o_f);
+        int32_t* l = (int32_t*)(stage.data() + o_l);
+        const double dl = nx >= 2 ? X[1] - X[0] : 1.0;  // LookupEdgePoint's delta (mc.go:649)
+        size_t at = 0;
+        for (const std::vector<double>* A : {&X, &Y, &Z}) {
+            for (size_t i = 0; i < A->size(); i++) {
+                d[at + i] = (*A)[i];
+                f[at + i] = (float)(*A)[i];
+            }
+            edge_lookup_table(*A, dl, l + 2 * at);
+            at += A->size();
+        }
+    }
+    CK(ctx->grid.ensure(grid_bytes));
+    CK(cudaMemcpyAsync(ctx->grid.p, stage.data(), grid_bytes, cudaMemcpyHostToDevice, sm));
     CK(ctx->stats.ensure(ST_N * 8));
     CK(ctx->errs.ensure(ER_N * 4));
     CK(ctx->totals.ensure(32));  // vertices, triangles, non-empty chunks, scan ticket
-    CK(cudaMemcpyAsync(ctx->xs.p, X.data(), nx * 8, cudaMemcpyHostToDevice, sm));
-    CK(cudaMemcpyAsync(ctx->ys.p, Y.data(), ny * 8, cudaMemcpyHostToDevice, sm));
-    CK(cudaMemcpyAsync(ctx->zs.p, Z.data(), nz * 8, cudaMemcpyHostToDevice, sm));
-    std::vector<float> XF(X.begin(), X.end()), YF(Y.begin(), Y.end()), ZF(Z.begin(), Z.end());
-    CK(ctx->xf.ensure(nx * 4));
-    CK(ctx->yf.ensure(ny * 4));
-    CK(ctx->zf.ensure(nz * 4));
-    CK(cudaMemcpyAsync(ctx->xf.p, XF.data(), nx * 4, cudaMemcpyHostToDevice, sm));
-    CK(cudaMemcpyAsync(ctx->yf.p, YF.data(), ny * 4, cudaMemcpyHostToDevice, sm));
-    CK(cudaMemcpyAsync(ctx->zf.p, ZF.data(), nz * 4, cudaMemcpyHostToDevice, sm));
     CK(cudaMemsetAsync(ctx->stats.p, 0, ST_N * 8, sm));
     CK(cudaMemsetAsync(ctx->errs.p, 0, ER_N * 4, sm));
     CK(cudaMemsetAsync(ctx->totals.p, 0, 32, sm));
-    g.xs = ctx->xs.as<double>();
-    g.ys = ctx->ys.as<double>();
-    g.zs = ctx->zs.as<double>();
+    unsigned char* gb = (unsigned char*)ctx->grid.p;
+    g.xs = (const double*)(gb + o_d);
+    g.ys = g.xs + nx;
+    g.zs = g.ys + ny + zb;
+    g.lk[0] = (const int32_t*)(gb + o_l);
+    g.lk[1] = g.lk[0] + 2 * nx;
+    g.lk[2] = g.lk[1] + 2 * ny + 2 * zb;
+    g.z0 = zb;
+    g.zb0 = zb == 0;
+    g.zb1 = zb + nz == nzg;
+    g.nzc = nz - 1 + (g.zb1 ? 0 : 1);
+    const float* gxf = (const float*)(gb + o_f);
     const size_t nbits = (size_t)nz * ny * g.W;
     CK(ctx->bits.ensure(nbits * 4));
     CK(cudaMemsetAsync(ctx->bits.p, 0, nbits * 4, sm));
@@ -2494,11 +2498,12 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     ca.prec = opts.precision;
     ca.cull = opts.cull;
     ca.work = (unsigned int*)(ctx->stats.as<unsigned long long>() + ST_WORK);
-    ca.xf = ctx->xf.as<float>();
-    ca.yf = ctx->yf.as<float>();
-    ca.zf = ctx->zf.as<float>();
+    ca.xf = gxf;
+    ca.yf = gxf + nx;
+    ca.zf = gxf + nx + ny + zb;
     const size_t smem_c = classify_smem(P);
-    auto kc = MC_PICK(k_classify, opts.precision, P.has_metaball);
+    auto kc = H.trees.empty() && H.metas.empty() ? MC_PICK(k_classify_wide, opts.precision, P.has_metaball)
+                                                 : MC_PICK(k_classify, opts.precision, P.has_metaball);
     if (smem_c > 48 * 1024) CK(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kc, 256, smem_c));
@@ -2517,7 +2522,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev[1], sm));
 
-    long long nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)g.CX * (ny - 1) * (nz - 1) : 0;
+    long long nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)g.CX * (ny - 1) * g.nzc : 0;
     const int nblk = (int)((nchunks + kChunksPerBlock - 1) / kChunksPerBlock);
     const int ngrp = (nblk + kScanGroup - 1) / kScanGroup;
     if (nchunks > 0) {
@@ -2566,7 +2571,6 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     CK(cudaEventRecord(ctx->ev[3], sm));
     if (V > 0) {
         SearchArgs sa{};
-        sa.inv_dl = nx >= 2 ? 1.0 / (X[1] - X[0]) : 0.0;
         sa.bits = ctx->bits.as<uint32_t>();
         sa.keys = ctx->keys.as<unsigned long long>();
         sa.verts = ctx->verts.as<double>();
@@ -2608,7 +2612,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     CK(cudaEventRecord(ctx->ev[4], sm));
     CK(cudaMemcpyAsync(hp + 8, ctx->stats.p, ST_N * 8, cudaMemcpyDeviceToHost, sm));
     CK(cudaMemcpyAsync(hp + 2, ctx->errs.p, ER_N * 4, cudaMemcpyDeviceToHost, sm));
-    st.h2d_bytes = (int64_t)(nx + ny + nz) * 8;
+    st.h2d_bytes = (int64_t)grid_bytes;
     st.d2h_bytes = 16 + 2 * ER_N * 4 + ST_N * 8;
     *stats = st;
     return MC_OK;
@@ -2998,6 +3002,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         if (!jobs[i].solid) return fail(ctx, MC_ERR_ARG, "null solid in batch");
     }
     if (n == 0) return MC_OK;
+    if (opts_in && (opts_in->z_begin || opts_in->z_end)) return fail(ctx, MC_ERR_ARG, "z slabs are for single calls");
     CK(cudaSetDevice(ctx->device));
     mc_opts opts = default_opts(opts_in);
     if (opts.tile_y <= 0) opts.tile_y = ctx->tuned_ty > 0 ? ctx->tuned_ty : kTileY;
@@ -3019,8 +3024,9 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         pl->pre_status.assign(n, MC_OK);
         std::vector<double> gd;
         std::vector<float> gf;
+        std::vector<int32_t> gl;  // LookupEdgePoint tables (edge_lookup_table)
         struct Lay {
-            size_t xd, yd, zd, xf, yf, zf, bits, nbits;
+            size_t xd, yd, zd, xf, yf, zf, xl, yl, zl, bits, nbits;
             long long items, cost;
         };
         std::vector<Lay> lay;
@@ -3053,6 +3059,8 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             J.g.nx = nx;
             J.g.ny = ny;
             J.g.nz = nz;
+            J.g.zb0 = J.g.zb1 = 1;
+            J.g.nzc = nz - 1;
             J.g.W = (nx + 31) / 32 + 1;
             J.g.CX = nx >= 2 ? (nx - 1 + 31) / 32 : 0;
             J.P = jobs[i].solid->view;
@@ -3064,7 +3072,6 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             J.ca.ntz = (nz + J.ca.tz - 1) / J.ca.tz;
             J.nchunks = (nx >= 2 && ny >= 2 && nz >= 2) ? (long long)J.g.CX * (ny - 1) * (nz - 1) : 0;
             J.iters = jobs[i].iters;
-            J.inv_dl = nx >= 2 ? 1.0 / (X[1] - X[0]) : 0.0;
             Lay L{};
             L.xd = gd.size();
             gd.insert(gd.end(), X.begin(), X.end());
@@ -3078,6 +3085,16 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             gf.insert(gf.end(), Y.begin(), Y.end());
             L.zf = gf.size();
             gf.insert(gf.end(), Z.begin(), Z.end());
+            {
+                const double dl = nx >= 2 ? X[1] - X[0] : 1.0;
+                size_t* at[3] = {&L.xl, &L.yl, &L.zl};
+                const std::vector<double>* A[3] = {&X, &Y, &Z};
+                for (int a = 0; a < 3; a++) {
+                    *at[a] = gl.size();
+                    gl.resize(gl.size() + 2 * A[a]->size());
+                    edge_lookup_table(*A[a], dl, gl.data() + *at[a]);
+                }
+            }
             L.nbits = (size_t)nz * ny * J.g.W;
             L.bits = nbits_total;
             nbits_total += L.nbits;
@@ -3092,8 +3109,8 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         const int nd = (int)pl->hjobs.size();
         pl->fold_words = fold_words;
         // Device buffers.
-        const size_t gd_bytes = gd.size() * 8, gf_off = align256(gd_bytes);
-        CK(pl->grid.ensure(gf_off + gf.size() * 4 + 8));
+        const size_t gd_bytes = gd.size() * 8, gf_off = align256(gd_bytes), gl_off = gf_off + align256(gf.size() * 4);
+        CK(pl->grid.ensure(gl_off + gl.size() * 4 + 8));
         CK(pl->bits.ensure(std::max<size_t>(nbits_total, 1) * 4));
         CK(pl->errs.ensure(std::max(nd, 1) * ER_N * 4));
         CK(pl->stats.ensure(ST_N * 8));
@@ -3110,6 +3127,9 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             J.ca.xf = (const float*)(gbase + gf_off) + L.xf;
             J.ca.yf = (const float*)(gbase + gf_off) + L.yf;
             J.ca.zf = (const float*)(gbase + gf_off) + L.zf;
+            J.g.lk[0] = (const int32_t*)(gbase + gl_off) + L.xl;
+            J.g.lk[1] = (const int32_t*)(gbase + gl_off) + L.yl;
+            J.g.lk[2] = (const int32_t*)(gbase + gl_off) + L.zl;
             J.ca.bits = pl->bits.as<uint32_t>() + L.bits;
             J.ca.err = pl->errs.as<int>() + d * ER_N;
             J.ca.stats = pl->stats.as<unsigned long long>();
@@ -3151,6 +3171,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         }
         CK(cudaMemcpyAsync(pl->grid.p, gd.data(), gd_bytes, cudaMemcpyHostToDevice, sm));
         CK(cudaMemcpyAsync(gbase + gf_off, gf.data(), gf.size() * 4, cudaMemcpyHostToDevice, sm));
+        if (!gl.empty()) CK(cudaMemcpyAsync(gbase + gl_off, gl.data(), gl.size() * 4, cudaMemcpyHostToDevice, sm));
         if (nd) CK(cudaMemcpyAsync(pl->jobs.p, pl->hjobs.data(), nd * sizeof(JobD), cudaMemcpyHostToDevice, sm));
         CK(cudaMemcpyAsync(pl->sched_off.p, sched_off.data(), sched_off.size() * 8, cudaMemcpyHostToDevice, sm));
         CK(cudaMemcpyAsync(pl->sched_job.p, sched_job.data(), sched_job.size() * 4, cudaMemcpyHostToDevice, sm));
@@ -3399,6 +3420,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
                                        int64_t* n_vertices, int64_t* n_triangles) {
     if (!nodes || n_nodes == 0 || iters < 0 || vertex_cap < 0 || triangle_cap < 0) return MC_ERR_ARG;
     if (opts_in && opts_in->interior) return MC_ERR_ARG;  // interior points need an array of their own
+    if (opts_in && (opts_in->z_begin || opts_in->z_end)) return MC_ERR_ARG;  // whole grids only
     if (n_vertices) *n_vertices = 0;
     if (n_triangles) *n_triangles = 0;
     int dev = 0;
@@ -3425,6 +3447,13 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         return MC_ERR_GRID;
     const int nx = (int)X.size(), ny = (int)Y.size(), nz = (int)Z.size();
     std::vector<float> XF(X.begin(), X.end()), YF(Y.begin(), Y.end()), ZF(Z.begin(), Z.end());
+    std::vector<int32_t> LK(2 * ((size_t)nx + ny + nz));
+    {
+        const double dl = nx >= 2 ? X[1] - X[0] : 1.0;  // LookupEdgePoint's delta (mc.go:649)
+        edge_lookup_table(X, dl, LK.data());
+        edge_lookup_table(Y, dl, LK.data() + 2 * nx);
+        edge_lookup_table(Z, dl, LK.data() + 2 * (nx + ny));
+    }
 
     // Carve the scratch array; refuse anything that does not fit.
     Carver cv{base};
@@ -3446,6 +3475,7 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
         {H.metas_f.data(), H.metas_f.size() * sizeof(MetaF), nullptr},
         {H.balls.data(), H.balls.size() * sizeof(BallD), nullptr},
         {H.balls_f.data(), H.balls_f.size() * sizeof(BallF), nullptr},
+        {LK.data(), LK.size() * 4, nullptr},
     };
     for (auto& p : up) p.dst = cv.take(p.bytes);
     int* errs = (int*)cv.take(ER_N * 4);
@@ -3455,6 +3485,8 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     g.nx = nx;
     g.ny = ny;
     g.nz = nz;
+    g.zb0 = g.zb1 = 1;
+    g.nzc = nz - 1;
     g.W = (nx + 31) / 32 + 1;
     g.CX = nx >= 2 ? (nx - 1 + 31) / 32 : 0;
     const size_t nbits = (size_t)nz * ny * g.W;
@@ -3488,6 +3520,9 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     g.xs = (const double*)up[8].dst;
     g.ys = (const double*)up[9].dst;
     g.zs = (const double*)up[10].dst;
+    g.lk[0] = (const int32_t*)up[19].dst;
+    g.lk[1] = g.lk[0] + 2 * nx;
+    g.lk[2] = g.lk[1] + 2 * ny;
     ProgView P{};
     P.ops = (const uint32_t*)up[0].dst;
     P.ops_allfalse = (const uint32_t*)up[1].dst;
@@ -3570,7 +3605,6 @@ extern "C" mc_status mc_search_noalloc(const mc_node* nodes, size_t n_nodes, dou
     }
     if (V > 0) {
         SearchArgs sa{};
-        sa.inv_dl = nx >= 2 ? 1.0 / (X[1] - X[0]) : 0.0;
         sa.bits = bits;
         sa.keys = (const unsigned long long*)keys_base;
         sa.verts = vertices;

@@ -1184,6 +1184,34 @@ int spacer_axis(double lo, double hi, double delta, std::vector<double>* out, in
     return MC_OK;
 }
 
+// LookupEdgePoint (model3d/mc.go:647-660) for one axis, decided ahead of the
+// search for every coordinate a vertex can have on that axis.  A vertex is the
+// midpoint (a + b) * 0.5 of its edge's corners (mc.go:401-407), so on its edge
+// axis the coordinate is (vals[k] + vals[k+1]) * 0.5 and on the other axes
+// (vals[k] + vals[k]) * 0.5, which is vals[k] unless the sum overflows.  For
+// each the reference's test -- |math.Mod(c - origin, delta)| strictly between
+// delta/4 and 3*delta/4, then idx = int((c - origin) / delta) -- is evaluated
+// here in float64 with the reference's operations: out[2k] for the grid value
+// k, out[2k+1] for the midpoint of edge k; -1 outside the band, -2 when
+// values[idx + 1] would be out of range, else idx.
+void edge_lookup_table(const std::vector<double>& vals, double delta, int32_t* out) {
+    const size_t n = vals.size();
+    const double origin = n ? vals[0] : 0.0;
+    auto code = [&](double c) -> int32_t {
+        const double av = c - origin;
+        const double m = std::fabs(std::fmod(av, delta));
+        if (!(m > delta / 4 && m < 3 * delta / 4)) return -1;
+        const double q = av / delta;
+        if (!(q >= 0) || q >= (double)n) return -2;
+        const int64_t idx = (int64_t)q;  // Go int(): truncation
+        return idx + 1 < (int64_t)n ? (int32_t)idx : -2;
+    };
+    for (size_t k = 0; k < n; k++) {
+        out[2 * k] = code((vals[k] + vals[k]) * 0.5);
+        out[2 * k + 1] = k + 1 < n ? code((vals[k] + vals[k + 1]) * 0.5) : -1;
+    }
+}
+
 // ---------------------------------------------------------------- case table
 
 namespace {

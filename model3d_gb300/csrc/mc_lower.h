@@ -60,6 +60,11 @@ double go_pow_int(double x, long y);
 // newSquareSpacer for one axis; MC_OK or MC_ERR_GRID.
 int spacer_axis(double lo, double hi, double delta, std::vector<double>* out, int64_t limit);
 
+// LookupEdgePoint of every grid value (out[2k]) and edge midpoint (out[2k+1])
+// of one spacer axis; delta = Xs[1] - Xs[0].  Codes: idx, -1 (not on an edge
+// along this axis), -2 (index out of range).  out holds 2 * vals.size().
+void edge_lookup_table(const std::vector<double>& vals, double delta, int32_t* out);
+
 // mcLookupTable; 0 when all 256 cases are covered without conflicts.
 int build_case_table(uint8_t counts[256], uint8_t tris[256][5][6]);
 

@@ -177,12 +177,14 @@ class Mesh:
         return float(abs(np.linalg.det(t).sum() / 6.0)) if len(t) else 0.0
 
 
-def _opts(precision="fp32", cull=True, tile_y=0, tile_z=0):
+def _opts(precision="fp32", cull=True, tile_y=0, tile_z=0, z_range=None):
     o = N.MCOpts()
     o.precision = N.MC_PREC_FP64 if precision in ("fp64", N.MC_PREC_FP64) else N.MC_PREC_FP32_FILTERED
     o.cull = 1 if cull else 0
     o.tile_y = int(tile_y)
     o.tile_z = int(tile_z)
+    if z_range is not None:
+        o.z_begin, o.z_end = int(z_range[0]), int(z_range[1])
     return o
 
 
@@ -224,11 +226,13 @@ class _HostMesh:
 
 def MarchingCubesSearch(solid, delta: float, iters: int, *, precision: str = "fp32",
                         cull: bool = True, ctx: Optional[Context] = None, tile_y: int = 0,
-                        tile_z: int = 0) -> Mesh:
-    """model3d.MarchingCubesSearch (model3d/mc.go:45-49) on the GPU."""
+                        tile_z: int = 0, z_range=None) -> Mesh:
+    """model3d.MarchingCubesSearch (model3d/mc.go:45-49) on the GPU.  With
+    z_range = (z_begin, z_end) only the cube layers [z_begin, z_end) of the
+    grid are meshed (a z-slab; see shard.py)."""
     ctx = ctx or (solid.ctx if isinstance(solid, DeviceSolid) else default_context())
     ds = _as_device_solid(solid, ctx)
-    o = _opts(precision, cull, tile_y, tile_z)
+    o = _opts(precision, cull, tile_y, tile_z, z_range)
     m = N.MCMesh()
     _check(N.lib().mc_search(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
                              ctypes.byref(m)), ctx.ptr)
