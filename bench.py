@@ -257,14 +257,14 @@ def run_ours(args):
     e2e_s = float(np.median(e2e_t))
 
     # Roofline of the dominant kernel.
+    pk = measure_peaks(ctx)
     phases = {k: float(np.mean([s[k] for s in sts]))
               for k in ("ms_classify", "ms_count", "ms_emit", "ms_search")}
     dom = max(phases, key=phases.get)
     peaks, kind = measured_peaks()
-    roof = roofline(dom, phases[dom], sts[0], peaks, kind)
+    roof = roofline(dom, phases[dom], sts[0], peaks, kind, pk[0])
 
     others = {} if args.no_extra else other_configs(ctx, torch, flush, value, args.collider_batch)
-    pk = measure_peaks(ctx)
 
     if rank == 0:
         cpu = None
@@ -276,8 +276,7 @@ def run_ours(args):
                    "sample": (f"oracle port, {threads} threads, one run over the whole grid "
                               f"({info['corners']} corners, {info['seconds']:.1f} s)")}
         s0 = sts[0]
-        alu = alu_roofline(s0, serialize(solid)[0], phases["ms_classify"] + phases["ms_search"], pk[0],
-                           info if cpu else None)
+        alu = alu_roofline(s0, phases["ms_classify"] + phases["ms_search"], pk[0], info if cpu else None)
         out = {
             "metric": METRIC, "value": value, "unit": "corners/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -394,13 +393,34 @@ def collider_line(ctx, torch, flush):
     a = _device_rate(L, N, ctx, cds, d, 8, N.MC_PREC_FP32_FILTERED, flush, torch, reps=2)
     b = _device_rate(L, N, ctx, cds, d, 8, N.MC_PREC_FP64, flush, torch, reps=1)
     tests = a["bvh_nodes"] + a["bvh_tris"]
+    # End to end through MarchingCubesSearch with host arrays: from the host
+    # triangles (MeshToCollider's lowering: grouping, tree, ray grid; upload;
+    # search; mesh copied back), and with the lowered solid resident.
+    from model3d_gb300 import MarchingCubesSearch
+    full, resident, m = [], [], None
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        m = MarchingCubesSearch(col, d, 8, ctx=ctx)
+        torch.cuda.synchronize()
+        full.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        m = MarchingCubesSearch(cds, d, 8, ctx=ctx)
+        torch.cuda.synchronize()
+        resident.append(time.perf_counter() - t)
+    e2e = {"from_host_triangles_ms": 1e3 * float(np.median(full)),
+           "solid_resident_ms": 1e3 * float(np.median(resident)),
+           "corners_per_s_from_host_triangles": a["corners"] / float(np.median(full)),
+           "corners_per_s_solid_resident": a["corners"] / float(np.median(resident)),
+           "h2d_bytes_solid": int(sum(t.nbytes for t in [tris]) + cds.nodes.nbytes),
+           "d2h_bytes": int(m.stats["d2h_bytes"])}
     return {"collider_icosphere_1048820_tris_256cubed": {
         "grid": [a["nx"], a["ny"], a["nz"]], "triangles_in": len(tris), "triangles_out": a["triangles"],
         "fp32_corners_per_s": a["corners"] / (a["ms_total"] / 1e3),
         "fp64_corners_per_s": b["corners"] / (b["ms_total"] / 1e3),
         "ms_fp32": a["ms_total"], "ms_fp64": b["ms_total"],
         "escalation_rate": a["escalations"] / max(1, tests), "bvh_box_tests": a["bvh_nodes"],
-        "triangle_tests": a["bvh_tris"], "host_lowering_s": lower_s}}
+        "triangle_tests": a["bvh_tris"], "host_lowering_s": lower_s, "e2e": e2e}}
 
 
 def batch_line(ctx, torch, flush, single_rate):
@@ -516,59 +536,70 @@ def collider_batch_line(ctx, count):
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
-# each kernel on this workload, from an ncu capture of the full-size grid.
-# Below the algorithmic bytes where a kernel reads what the previous one
-# left in the 129 MB L2 (keys, corner bits) or its writes stay in L2.
-NCU_TRAFFIC = {"k_classify": 14012416, "k_count": 29758976, "k_emit": 69824768, "k_search": 39974144}
+# each kernel on this workload, from the ncu capture of the full-size grid
+# summarised in profiles/launches_csg48_delta0.004.md (same kernels as this
+# source).  Below the algorithmic bytes where a kernel reads what the previous
+# one left in the 129 MB L2 (keys, corner bits) or its writes stay in L2.
+NCU_TRAFFIC = {}
 
 
-def roofline(kernel, ms, st, peaks, kind):
-    """Algorithmic bytes of one launch of the dominant kernel over its CUDA-
-    event time, against the measured HBM copy bandwidth.  The kernels are
-    bound by issue latency of the predicate interpreter (ALU), not by HBM,
-    so the fraction is small by construction."""
+def algorithmic_bytes(kernel, st):
+    """Bytes a kernel must move per launch: corner bits, chunk counts and
+    offsets, keys, vertices and triangles."""
     nx, ny, nz = st["nx"], st["ny"], st["nz"]
     W = (nx + 31) // 32 + 1
     bits = nz * ny * W * 4
     chunks = ((nx - 1 + 31) // 32) * (ny - 1) * (nz - 1)
     V, T = st["vertices"], st["triangles"]
-    if kernel == "ms_classify":
-        alg = bits                                  # one bit per corner written
-    elif kernel == "ms_count":
-        alg = bits + chunks * 4 * 3                 # bits read; counts + 2 prefixes written
-    elif kernel == "ms_emit":
-        alg = bits + chunks * 12 + V * 8 + T * 12   # bits + offsets read; keys, triangles written
-    else:
-        alg = V * 8 + V * 24                        # keys read, vertices written
-    achieved = alg / (ms / 1000.0) / 1e9
-    peak = float(peaks.get("hbm_gbs", 6800.0))
+    if kernel == "k_classify":
+        return bits                                  # one bit per corner written
+    if kernel == "k_count":
+        return bits + chunks * 4 * 3                 # bits read; counts + 2 prefixes written
+    if kernel == "k_emit":
+        return bits + chunks * 12 + V * 8 + T * 12   # bits + offsets read; keys, triangles written
+    return V * 8 + V * 24                            # keys read, vertices written
+
+
+def roofline(kernel, ms, st, peaks, kind, fp32_tflops):
+    """The dominant kernel against the bound that limits it.  Classification
+    and search evaluate leaf predicates: their bound is the FP32 ALU, and
+    `achieved` is the float operations of the reference formulas of the
+    leaves they evaluated (their own device counter, weighted by kind) over
+    the kernel's event time, against the FP32 peak measured on this GPU.  The
+    HBM figures of the same launch ride along under `hbm`.  Count, scan and
+    emission are bound by HBM / L2 and report against the measured copy
+    bandwidth."""
     name = kernel.replace("ms_", "k_")
-    return {"kernel": name, "bound": "hbm", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": NCU_TRAFFIC.get(name),
-            "algorithmic_bytes": int(alg), "ms": ms, "peak_kind": kind}
+    alg = algorithmic_bytes(name, st)
+    gbs = alg / (ms / 1000.0) / 1e9
+    peak_hbm = float(peaks.get("hbm_gbs", 6800.0))
+    hbm = {"achieved": gbs, "peak": peak_hbm, "unit": "GB/s", "frac": gbs / peak_hbm,
+           "algorithmic_bytes": int(alg), "traffic": NCU_TRAFFIC.get(name), "peak_kind": kind}
+    if name in ("k_classify", "k_search"):
+        flops = st["flops_search" if name == "k_search" else "flops_classify"]
+        tf = flops / (ms / 1000.0) / 1e12
+        return {"kernel": name, "bound": "alu_fp32", "achieved": tf, "peak": fp32_tflops, "unit": "TFLOP/s",
+                "frac": tf / fp32_tflops, "traffic": NCU_TRAFFIC.get(name), "flops": int(flops), "ms": ms,
+                "peak_kind": "measured on this GPU (mc_measure_peaks: dense FP32 FMA loop)", "hbm": hbm}
+    return {"kernel": name, "bound": "hbm", "achieved": gbs, "peak": peak_hbm, "unit": "GB/s",
+            "frac": gbs / peak_hbm, "traffic": NCU_TRAFFIC.get(name), "algorithmic_bytes": int(alg), "ms": ms,
+            "peak_kind": kind}
 
 
-# Float operations of one leaf predicate (precomputed constants; compares
-# count as operations): Sphere 9 + 1, Rect 6, Cylinder 21 + 2, Capsule 21 + 2,
-# Torus about 36.
-LEAF_FLOPS = {1: 10, 2: 6, 3: 23, 4: 23, 5: 36}
-
-
-def alu_roofline(st, nodes, ms, fp32_tflops, ref=None):
-    """Float operations of the leaf evaluations the classification and search
-    kernels performed (their own counter, times the mean operation count of
-    the solid's leaf kinds) over those kernels' event time, against the
-    measured FP32 peak (dense FMA loop).  With ref (the oracle's leaf
-    evaluations per corner on a sample of the same grid) it adds the
-    operations the reference's short-circuit evaluation performs for the
-    whole grid, over the same time: tile culling skips most of them."""
-    kinds = [int(k) for k in nodes["kind"] if int(k) in LEAF_FLOPS]
-    per_leaf = sum(LEAF_FLOPS[k] for k in kinds) / max(1, len(kinds))
-    flops = st["leaf_evals"] * per_leaf
+def alu_roofline(st, ms, fp32_tflops, ref=None):
+    """Float operations of the reference formulas of the leaves that the
+    classification and search kernels evaluated (their device counters,
+    weighted by kind: Sphere 10, Rect 6, Cylinder and Capsule 23, Torus 36)
+    over those kernels' event time, against the measured FP32 peak.  With
+    ref (the oracle's leaf evaluations per corner over the same grid) it adds
+    the operations of the reference's short-circuit evaluation of the whole
+    grid, over the same time: tile culling skips most of them."""
+    flops = st["flops_classify"] + st["flops_search"]
     achieved = flops / (ms / 1000.0) / 1e12
+    per_leaf = flops / max(1, st["leaf_evals"])
     out = {"bound": "fp32_alu", "kernels": ["k_classify", "k_search"], "achieved": achieved,
            "peak": fp32_tflops, "unit": "TFLOP/s", "frac": achieved / fp32_tflops,
-           "leaf_evals": int(st["leaf_evals"]), "flops_per_leaf_eval": per_leaf, "ms": ms,
+           "leaf_evals": int(st["leaf_evals"]), "flops": int(flops), "flops_per_leaf_eval": per_leaf, "ms": ms,
            "peak_kind": "measured on this GPU (mc_measure_peaks)"}
     if ref:
         ref_flops = ref["leaf_evals"] / ref["corners"] * st["corners"] * per_leaf
@@ -585,7 +616,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extra", action="store_true", help="skip the other configurations")
-    ap.add_argument("--collider-batch", type=int, default=16,
+    ap.add_argument("--collider-batch", type=int, default=64,
                     help="meshes in the batched-collider line (64 = the full configuration)")
     args = ap.parse_args()
     if args.warmup < 3:

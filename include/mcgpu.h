@@ -192,6 +192,9 @@ typedef struct mc_stats {
     double ms_total;         /* first upload to last kernel, including the totals read-back */
     int64_t h2d_bytes;       /* host-to-device bytes of the call */
     int64_t d2h_bytes;       /* device-to-host bytes of the call (incl. the mesh for mc_search) */
+    int64_t flops_classify;  /* float operations of the reference formulas of the leaves the */
+    int64_t flops_search;    /* classification / search evaluated (Sphere 10, Rect 6, Cylinder and
+                                Capsule 23, Torus 36 per evaluation; colliders and metaballs 0) */
 } mc_stats;
 
 /* Indexed mesh: vertices n_vertices x 3 float64, triangles n_triangles x 3

@@ -53,7 +53,7 @@ class MCStats(ctypes.Structure):
         "tiles", "tiles_const", "bvh_nodes", "bvh_tris")] + [
         (n, ctypes.c_double) for n in ("ms_classify", "ms_count", "ms_emit", "ms_search",
                                        "ms_total")] + [
-        (n, ctypes.c_int64) for n in ("h2d_bytes", "d2h_bytes")]
+        (n, ctypes.c_int64) for n in ("h2d_bytes", "d2h_bytes", "flops_classify", "flops_search")]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -54,19 +54,32 @@ namespace mcgpu {
 
 struct Counts {
     unsigned long long leaf = 0, esc = 0, nodes = 0, tris = 0;
+    uint32_t flops = 0;  // operations of the reference formulas of the evaluated leaves (leaf_flops)
 };
 
-enum StatSlot { ST_LEAF = 0, ST_ESC, ST_NODES, ST_TRIS, ST_TILES_CONST, ST_WORK, ST_N };
+enum StatSlot { ST_LEAF = 0, ST_ESC, ST_NODES, ST_TRIS, ST_TILES_CONST, ST_WORK, ST_FLOPS_CLASSIFY, ST_FLOPS_SEARCH, ST_N };
 enum ErrSlot { ER_BORDER = 0, ER_NOT_ON_EDGE, ER_EDGE_INDEX, ER_N };
 
-__device__ __forceinline__ void flush_counts(const Counts& c, unsigned long long* stats) {
-    unsigned long long v[4] = {c.leaf, c.esc, c.nodes, c.tris};
+// Float operations of one leaf predicate as the reference computes it, with
+// the constants precomputed (compares count): Sphere 9 + 1, Rect 6,
+// Cylinder 21 + 2, Capsule 21 + 2, Torus about 36.  Colliders and metaballs
+// count 0: their work is tree and triangle traffic and ball sums.  Six bits
+// per kind, so the count is a shift and a mask.
+__device__ __forceinline__ uint32_t leaf_flops(int kind) {
+    constexpr unsigned long long K = (10ull << (6 * LK_SPHERE)) | (6ull << (6 * LK_RECT)) |
+                                     (23ull << (6 * LK_CYLINDER)) | (23ull << (6 * LK_CAPSULE)) |
+                                     (36ull << (6 * LK_TORUS));
+    return (uint32_t)((K >> (6 * kind)) & 63u);
+}
+
+__device__ __forceinline__ void flush_counts(const Counts& c, unsigned long long* stats, int flop_slot) {
+    unsigned long long v[5] = {c.leaf, c.esc, c.nodes, c.tris, c.flops};
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
+    for (int i = 0; i < 5; i++) {
         unsigned long long x = v[i];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if ((threadIdx.x & 31) == 0 && x) atomicAdd(&stats[i], x);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(&stats[i < 4 ? i : flop_slot], x);
     }
 }
 
@@ -209,6 +222,7 @@ __device__ __noinline__ bool leaf64_point(const ProgView& P, int id, P3 p, Count
 template <int PREC>
 __device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf, Counts& cnt, int* err) {
     cnt.leaf++;
+    cnt.flops += leaf_flops(P.leaf_kind[id]);
     if (mode_f32(PREC)) {
         const int kind = P.leaf_kind[id];
         if (kind <= LK_TORUS) {
@@ -569,6 +583,7 @@ __device__ __forceinline__ uint32_t leaf_rows(const ProgView& P, int id, const R
     const double* d = P.leaf_d + (size_t)id * LEAF_D;
     const float* f = P.leaf_f + (size_t)id * LEAF_F;
     cnt.leaf += rc.nrows;
+    cnt.flops += rc.nrows * leaf_flops(kind);
     constexpr bool f32 = mode_f32(PREC);
     switch (kind) {
         case LK_RECT: return rect_rows(d, rc);
@@ -867,7 +882,7 @@ __device__ __forceinline__ void classify_items(const GridView& g, const ProgView
         if (item >= nitems) break;
         classify_column<PREC>(g, P, a, item, q, cur, prev, cnt, nconst);
     }
-    flush_counts(cnt, a.stats);
+    flush_counts(cnt, a.stats, ST_FLOPS_CLASSIFY);
     if (lane == 0 && nconst) atomicAdd(&a.stats[ST_TILES_CONST], nconst);
 }
 
@@ -1603,7 +1618,7 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search(GridView g
         }
         __syncwarp();
     }
-    flush_counts(cnt, a.stats);
+    flush_counts(cnt, a.stats, ST_FLOPS_SEARCH);
 }
 
 // ------------------------------------------------------------ k_apply_steps
@@ -1666,7 +1681,7 @@ __global__ void k_contains(ProgView P, const double* pts, long long n, uint8_t* 
         P3 p{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
         out[i] = eval_program<PREC>(P, P.ops, P.n_ops, p, to_f3(p), cnt, err) ? 1 : 0;
     }
-    flush_counts(cnt, stats);
+    flush_counts(cnt, stats, ST_FLOPS_CLASSIFY);
 }
 
 // ------------------------------------------------------------ batched launch
@@ -1750,7 +1765,7 @@ __global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify_batch(
         uint32_t* cur = base + J.P.fold_cap;
         classify_column<PREC>(J.g, J.P, J.ca, (int)(item - b.sched_off[k]), base, cur, cur + nw, cnt, nconst);
     }
-    flush_counts(cnt, b.stats);
+    flush_counts(cnt, b.stats, ST_FLOPS_CLASSIFY);
     if (lane == 0 && nconst) atomicAdd(&b.stats[ST_TILES_CONST], nconst);
 }
 
@@ -1893,7 +1908,7 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(Batc
         }
         __syncwarp();
     }
-    flush_counts(cnt, b.stats);
+    flush_counts(cnt, b.stats, ST_FLOPS_SEARCH);
 }
 
 // ------------------------------------------------------------ peak probes
@@ -2630,6 +2645,8 @@ mc_status search_finish(mc_ctx* ctx, mc_stats* stats) {
     st.bvh_nodes = (int64_t)hp[8 + ST_NODES];
     st.bvh_tris = (int64_t)hp[8 + ST_TRIS];
     st.tiles_const = (int64_t)hp[8 + ST_TILES_CONST];
+    st.flops_classify = (int64_t)hp[8 + ST_FLOPS_CLASSIFY];
+    st.flops_search = (int64_t)hp[8 + ST_FLOPS_SEARCH];
     float ms;
     cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[1]);
     st.ms_classify = ms;
@@ -3349,6 +3366,8 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         m.stats.bvh_nodes = (int64_t)hstats[ST_NODES];
         m.stats.bvh_tris = (int64_t)hstats[ST_TRIS];
         m.stats.tiles_const = (int64_t)hstats[ST_TILES_CONST];
+        m.stats.flops_classify = (int64_t)hstats[ST_FLOPS_CLASSIFY];
+        m.stats.flops_search = (int64_t)hstats[ST_FLOPS_SEARCH];
         m.stats.ms_total = ms_total;
         m.stats.d2h_bytes = nv * 24 + nt * 12;
     }
