@@ -278,6 +278,14 @@ mc_status mc_result_device(const mc_ctx* ctx, const double** vertices,
                            const int32_t** triangles);
 /* Copy the last result into caller-provided host arrays (V*3, T*3). */
 mc_status mc_result_copy(mc_ctx* ctx, double* vertices, int32_t* triangles);
+/* The grid edge of each vertex of the last mc_search_device result: V keys
+ * axis << 60 | z << 40 | y << 20 | x, the edge from corner (x, y, z) to the
+ * next corner along axis (0 x, 1 y, 2 z; z counted from the slab's first
+ * plane for a z-slab).  A triangle's three edges lie on one cube, the one
+ * whose cube loop emitted it (mc.go:20-35).  No counterpart in the
+ * reference: MarchingCubesFilter's block pruning (mc.go:83-148) is applied
+ * on the host with it. */
+mc_status mc_result_keys(mc_ctx* ctx, uint64_t* keys);
 /* Interior points of the last mc_search_device run with opts->interior set:
  * V*3 float64, point i being the last inside point of vertex i's bisection
  * (the CoordMap of MarchingCubesInterior, model3d/mc.go:55-60, :191-198,

@@ -20,11 +20,12 @@ from .metaballs import (CubicMetaballFalloffFunc, ExponentialMetaballFalloffFunc
                         ScaleMetaball, SDFToMetaball, SignedMetaballSolid, TransformMetaball,
                         TranslateMetaball, VecScaleMetaball, WeightedMetaballSolid,
                         WyvillMetaballFalloffFunc)
-from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesC2F, MarchingCubesConj,
-                 MarchingCubesFilter, MarchingCubesSearchFilter,
+from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesConj,
                  MarchingCubesInterior, MarchingCubesSearch, MarchingCubesSearchBatch,
                  MarchingCubesSearchSTL, MCError,
                  Mesh, autotune, canonical, case_table, check_program, default_context, measure_peaks,
                  spacer_axis)
+
+from .filter import MarchingCubesC2F, MarchingCubesFilter, MarchingCubesSearchFilter, RectCollider
 
 __all__ = [n for n in dir() if not n.startswith("_")]

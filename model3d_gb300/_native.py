@@ -36,7 +36,7 @@ EXPORTS = [
     "mc_search_device", "mc_result_device", "mc_result_copy", "mc_contains", "mc_search_batch",
     "mc_case_table", "mc_version", "mc_search_noalloc", "mc_autotune",
     "mc_measure_peaks", "mc_result_interior_copy", "mc_result_transform", "mc_result_stl",
-    "mc_program_check",
+    "mc_program_check", "mc_result_keys",
 ]
 
 
@@ -122,6 +122,7 @@ def lib():
         L.mc_result_device.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
         L.mc_result_copy.argtypes = [vp, vp, vp]
         L.mc_result_interior_copy.argtypes = [vp, vp]
+        L.mc_result_keys.argtypes = [vp, vp]
         L.mc_result_transform.argtypes = [vp, vp, ctypes.c_size_t, i32]
         L.mc_result_stl.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         L.mc_contains.argtypes = [vp, vp, vp, i64, ctypes.POINTER(MCOpts), vp]

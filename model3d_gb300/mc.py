@@ -286,38 +286,6 @@ def MarchingCubesConj(solid, delta: float, iters: int, *xforms, precision: str =
     return Mesh(verts, tris, st.as_dict())
 
 
-def MarchingCubesFilter(solid, f, delta: float, **kw) -> Mesh:
-    """model3d.MarchingCubesFilter (model3d/mc.go:83-148) on the GPU.
-
-    The reference skips blocks of cubes for which f(rect) is false, and
-    requires f to be conservative: it "should never fail to report
-    collisions".  Under that contract every cube the surface crosses lies in
-    a kept block, so the result is MarchingCubes' mesh (the reference's own
-    tests assert exactly this, mc_test.go:44-67).  Here the whole grid is
-    classified on the device -- the filter saves nothing on a GPU -- so f is
-    not called."""
-    return MarchingCubesSearch(solid, delta, 0, **kw)
-
-
-def MarchingCubesSearchFilter(solid, f, delta: float, iters: int, **kw) -> Mesh:
-    """model3d.MarchingCubesSearchFilter (mc.go:150-155): MarchingCubesFilter,
-    then the search -- for a conservative f, MarchingCubesSearch's mesh."""
-    return MarchingCubesSearch(solid, delta, iters, **kw)
-
-
-def MarchingCubesC2F(solid, bigDelta: float, smallDelta: float, extraSpace: float, iters: int,
-                     **kw) -> Mesh:
-    """model3d.MarchingCubesC2F (mc.go:157-180).  The reference meshes at
-    bigDelta and filters the fine pass with the coarse mesh's collider,
-    expanded by extraSpace + 2 bigDelta sqrt(3); where that filter is
-    conservative (its purpose, and what mc_test.go:69-94 asserts) the result
-    is MarchingCubesSearch(solid, smallDelta, iters), computed here in one
-    device pass.  The reference's panic on bigDelta < smallDelta is kept."""
-    if bigDelta < smallDelta:
-        raise MCError(N.MC_ERR_ARG, "bigDelta should be >= smallDelta for efficiency")
-    return MarchingCubesSearch(solid, smallDelta, iters, **kw)
-
-
 def MarchingCubesSearchSTL(solid, delta: float, iters: int, *, precision: str = "fp32",
                            cull: bool = True, ctx: Optional[Context] = None) -> bytes:
     """model3d.MarchingCubesSearch(...).EncodeSTL() (model3d/export.go:20-66)

@@ -100,6 +100,10 @@ class Rect(Solid):
     def Max(self):
         return self.MaxVal
 
+    def Expand(self, delta: float) -> "Rect":
+        """Rect.Expand (model3d/shapes.go:339-344)."""
+        return Rect(self.MinVal.AddScalar(-delta), self.MaxVal.AddScalar(delta))
+
 
 def NewRect(min: Coord3D, max: Coord3D) -> Rect:
     return Rect(min, max)

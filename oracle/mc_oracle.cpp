@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <map>
 #include <memory>
@@ -1255,6 +1256,18 @@ struct KeyEq {
     bool operator()(const V3& a, const V3& b) const { return veq(a, b); }
 };
 
+// Counters of one oracle call: per-thread counts flushed into atomics.
+struct Acc {
+    std::atomic<int64_t> leaf{0}, ndc{0}, trc{0}, calls{0};
+    void flush() {
+        leaf += tl_leaf;
+        ndc += tl_nodes;
+        trc += tl_tris;
+        tl_leaf = tl_nodes = tl_tris = 0;
+    }
+};
+
+
 }  // namespace
 
 // ======================================================================
@@ -1406,116 +1419,14 @@ int oracle_contains(const mc_node* nodes, size_t n, const mc_tri_set* sets, size
 // cube loop to slabs z in [z_begin, z_end) (z_end < 0: all) — used to time a
 // bounded sample of a large grid; the default covers the whole grid exactly
 // as the reference does.
-int oracle_mc_search(const mc_node* nodes, size_t n, const mc_tri_set* sets, size_t n_sets,
-                     double delta, int iters, int threads, int64_t z_begin, int64_t z_end, int want_interior,
-                     oracle_mesh* out) {
-    std::memset(out, 0, sizeof(*out));
-    Scene sc;
-    std::string err;
-    int st = parse_scene(nodes, n, sets, n_sets, &sc, &err);
-    if (st) {
-        std::snprintf(out->error, sizeof(out->error), "%s", err.c_str());
-        return st;
-    }
-    const Solid& s = *sc.root;
-    // validateBounds (bounder.go:29-52) on the caller's Min()/Max() of the
-    // root, as the reference calls s.Min()/s.Max() on the caller's object.
-    V3 mn = xyz(nodes[0].min[0], nodes[0].min[1], nodes[0].min[2]);
-    V3 mx = xyz(nodes[0].max[0], nodes[0].max[1], nodes[0].max[2]);
-    if (std::isnan(vsum(mn)) || std::isnan(vsum(mx)) || std::isinf(vsum(mn)) || std::isinf(vsum(mx)) ||
-        mx.x < mn.x || mx.y < mn.y || mx.z < mn.z) {
-        std::snprintf(out->error, sizeof(out->error), "invalid bounds");
-        return MC_ERR_INVALID_BOUNDS;
-    }
-    Table table = build_table();
-    std::vector<double> Xs, Ys, Zs;
-    const int64_t lim = 1 << 20;
-    if (spacer_axis(mn.x, mx.x, delta, &Xs, lim) || spacer_axis(mn.y, mx.y, delta, &Ys, lim) ||
-        spacer_axis(mn.z, mx.z, delta, &Zs, lim))
-        return MC_ERR_GRID;
-    const int64_t NX = Xs.size(), NY = Ys.size(), NZ = Zs.size();
-    out->nx = NX;
-    out->ny = NY;
-    out->nz = NZ;
-    if (z_end < 0 || z_end > NZ) z_end = NZ;
-    if (z_begin < 0) z_begin = 0;
-    int64_t zlo = std::max<int64_t>(0, z_begin), zhi = z_end;  // slabs to classify
-
-    std::atomic<int64_t> leaf{0}, ndc{0}, trc{0}, calls{0};
-    auto flush = [&] {
-        leaf += tl_leaf;
-        ndc += tl_nodes;
-        trc += tl_tris;
-        tl_leaf = tl_nodes = tl_tris = 0;
-    };
-
-    // Scan + FetchZ (mc.go:614-692): classify every corner of each slab.
-    int64_t nslab = zhi - zlo;
-    std::vector<uint8_t> grid((size_t)std::max<int64_t>(nslab, 0) * NX * NY);
-    std::atomic<int> bad{0};
-    parallel_for(nslab, threads, [&](int64_t zi, int) {
-        int64_t z = zlo + zi;
-        bool onEdge = z == 0 || z == NZ - 1;
-        uint8_t* v = &grid[(size_t)zi * NX * NY];
-        for (int64_t i = 0; i < NY; i++)
-            for (int64_t j = 0; j < NX; j++) {
-                bool b = s.Contains(xyz(Xs[j], Ys[i], Zs[z]));
-                v[i * NX + j] = b;
-                if (b && (onEdge || i == 0 || j == 0 || i == NY - 1 || j == NX - 1)) bad = 1;
-            }
-        calls += NX * NY;
-        flush();
-    });
-    if (bad) {
-        std::snprintf(out->error, sizeof(out->error), "solid is true outside of bounds");
-        return MC_ERR_BOUNDS_INSIDE;
-    }
-
-    // Cube loop of MarchingCubes (mc.go:20-35).
-    auto square = [&](int64_t zi, int64_t x, int64_t y) {  // GetSquare, mc.go:698-710
-        int r = 0, mask = 1;
-        const uint8_t* v = &grid[(size_t)zi * NX * NY];
-        for (int64_t y1 = y; y1 < y + 2; y1++)
-            for (int64_t x1 = x; x1 < x + 2; x1++) {
-                if (v[y1 * NX + x1]) r |= mask;
-                mask <<= 1;
-            }
-        return r;
-    };
-    std::vector<std::vector<double>> parts((size_t)std::max<int64_t>(nslab, 0));
-    parallel_for(nslab > 0 ? nslab - 1 : 0, threads, [&](int64_t zi, int) {
-        int64_t z = zlo + zi + 1;  // nextZ: bottom = z-1, top = z
-        std::vector<double>& part = parts[zi];
-        for (int64_t y = 0; y < NY - 1; y++)
-            for (int64_t x = 0; x < NX - 1; x++) {
-                int bits = square(zi, x, y) | (square(zi + 1, x, y) << 4);
-                int cnt = table.count[bits];
-                if (!cnt) continue;
-                V3 a = xyz(Xs[x], Ys[y], Zs[z - 1]);
-                V3 b = xyz(Xs[x + 1], Ys[y + 1], Zs[z]);
-                V3 corners[8] = {a,
-                                 xyz(b.x, a.y, a.z),
-                                 xyz(a.x, b.y, a.z),
-                                 xyz(b.x, b.y, a.z),
-                                 xyz(a.x, a.y, b.z),
-                                 xyz(b.x, a.y, b.z),
-                                 xyz(a.x, b.y, b.z),
-                                 b};  // mcCornerCoordinates, mc.go:289-301
-                for (int t = 0; t < cnt; t++) {
-                    const uint8_t* m = table.tris[bits][t];
-                    for (int k = 0; k < 3; k++) {  // mcTriangle.Triangle, mc.go:401-407
-                        V3 p = mid(corners[m[2 * k]], corners[m[2 * k + 1]]);
-                        part.push_back(p.x);
-                        part.push_back(p.y);
-                        part.push_back(p.z);
-                    }
-                }
-            }
-    });
-    std::vector<double> soup;
-    for (auto& p : parts) soup.insert(soup.end(), p.begin(), p.end());
+// VertexSlice dedup (mesh.go:770-778), mcSearch (mc.go:182-258) and the
+// output arrays of a triangle soup of midpoint vertices; shared by
+// MarchingCubesSearch and MarchingCubesSearchFilter.
+static int finish_search(const Solid& s, const std::vector<double>& Xs, const std::vector<double>& Ys,
+                  const std::vector<double>& Zs, std::vector<double>& soup, int iters, int threads, int want_interior,
+                  Acc& acc, oracle_mesh* out) {
+    const int64_t NX = Xs.size();
     int64_t T = soup.size() / 9;
-
     // Unique vertices (VertexSlice, mesh.go:770-778).
     std::unordered_map<V3, int64_t, KeyHash, KeyEq> vid;
     std::vector<V3> verts;
@@ -1589,10 +1500,10 @@ int oracle_mc_search(const mc_node* nodes, size_t n, const mc_tri_set* sets, siz
                     inner[i] = ip;
                 }
             }
-            calls += 0;
-            flush();
+            acc.calls += 0;
+            acc.flush();
         });
-        calls += (int64_t)verts.size() * (1 + iters);
+        acc.calls += (int64_t)verts.size() * (1 + iters);
         if (err2) {
             std::snprintf(out->error, sizeof(out->error),
                           err2 == MC_ERR_NOT_ON_EDGE ? "vertex not on edge" : "index out of range");
@@ -1617,11 +1528,252 @@ int oracle_mc_search(const mc_node* nodes, size_t n, const mc_tri_set* sets, siz
             out->interior[3 * i + 2] = p.z;
         }
     }
-    out->contains_calls = calls;
-    out->leaf_evals = leaf;
-    out->bvh_nodes = ndc;
-    out->bvh_tris = trc;
+    out->contains_calls = acc.calls;
+    out->leaf_evals = acc.leaf;
+    out->bvh_nodes = acc.ndc;
+    out->bvh_tris = acc.trc;
     return MC_OK;
+}
+
+int oracle_mc_search(const mc_node* nodes, size_t n, const mc_tri_set* sets, size_t n_sets,
+                     double delta, int iters, int threads, int64_t z_begin, int64_t z_end, int want_interior,
+                     oracle_mesh* out) {
+    std::memset(out, 0, sizeof(*out));
+    Scene sc;
+    std::string err;
+    int st = parse_scene(nodes, n, sets, n_sets, &sc, &err);
+    if (st) {
+        std::snprintf(out->error, sizeof(out->error), "%s", err.c_str());
+        return st;
+    }
+    const Solid& s = *sc.root;
+    // validateBounds (bounder.go:29-52) on the caller's Min()/Max() of the
+    // root, as the reference calls s.Min()/s.Max() on the caller's object.
+    V3 mn = xyz(nodes[0].min[0], nodes[0].min[1], nodes[0].min[2]);
+    V3 mx = xyz(nodes[0].max[0], nodes[0].max[1], nodes[0].max[2]);
+    if (std::isnan(vsum(mn)) || std::isnan(vsum(mx)) || std::isinf(vsum(mn)) || std::isinf(vsum(mx)) ||
+        mx.x < mn.x || mx.y < mn.y || mx.z < mn.z) {
+        std::snprintf(out->error, sizeof(out->error), "invalid bounds");
+        return MC_ERR_INVALID_BOUNDS;
+    }
+    Table table = build_table();
+    std::vector<double> Xs, Ys, Zs;
+    const int64_t lim = 1 << 20;
+    if (spacer_axis(mn.x, mx.x, delta, &Xs, lim) || spacer_axis(mn.y, mx.y, delta, &Ys, lim) ||
+        spacer_axis(mn.z, mx.z, delta, &Zs, lim))
+        return MC_ERR_GRID;
+    const int64_t NX = Xs.size(), NY = Ys.size(), NZ = Zs.size();
+    out->nx = NX;
+    out->ny = NY;
+    out->nz = NZ;
+    if (z_end < 0 || z_end > NZ) z_end = NZ;
+    if (z_begin < 0) z_begin = 0;
+    int64_t zlo = std::max<int64_t>(0, z_begin), zhi = z_end;  // slabs to classify
+
+    Acc acc;
+    auto flush = [&] { acc.flush(); };
+    std::atomic<int64_t>& calls = acc.calls;
+
+    // Scan + FetchZ (mc.go:614-692): classify every corner of each slab.
+    int64_t nslab = zhi - zlo;
+    std::vector<uint8_t> grid((size_t)std::max<int64_t>(nslab, 0) * NX * NY);
+    std::atomic<int> bad{0};
+    parallel_for(nslab, threads, [&](int64_t zi, int) {
+        int64_t z = zlo + zi;
+        bool onEdge = z == 0 || z == NZ - 1;
+        uint8_t* v = &grid[(size_t)zi * NX * NY];
+        for (int64_t i = 0; i < NY; i++)
+            for (int64_t j = 0; j < NX; j++) {
+                bool b = s.Contains(xyz(Xs[j], Ys[i], Zs[z]));
+                v[i * NX + j] = b;
+                if (b && (onEdge || i == 0 || j == 0 || i == NY - 1 || j == NX - 1)) bad = 1;
+            }
+        calls += NX * NY;
+        flush();
+    });
+    if (bad) {
+        std::snprintf(out->error, sizeof(out->error), "solid is true outside of bounds");
+        return MC_ERR_BOUNDS_INSIDE;
+    }
+
+    // Cube loop of MarchingCubes (mc.go:20-35).
+    auto square = [&](int64_t zi, int64_t x, int64_t y) {  // GetSquare, mc.go:698-710
+        int r = 0, mask = 1;
+        const uint8_t* v = &grid[(size_t)zi * NX * NY];
+        for (int64_t y1 = y; y1 < y + 2; y1++)
+            for (int64_t x1 = x; x1 < x + 2; x1++) {
+                if (v[y1 * NX + x1]) r |= mask;
+                mask <<= 1;
+            }
+        return r;
+    };
+    std::vector<std::vector<double>> parts((size_t)std::max<int64_t>(nslab, 0));
+    parallel_for(nslab > 0 ? nslab - 1 : 0, threads, [&](int64_t zi, int) {
+        int64_t z = zlo + zi + 1;  // nextZ: bottom = z-1, top = z
+        std::vector<double>& part = parts[zi];
+        for (int64_t y = 0; y < NY - 1; y++)
+            for (int64_t x = 0; x < NX - 1; x++) {
+                int bits = square(zi, x, y) | (square(zi + 1, x, y) << 4);
+                int cnt = table.count[bits];
+                if (!cnt) continue;
+                V3 a = xyz(Xs[x], Ys[y], Zs[z - 1]);
+                V3 b = xyz(Xs[x + 1], Ys[y + 1], Zs[z]);
+                V3 corners[8] = {a,
+                                 xyz(b.x, a.y, a.z),
+                                 xyz(a.x, b.y, a.z),
+                                 xyz(b.x, b.y, a.z),
+                                 xyz(a.x, a.y, b.z),
+                                 xyz(b.x, a.y, b.z),
+                                 xyz(a.x, b.y, b.z),
+                                 b};  // mcCornerCoordinates, mc.go:289-301
+                for (int t = 0; t < cnt; t++) {
+                    const uint8_t* m = table.tris[bits][t];
+                    for (int k = 0; k < 3; k++) {  // mcTriangle.Triangle, mc.go:401-407
+                        V3 p = mid(corners[m[2 * k]], corners[m[2 * k + 1]]);
+                        part.push_back(p.x);
+                        part.push_back(p.y);
+                        part.push_back(p.z);
+                    }
+                }
+            }
+    });
+    std::vector<double> soup;
+    for (auto& p : parts) soup.insert(soup.end(), p.begin(), p.end());
+    return finish_search(s, Xs, Ys, Zs, soup, iters, threads, want_interior, acc, out);
+}
+
+// MarchingCubesSearchFilter (mc.go:83-155): the block kd-split with the
+// caller's filter f (called with the block's bounds widened by delta * 1e-3,
+// as min x, y, z, max x, y, z), each kept leaf block's corners evaluated by
+// its own cache (mcBlockCache.Populate, mc.go:847-868, with the border panic
+// for the block's corners on the grid's border), its cubes' triangles, then
+// mcSearch of their vertices.  Single-threaded over blocks; f is called in
+// the reference's depth-first visiting order.
+typedef int (*oracle_rect_filter)(const double* rect, void* user);
+
+int oracle_mc_search_filter(const mc_node* nodes, size_t n, const mc_tri_set* sets, size_t n_sets, double delta,
+                            int iters, int threads, oracle_rect_filter f, void* user, oracle_mesh* out) {
+    std::memset(out, 0, sizeof(*out));
+    Scene sc;
+    std::string err;
+    int st = parse_scene(nodes, n, sets, n_sets, &sc, &err);
+    if (st) {
+        std::snprintf(out->error, sizeof(out->error), "%s", err.c_str());
+        return st;
+    }
+    const Solid& s = *sc.root;
+    V3 mn = xyz(nodes[0].min[0], nodes[0].min[1], nodes[0].min[2]);
+    V3 mx = xyz(nodes[0].max[0], nodes[0].max[1], nodes[0].max[2]);
+    if (std::isnan(vsum(mn)) || std::isnan(vsum(mx)) || std::isinf(vsum(mn)) || std::isinf(vsum(mx)) ||
+        mx.x < mn.x || mx.y < mn.y || mx.z < mn.z) {
+        std::snprintf(out->error, sizeof(out->error), "invalid bounds");
+        return MC_ERR_INVALID_BOUNDS;
+    }
+    Table table = build_table();
+    std::vector<double> Xs, Ys, Zs;
+    const int64_t lim = 1 << 20;
+    if (spacer_axis(mn.x, mx.x, delta, &Xs, lim) || spacer_axis(mn.y, mx.y, delta, &Ys, lim) ||
+        spacer_axis(mn.z, mx.z, delta, &Zs, lim))
+        return MC_ERR_GRID;
+    const int64_t NX = Xs.size(), NY = Ys.size(), NZ = Zs.size();
+    out->nx = NX;
+    out->ny = NY;
+    out->nz = NZ;
+    Acc acc;
+    std::vector<double> soup;
+    if (NX < 2 || NY < 2 || NZ < 2) return finish_search(s, Xs, Ys, Zs, soup, iters, threads, 0, acc, out);
+
+    struct Block {
+        int64_t lo[3], hi[3];
+    };
+    const std::vector<double>* vals[3] = {&Xs, &Ys, &Zs};
+    const double eps = delta * 1e-3;
+    auto keep = [&](const Block& b) {  // blockFilter + mcBlock.Bounds (mc.go:96-102, :748-752)
+        double r[6];
+        for (int a = 0; a < 3; a++) {
+            r[a] = (*vals[a])[b.lo[a]] + -eps;
+            r[3 + a] = (*vals[a])[b.hi[a]] + eps;
+        }
+        return f(r, user) != 0;
+    };
+    auto volume = [](const Block& b) { return (b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]) * (b.hi[2] - b.lo[2]); };
+    // mcBlock.Pieces (mc.go:791-801) with mcBlock.Split (mc.go:803-826).
+    std::function<void(const Block&, int64_t, std::vector<Block>*)> pieces = [&](const Block& b, int64_t minv,
+                                                                                 std::vector<Block>* outb) {
+        if (!keep(b)) return;
+        if (volume(b) / 2 < minv) {
+            outb->push_back(b);
+            return;
+        }
+        const int64_t lx = b.hi[0] - b.lo[0], ly = b.hi[1] - b.lo[1], lz = b.hi[2] - b.lo[2];
+        int axis = 0;
+        if (ly >= lx && ly >= lz) axis = 1;
+        else if (lz >= lx && lz >= ly) axis = 2;
+        Block b1 = b, b2 = b;
+        b1.hi[axis] = (b.hi[axis] + b.lo[axis]) / 2;
+        b2.lo[axis] = b1.hi[axis];
+        pieces(b1, minv, outb);
+        pieces(b2, minv, outb);
+    };
+    Block root{{0, 0, 0}, {NX - 1, NY - 1, NZ - 1}};
+    std::vector<Block> queued, leaves;
+    pieces(root, std::max<int64_t>(volume(root) / 4096, 64), &queued);
+    for (const Block& b : queued) pieces(b, 64, &leaves);
+
+    for (const Block& b : leaves) {
+        // mcBlockCache.Populate (mc.go:847-868)
+        const int64_t sx = b.hi[0] - b.lo[0] + 1, sy = b.hi[1] - b.lo[1] + 1, sz = b.hi[2] - b.lo[2] + 1;
+        std::vector<uint8_t> v((size_t)sx * sy * sz);
+        for (int64_t z = b.lo[2]; z <= b.hi[2]; z++)
+            for (int64_t y = b.lo[1]; y <= b.hi[1]; y++)
+                for (int64_t x = b.lo[0]; x <= b.hi[0]; x++) {
+                    const bool in = s.Contains(xyz(Xs[x], Ys[y], Zs[z]));
+                    const bool edge = z == 0 || z == NZ - 1 || y == 0 || y == NY - 1 || x == 0 || x == NX - 1;
+                    if (in && edge) {
+                        std::snprintf(out->error, sizeof(out->error), "solid is true outside of bounds");
+                        return MC_ERR_BOUNDS_INSIDE;
+                    }
+                    v[(size_t)((z - b.lo[2]) * sy + (y - b.lo[1])) * sx + (x - b.lo[0])] = in;
+                }
+        acc.calls += sx * sy * sz;
+        acc.flush();
+        auto square = [&](int64_t x, int64_t y, int64_t z) {  // mcBlockCache.getSquare (mc.go:878-892)
+            int r = 0, mask = 1;
+            for (int64_t y1 = y; y1 < y + 2; y1++)
+                for (int64_t x1 = x; x1 < x + 2; x1++) {
+                    if (v[(size_t)((z - b.lo[2]) * sy + (y1 - b.lo[1])) * sx + (x1 - b.lo[0])]) r |= mask;
+                    mask <<= 1;
+                }
+            return r;
+        };
+        for (int64_t z = b.lo[2]; z < b.hi[2]; z++)
+            for (int64_t y = b.lo[1]; y < b.hi[1]; y++)
+                for (int64_t x = b.lo[0]; x < b.hi[0]; x++) {
+                    const int bits = square(x, y, z) | (square(x, y, z + 1) << 4);
+                    const int cnt = table.count[bits];
+                    if (!cnt) continue;
+                    V3 a = xyz(Xs[x], Ys[y], Zs[z]);
+                    V3 c = xyz(Xs[x + 1], Ys[y + 1], Zs[z + 1]);
+                    V3 corners[8] = {a,
+                                     xyz(c.x, a.y, a.z),
+                                     xyz(a.x, c.y, a.z),
+                                     xyz(c.x, c.y, a.z),
+                                     xyz(a.x, a.y, c.z),
+                                     xyz(c.x, a.y, c.z),
+                                     xyz(a.x, c.y, c.z),
+                                     c};  // mcCornerCoordinates, mc.go:289-301
+                    for (int t = 0; t < cnt; t++) {
+                        const uint8_t* m = table.tris[bits][t];
+                        for (int k = 0; k < 3; k++) {
+                            V3 p = mid(corners[m[2 * k]], corners[m[2 * k + 1]]);
+                            soup.push_back(p.x);
+                            soup.push_back(p.y);
+                            soup.push_back(p.z);
+                        }
+                    }
+                }
+    }
+    return finish_search(s, Xs, Ys, Zs, soup, iters, threads, 0, acc, out);
 }
 
 }  // extern "C"

@@ -121,6 +121,42 @@ def mc_search(nodes, sets, delta, iters, threads=None, z_range=(0, -1), interior
     return res
 
 
+RECT_FILTER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
+
+
+def mc_search_filter(nodes, sets, delta, iters, f, threads=None):
+    """MarchingCubesSearchFilter (mc.go:83-155) with the Python filter f,
+    called with a Rect (MinVal, MaxVal as Coord3D); iters == 0 is
+    MarchingCubesFilter.  Returns dict(tris=(T,9) soup, ...)."""
+    from model3d_gb300.geometry import XYZ
+    from model3d_gb300.solids import Rect
+    calls = [0]
+
+    def cb(r, _user):
+        calls[0] += 1
+        return 1 if f(Rect(XYZ(r[0], r[1], r[2]), XYZ(r[3], r[4], r[5]))) else 0
+
+    fn = RECT_FILTER(cb)
+    L = lib()
+    L.oracle_mc_search_filter.restype = ctypes.c_int
+    L.oracle_mc_search_filter.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                                          ctypes.c_double, ctypes.c_int, ctypes.c_int, RECT_FILTER,
+                                          ctypes.c_void_p, ctypes.POINTER(OracleMesh)]
+    nodes, arr, keep = _scene(nodes, sets)
+    out = OracleMesh()
+    st = L.oracle_mc_search_filter(nodes.ctypes.data, len(nodes), ctypes.addressof(arr), len(sets), float(delta),
+                                   int(iters), int(threads or os.cpu_count() or 1), fn, None, ctypes.byref(out))
+    if st != 0:
+        msg = out.error.decode()
+        L.oracle_mesh_free(ctypes.byref(out))
+        raise OracleError(st, msg)
+    T = out.n_triangles
+    tris = np.ctypeslib.as_array(out.tris, shape=(max(T, 1) * 9,))[:T * 9].reshape(T, 9).copy()
+    res = dict(tris=tris, n_vertices=out.n_vertices, nx=out.nx, ny=out.ny, nz=out.nz, filter_calls=calls[0])
+    L.oracle_mesh_free(ctypes.byref(out))
+    return res
+
+
 def encode_stl(tris):
     """EncodeSTL (model3d/export.go) of a (T, 9) triangle soup, as bytes."""
     t = np.ascontiguousarray(tris, dtype=np.float64).reshape(-1, 9)
