@@ -1397,40 +1397,6 @@ struct SearchArgs {
     double* interior;  // V x 3 interior points, or null
 };
 
-// Conversions without the float64 pipe.  On this part the float64 pipe runs
-// at 1/64 of the FP32 rate, and a warp-wide conversion occupies it as long as
-// a float64 multiply; the search needs several per vertex.  The rare cases
-// (values outside float's normal range, edges across a binade) call out of
-// line, so the compiler cannot run them speculatively.
-__device__ __noinline__ float to_float_slow(double v) { return (float)v; }
-__device__ __noinline__ double mid_slow(double a, double b) { return D_MUL(D_ADD(a, b), 0.5); }
-
-// Nearest float of v (round to nearest even, as (float)v).
-__device__ __forceinline__ float to_float_rn(double v) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const unsigned long long e = (b >> 52) & 0x7ff;
-    if (e >= 897 && e <= 1150) return __uint_as_float(float_bits_of(b));
-    return to_float_slow(v);
-}
-__device__ __forceinline__ F3 to_f3_rn(const P3& p) { return F3{to_float_rn(p.x), to_float_rn(p.y), to_float_rn(p.z)}; }
-
-// The float just below / above a finite float x.  With x the nearest float
-// of a double v, f_down(x) <= v <= f_up(x): an outward-rounded bound of v.
-__device__ __forceinline__ float f_down(float x) {
-    const uint32_t b = __float_as_uint(x);
-    return x > 0.f ? __uint_as_float(b - 1u) : (x < 0.f ? __uint_as_float(b + 1u) : -1.40129846e-45f);
-}
-__device__ __forceinline__ float f_up(float x) {
-    const uint32_t b = __float_as_uint(x);
-    return x > 0.f ? __uint_as_float(b + 1u) : (x < 0.f ? __uint_as_float(b - 1u) : 1.40129846e-45f);
-}
-
-__device__ __forceinline__ void set_compf(F3& p, int a, float v) {
-    if (a == 0) p.x = v;
-    else if (a == 1) p.y = v;
-    else p.z = v;
-}
-
 __device__ __forceinline__ float warp_minf(float v) {
     for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
@@ -1472,23 +1438,18 @@ __device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* b
                                             P3* cpt, int* axis, double* lo, double* hi, int* hi_bit) {
     const int ax = (int)(key >> 60);
     const int z = (int)((key >> 40) & 0xfffff), y = (int)((key >> 20) & 0xfffff), x = (int)(key & 0xfffff);
-    P3 c{g.xs[x], g.ys[y], g.zs[z]};
+    const P3 c0{g.xs[x], g.ys[y], g.zs[z]};
+    P3 c1 = c0;
+    if (ax == 0) c1.x = g.xs[x + 1];
+    else if (ax == 1) c1.y = g.ys[y + 1];
+    else c1.z = g.zs[z + 1];
     // (v + v) * 0.5 == v exactly unless v + v overflows (|v| >= 2^1023), so
     // off the edge axis the midpoint is the grid value itself.
-    auto off_axis = [](double v) {
-        const bool big = ((unsigned long long)__double_as_longlong(v) & 0x7ff0000000000000ull) >= 0x7fe0000000000000ull;
-        return big ? mid_slow(v, v) : v;
+    auto mid = [](double a, double b, bool same) {
+        const bool big = ((unsigned long long)__double_as_longlong(a) & 0x7ff0000000000000ull) >= 0x7fe0000000000000ull;
+        return (same && !big) ? a : D_MUL(D_ADD(a, b), 0.5);
     };
-    c = P3{off_axis(c.x), off_axis(c.y), off_axis(c.z)};
-    // On the edge axis (a + b) * 0.5; for two values of one sign and binade
-    // (almost every edge) mid_bits rounds the same in integer arithmetic.
-    const double e0 = ax == 0 ? g.xs[x] : (ax == 1 ? g.ys[y] : g.zs[z]);
-    const double e1 = ax == 0 ? g.xs[x + 1] : (ax == 1 ? g.ys[y + 1] : g.zs[z + 1]);
-    const unsigned long long ab = (unsigned long long)__double_as_longlong(e0);
-    const unsigned long long bb = (unsigned long long)__double_as_longlong(e1);
-    const double m = bisect_bits_ok(ab, bb) ? __longlong_as_double((long long)mid_bits(ab, bb)) : mid_slow(e0, e1);
-    set_comp(c, ax, m);
-    *cpt = c;
+    *cpt = P3{mid(c0.x, c1.x, ax != 0), mid(c0.y, c1.y, ax != 1), mid(c0.z, c1.z, ax != 2)};
     *axis = 0;
     *hi_bit = -1;
     if (!lookup) return 0;
@@ -1510,17 +1471,24 @@ __device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* b
     return 0;
 }
 
-// mcSearchPoint (mc.go:223-258) with `contains(point, float of the moving
-// coordinate)` as Solid.Contains: only the axis coordinate moves.  hif is the
-// float of hi, the first point tested unless the classification's bit for it
-// is known (hi_bit >= 0).
-template <class Contains>
-__device__ __forceinline__ P3 bisect_core(Contains contains, P3 cpt, int axis, double lo, double hi, float hif,
-                                          int iters, int hi_bit, double* true_point) {
+// mcSearchPoint (mc.go:223-258) against a (folded) program; only the axis
+// coordinate moves, so the float point is updated in place.
+template <int PREC>
+__device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, int len, P3 cpt, int axis, double lo,
+                                     double hi, int iters, int hi_bit, Counts& cnt, int* err, double* true_point) {
+    F3 pf = to_f3(cpt);
+    auto contains_f = [&](P3 pt, float vf) -> bool {
+        if (len == FOLD_FALSE) return false;
+        if (len == FOLD_TRUE) return true;
+        if (axis == 0) pf.x = vf;
+        else if (axis == 1) pf.y = vf;
+        else pf.z = vf;
+        return eval_program<PREC>(P, prog, len, pt, pf, cnt, err);
+    };
     double fp = lo, tp = hi;
     P3 t = cpt;
     set_comp(t, axis, tp);
-    if (!(hi_bit >= 0 ? hi_bit == 1 : contains(t, hif))) {
+    if (!(hi_bit >= 0 ? hi_bit == 1 : contains_f(t, (float)tp))) {
         fp = hi;
         tp = lo;
     }
@@ -1537,15 +1505,15 @@ __device__ __forceinline__ P3 bisect_core(Contains contains, P3 cpt, int axis, d
             return m;
         }
         // x / 2 and x * 0.5 round the same real
-        const double mid = mid_slow(__longlong_as_double((long long)a), __longlong_as_double((long long)b));
-        *vf = to_float_rn(mid);
+        const double mid = D_MUL(D_ADD(__longlong_as_double((long long)a), __longlong_as_double((long long)b)), 0.5);
+        *vf = (float)mid;
         return (unsigned long long)__double_as_longlong(mid);
     };
     float vf;
     for (int k = 0; k < iters; k++) {
         const unsigned long long mb = midpoint(fb, tb, &vf);
         set_comp(arr, axis, __longlong_as_double((long long)mb));
-        if (contains(arr, vf)) tb = mb;
+        if (contains_f(arr, vf)) tb = mb;
         else fb = mb;
     }
     set_comp(arr, axis, __longlong_as_double((long long)midpoint(fb, tb, &vf)));
@@ -1553,38 +1521,22 @@ __device__ __forceinline__ P3 bisect_core(Contains contains, P3 cpt, int axis, d
     return arr;
 }
 
-// mcSearchPoint against the warp's (folded) program.  pf is the float point
-// of cpt.
-template <int PREC>
-__device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, int len, P3 cpt, F3 pf, int axis,
-                                     double lo, double hi, float hif, int iters, int hi_bit, Counts& cnt, int* err,
-                                     double* true_point) {
-    auto contains = [&](P3 pt, float vf) -> bool {
-        if (len == FOLD_FALSE) return false;
-        if (len == FOLD_TRUE) return true;
-        set_compf(pf, axis, vf);
-        return eval_program<PREC>(P, prog, len, pt, pf, cnt, err);
-    };
-    return bisect_core(contains, cpt, axis, lo, hi, hif, iters, hi_bit, true_point);
-}
-
 // Per-warp culling for the search: the union of the segments the warp
 // bisects, rounded outward to float, selects the active leaves; the program
 // is re-folded only when that set changed.  All lanes must call it.
-// pf is the float point of the vertex, lof / hif the floats of its edge's
-// ends: one float step outward of each bounds the double it rounds.
-__device__ __forceinline__ void search_cull(const ProgView& P, bool work, const F3& pf, int axis, float lof,
-                                            float hif, uint32_t* q, uint32_t* cur, uint32_t* prev, bool& have_prev,
+__device__ __forceinline__ void search_cull(const ProgView& P, bool work, const P3& cpt, int axis, double lo,
+                                            double hi, uint32_t* q, uint32_t* cur, uint32_t* prev, bool& have_prev,
                                             const uint32_t*& prog, int& len) {
     const int lane = threadIdx.x & 31;
     const int nw = (P.n_leaves + 31) >> 5;
     float blo[3], bhi[3];
-    const float pc[3] = {pf.x, pf.y, pf.z};
     for (int i = 0; i < 3; i++) {
         float vlo = CUDART_INF_F, vhi = -CUDART_INF_F;
         if (work) {
-            vlo = f_down(i == axis ? fminf(lof, hif) : pc[i]);
-            vhi = f_up(i == axis ? fmaxf(lof, hif) : pc[i]);
+            const double a = i == axis ? (lo < hi ? lo : hi) : comp(cpt, i);
+            const double b = i == axis ? (lo < hi ? hi : lo) : a;
+            vlo = __double2float_rd(a);
+            vhi = __double2float_ru(b);
         }
         blo[i] = warp_minf(vlo);
         bhi[i] = warp_maxf(vhi);
@@ -1649,18 +1601,10 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search(GridView g
         if (status == 1) atomicOr(&a.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&a.err[ER_EDGE_INDEX], 1);
         const bool work = live && lookup && status == 0;
-        F3 pf{0.f, 0.f, 0.f};
-        float lof = 0.f, hif = 0.f;
-        if (work) {
-            pf = to_f3_rn(cpt);
-            lof = to_float_rn(lo);
-            hif = to_float_rn(hi);
-        }
-        if (a.cull && __any_sync(0xffffffffu, work)) search_cull(P, work, pf, axis, lof, hif, q, cur, prev, have_prev, prog, len);
+        if (a.cull && __any_sync(0xffffffffu, work)) search_cull(P, work, cpt, axis, lo, hi, q, cur, prev, have_prev, prog, len);
         if (live && status == 0) {
             double tpt = 0;
-            const P3 out =
-                work ? bisect<PREC>(P, prog, len, cpt, pf, axis, lo, hi, hif, a.iters, hi_bit, cnt, a.err, &tpt) : cpt;
+            const P3 out = work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, a.iters, hi_bit, cnt, a.err, &tpt) : cpt;
             a.verts[3 * v] = out.x;
             a.verts[3 * v + 1] = out.y;
             a.verts[3 * v + 2] = out.z;
@@ -1930,13 +1874,6 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(Batc
         if (status == 1) atomicOr(&Jp->ca.err[ER_NOT_ON_EDGE], 1);
         if (status == 2) atomicOr(&Jp->ca.err[ER_EDGE_INDEX], 1);
         const bool work = live && Jp->iters != 0 && status == 0;
-        F3 pf{0.f, 0.f, 0.f};
-        float lof = 0.f, hif = 0.f;
-        if (work) {
-            pf = to_f3_rn(cpt);
-            lof = to_float_rn(lo);
-            hif = to_float_rn(hi);
-        }
         double tpt = 0;
         // One bisection call site (a second inlined copy of the evaluation
         // loop costs instruction fetch): the warp's culled program when its
@@ -1955,7 +1892,7 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(Batc
             const int nw = (P.n_leaves + 31) >> 5;
             uint32_t* cur = q + P.fold_cap;
             if (b.cull && __any_sync(0xffffffffu, work))
-                search_cull(P, work, pf, axis, lof, hif, q, cur, cur + nw, have_prev, prog, len);
+                search_cull(P, work, cpt, axis, lo, hi, q, cur, cur + nw, have_prev, prog, len);
             Pp = &P;
             pr = prog;
             ln = len;
@@ -1963,8 +1900,7 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(Batc
             prev_job = -1;
         }
         if (live && status == 0) {
-            const P3 out = work ? bisect<PREC>(*Pp, pr, ln, cpt, pf, axis, lo, hi, hif, Jp->iters, hi_bit, cnt,
-                                               Jp->ca.err, &tpt)
+            const P3 out = work ? bisect<PREC>(*Pp, pr, ln, cpt, axis, lo, hi, Jp->iters, hi_bit, cnt, Jp->ca.err, &tpt)
                                 : cpt;
             verts[3 * v] = out.x;
             verts[3 * v + 1] = out.y;
