@@ -356,7 +356,7 @@ def other_configs(ctx, torch, flush, single_rate, count=16):
              ("collider_icosphere_1048820_tris_256cubed", lambda: collider_line(ctx, torch, flush)),
              ("batch_512_csg", lambda: batch_line(ctx, torch, flush, single_rate)),
              ("metaball_blob64_quartic_delta0.005", lambda: metaball_line(ctx, torch, flush)),
-             ("batch_colliders", lambda: collider_batch_line(ctx, count))]
+             ("batch_colliders", lambda: collider_batch_line(ctx, count, torch))]
     for name, f in lines:
         try:
             out.update(f())
@@ -423,13 +423,34 @@ def collider_line(ctx, torch, flush):
         "triangle_tests": a["bvh_tris"], "host_lowering_s": lower_s, "e2e": e2e}}
 
 
+def rank_share(jobs, torch):
+    """Under torchrun: this rank's jobs of a largest-first partition by
+    corner count (model3d_gb300/shard.py), and a function that turns this
+    rank's (ms, corners) into the whole job's (slowest rank's ms, all
+    corners).  One process: all jobs, identity."""
+    ws, rank, _ = dist_env()
+    if ws == 1:
+        return jobs, (lambda ms, corners: (ms, corners)), "1 GPU"
+    from model3d_gb300.shard import job_costs, partition_jobs
+    mine = partition_jobs(job_costs(jobs), ws)[rank]
+
+    def combine(ms, corners):
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        c = torch.tensor([float(corners)], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
+        return float(t.item()), int(c.item())
+
+    return [jobs[i] for i in mine], combine, f"{ws} GPUs, jobs split largest-first by corners"
+
+
 def batch_line(ctx, torch, flush, single_rate):
     from model3d_gb300 import DeviceSolid, MarchingCubesSearchBatch
     from model3d_gb300 import _native as N
     from model3d_gb300.workloads import csg_batch
     L = N.lib()
     items = csg_batch(2024, count=512)
-    jobs = [(DeviceSolid(s, ctx), dd, 8) for s, dd in items]
+    jobs, combine, par = rank_share([(DeviceSolid(s, ctx), dd, 8) for s, dd in items], torch)
     res = {}
     for prec in ("fp32", "fp64"):
         ms = []
@@ -446,11 +467,14 @@ def batch_line(ctx, torch, flush, single_rate):
     (bds, bd, bit), _ = big
     br = _device_rate(L, N, ctx, bds, bd, bit, N.MC_PREC_FP32_FILTERED, flush, torch, reps=3)
     big_rate = br["corners"] / (br["ms_total"] / 1e3)
-    corners = res["fp32"][1]
+    ms32, corners = combine(res["fp32"][0], res["fp32"][1])
+    ms64, _ = combine(res["fp64"][0], res["fp64"][1])
+    res["fp32"] = (ms32, corners, res["fp32"][2])
+    res["fp64"] = (ms64, corners, res["fp64"][2])
     return {"batch_512_csg": {
-        "jobs": len(jobs), "corners": corners, "triangles": res["fp32"][2],
+        "jobs": len(items), "parallelism": par, "corners": corners, "triangles": res["fp32"][2],
         "fp32_corners_per_s": corners / (res["fp32"][0] / 1e3),
-        "fp32_meshes_per_s": len(jobs) / (res["fp32"][0] / 1e3),
+        "fp32_meshes_per_s": len(items) / (res["fp32"][0] / 1e3),
         "fp64_corners_per_s": corners / (res["fp64"][0] / 1e3),
         "ms_fp32_graph_replay": res["fp32"][0], "ms_fp64_graph_replay": res["fp64"][0],
         "sequential_single_calls_ms": seq,
@@ -485,7 +509,7 @@ def metaball_line(ctx, torch, flush):
         "bit_identical_fp32_fp64": same}}
 
 
-def collider_batch_line(ctx, count):
+def collider_batch_line(ctx, count, torch):
     """Displaced-icosphere colliders (triangles log-uniform in [20k, 2M], grid
     sides log-uniform in [128, 512]) meshed in one batched launch, FP32-filtered
     (graph replay) and FP64, with the two precisions' meshes compared."""
@@ -505,6 +529,7 @@ def collider_batch_line(ctx, count):
         ext = max(mx.X - mn.X, mx.Y - mn.Y, mx.Z - mn.Z)
         jobs.append((DeviceSolid(s, ctx), ext / (side - 3), 8))
     lower_s = time.perf_counter() - t0
+    jobs, combine, par = rank_share(jobs, torch)
     ms = {}
     outs = {}
     for prec, reps in (("fp32", 3), ("fp64", 1)):
@@ -520,12 +545,15 @@ def collider_batch_line(ctx, count):
     same = all(np.array_equal(a.vertices.view(np.uint64), b.vertices.view(np.uint64)) and
                np.array_equal(a.triangles, b.triangles) for a, b in zip(outs["fp32"], outs["fp64"]))
     corners = sum(x.stats["corners"] for x in outs["fp32"])
+    ms["fp32"], all_corners = combine(ms["fp32"], corners)
+    ms["fp64"], _ = combine(ms["fp64"], corners)
+    corners = all_corners
     st0 = outs["fp32"][0].stats  # counters of a batched launch are batch totals
     tests = st0["bvh_tris"] + st0["bvh_nodes"]
     esc = st0["escalations"]
     name = f"batch_{count}_colliders" + ("" if count == 64 else "_of_the_64_mesh_configuration")
     return {name: {
-        "jobs": count, "triangles_in": int(sum(len(t) for t, _, _ in meshes)),
+        "jobs": count, "parallelism": par, "triangles_in": int(sum(len(t) for t, _, _ in meshes)),
         "corners": corners, "triangles_out": sum(x.NumTriangles() for x in outs["fp32"]),
         "fp32_corners_per_s": corners / (ms["fp32"] / 1e3),
         "fp64_corners_per_s": corners / (ms["fp64"] / 1e3),
@@ -540,7 +568,7 @@ def collider_batch_line(ctx, count):
 # summarised in profiles/launches_csg48_delta0.004.md (same kernels as this
 # source).  Below the algorithmic bytes where a kernel reads what the previous
 # one left in the 129 MB L2 (keys, corner bits) or its writes stay in L2.
-NCU_TRAFFIC = {}
+NCU_TRAFFIC = {"k_count": 29755648, "k_emit": 50160128, "k_search": 45513216}
 
 
 def algorithmic_bytes(kernel, st):
