@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from model3d_gb300 import (Context, DeviceSolid, MarchingCubesSearch, MCError, MeshToCollider, NewColliderSolid,
-                           Sphere, XYZ)
+                           Sphere, XYZ, serialize)
 from model3d_gb300 import _native as N
 from model3d_gb300.workloads import csg_tree, displaced_icosphere, metaball_blob
 
@@ -37,7 +37,7 @@ def test_device_calls_grow_shrink_and_match_the_waiting_path():
     ctx = Context(0)
     cases = [(Sphere(XYZ(0, 0, 0), 1.0), 0.1),
              (csg_tree(1, 48, 16), 0.01),   # outgrows the first call's buffers
-             (Sphere(XYZ(0.2, 0, 0), 0.5), 0.05),
+             (Sphere(XYZ(0.21, -0.03, 0.02), 0.5), 0.05),
              (csg_tree(1, 48, 16), 0.008),  # larger again
              (NewColliderSolid(MeshToCollider(displaced_icosphere(10))), 0.03),
              (metaball_blob(2, 12), 0.02),
@@ -52,7 +52,7 @@ def test_device_calls_grow_shrink_and_match_the_waiting_path():
             assert (st.vertices, st.triangles) == (len(ref.vertices), len(ref.triangles))
 
 
-def test_border_panic_on_a_warm_context():
+def test_border_panic_on_a_warm_context(oracle):
     ctx = Context(0)
 
     class Lying(Sphere):
@@ -71,3 +71,16 @@ def test_border_panic_on_a_warm_context():
     v, t, _ = _device(ctx, good, 0.05)
     ref = MarchingCubesSearch(good, 0.05, 8)
     assert np.array_equal(v.view(np.uint64), ref.vertices.view(np.uint64))
+    # Right bounds, but the corner (0.7000000000000001, -6.9e-17, -6.9e-17)
+    # of the spacer's last x plane is inside in float64 (its squared distance
+    # to the centre rounds to 0.25): the reference panics, and so does every
+    # precision here.
+    tight = Sphere(XYZ(0.2, 0, 0), 0.5)
+    with pytest.raises(RuntimeError, match="outside of bounds"):
+        oracle.mc_search(*serialize(tight), 0.05, 8)
+    ds = DeviceSolid(tight, ctx)
+    for prec in (N.MC_PREC_FP32_FILTERED, N.MC_PREC_FP64):
+        with pytest.raises(MCError) as e:
+            _device(ctx, ds, 0.05, prec=prec)
+        assert e.value.status == N.MC_ERR_BOUNDS_INSIDE
+    _device(ctx, good, 0.05)
