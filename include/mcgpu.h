@@ -308,6 +308,25 @@ mc_status mc_result_transform(mc_ctx* ctx, const mc_node* steps, size_t n_steps,
  * T does not fit in uint32. */
 mc_status mc_result_stl(mc_ctx* ctx, uint8_t* out, size_t cap, size_t* n_bytes);
 
+/* GroupTriangles (model3d/bvh.go:118-217) of the last result's triangles, on
+ * the device: order[i] = the index of the triangle SaveGroupedSTL
+ * (model3d/mesh.go:724-742) writes i-th.  The reference sorts a slice in Go
+ * map order with an unstable sort; here each midpoint sort is stable over
+ * the library's triangle order (ties keep that order).  order: T int32. */
+mc_status mc_result_group(mc_ctx* ctx, int32_t* order);
+/* SaveGroupedSTL's bytes (model3d/mesh.go:724-742: GroupTriangles, then
+ * WriteSTL, model3d/export.go:28-60) of the last result, grouped and encoded
+ * on the device.  Sizes and errors as mc_result_stl. */
+mc_status mc_result_stl_grouped(mc_ctx* ctx, uint8_t* out, size_t cap, size_t* n_bytes);
+/* The same two for a caller's indexed mesh (n_vertices x 3 float64,
+ * n_triangles x 3 int32 vertex indices, checked on the host: MC_ERR_ARG for
+ * an index outside [0, n_vertices)).  The mesh is copied to the device; the
+ * last result is left as it was. */
+mc_status mc_mesh_group(mc_ctx* ctx, const double* vertices, int64_t n_vertices, const int32_t* triangles,
+                        int64_t n_triangles, int32_t* order);
+mc_status mc_mesh_stl_grouped(mc_ctx* ctx, const double* vertices, int64_t n_vertices, const int32_t* triangles,
+                              int64_t n_triangles, uint8_t* out, size_t cap, size_t* n_bytes);
+
 /* Solid.Contains on the GPU for n points (n x 3 float64) -> out[i] in {0,1}.
  * Same device predicates and precision modes as mc_search. */
 mc_status mc_contains(mc_ctx* ctx, const mc_solid* solid, const double* points, int64_t n,

@@ -20,9 +20,9 @@ from .metaballs import (CubicMetaballFalloffFunc, ExponentialMetaballFalloffFunc
                         ScaleMetaball, SDFToMetaball, SignedMetaballSolid, TransformMetaball,
                         TranslateMetaball, VecScaleMetaball, WeightedMetaballSolid,
                         WyvillMetaballFalloffFunc)
-from .mc import (Context, Contains, DeviceSolid, MarchingCubes, MarchingCubesConj,
+from .mc import (Context, Contains, DeviceSolid, GroupTriangles, MarchingCubes, MarchingCubesConj,
                  MarchingCubesInterior, MarchingCubesSearch, MarchingCubesSearchBatch,
-                 MarchingCubesSearchSTL, MCError,
+                 MarchingCubesSearchGroupedSTL, MarchingCubesSearchSTL, MCError,
                  Mesh, autotune, canonical, case_table, check_program, default_context, measure_peaks,
                  spacer_axis)
 

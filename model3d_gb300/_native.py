@@ -36,7 +36,8 @@ EXPORTS = [
     "mc_search_device", "mc_result_device", "mc_result_copy", "mc_contains", "mc_search_batch",
     "mc_case_table", "mc_version", "mc_search_noalloc", "mc_autotune",
     "mc_measure_peaks", "mc_result_interior_copy", "mc_result_transform", "mc_result_stl",
-    "mc_program_check", "mc_result_keys",
+    "mc_program_check", "mc_result_keys", "mc_result_group", "mc_result_stl_grouped", "mc_mesh_group",
+    "mc_mesh_stl_grouped",
 ]
 
 
@@ -125,6 +126,10 @@ def lib():
         L.mc_result_keys.argtypes = [vp, vp]
         L.mc_result_transform.argtypes = [vp, vp, ctypes.c_size_t, i32]
         L.mc_result_stl.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        L.mc_result_group.argtypes = [vp, vp]
+        L.mc_result_stl_grouped.argtypes = [vp, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+        L.mc_mesh_group.argtypes = [vp, vp, i64, vp, i64, vp]
+        L.mc_mesh_stl_grouped.argtypes = [vp, vp, i64, vp, i64, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
         L.mc_contains.argtypes = [vp, vp, vp, i64, ctypes.POINTER(MCOpts), vp]
         L.mc_search_batch.argtypes = [vp, ctypes.POINTER(MCJob), ctypes.c_size_t,
                                       ctypes.POINTER(MCOpts), ctypes.POINTER(MCMesh), vp]

@@ -1,8 +1,9 @@
 """Builds libmcgpu.so in-tree (model3d_gb300/libmcgpu.so) for sm_103a.
 
-Two translation units compiled in parallel: the CUDA kernels + C ABI
-(nvcc) and the host lowering (g++ with -ffp-contract=off, so the float64
-constants it precomputes are rounded exactly as the reference rounds them).
+Three translation units compiled in parallel: the CUDA kernels + C ABI
+(nvcc), the device GroupTriangles (nvcc) and the host lowering (g++ with
+-ffp-contract=off, so the float64 constants it precomputes are rounded
+exactly as the reference rounds them).
 """
 from __future__ import annotations
 
@@ -44,14 +45,15 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return OUT
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
-    cu = os.path.join(CSRC, "mc_kernels.cu")
+    cus = [os.path.join(CSRC, f) for f in ("mc_kernels.cu", "mc_group.cu")]
     cpp = os.path.join(CSRC, "mc_lower.cpp")
-    cu_o = os.path.join(BUILD, "mc_kernels.o")
+    cu_os = [os.path.join(BUILD, os.path.basename(f)[:-3] + ".o") for f in cus]
     cpp_o = os.path.join(BUILD, "mc_lower.o")
     cmds = [
         [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v" if verbose else "-O3",
-         "-c", cu, "-o", cu_o],
+         "-c", cu, "-o", cu_o] for cu, cu_o in zip(cus, cu_os)
+    ] + [
         ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-Wall", "-pthread",
          "-c", cpp, "-o", cpp_o],
     ]
@@ -62,12 +64,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError(f"build step failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         return r.stdout + r.stderr
 
-    with ThreadPoolExecutor(2) as ex:
+    with ThreadPoolExecutor(len(cmds)) as ex:
         logs = list(ex.map(run, cmds))
     if verbose:
         sys.stderr.write("".join(logs))
     tmp = OUT + ".tmp"
-    run([nvcc, ARCH, "-shared", "-cudart", "static", cu_o, cpp_o, "-o", tmp])
+    run([nvcc, ARCH, "-shared", "-cudart", "static", *cu_os, cpp_o, "-o", tmp])
     os.replace(tmp, OUT)
     return OUT
 

@@ -32,6 +32,7 @@
 #include <unistd.h>
 
 #include "../../include/mcgpu.h"
+#include "mc_group.h"
 #include "mc_internal.h"
 #include "mc_lower.h"
 #include "mc_predicates.cuh"
@@ -1639,12 +1640,14 @@ __global__ void k_apply_steps(double* verts, long long n, const XStepD* steps, i
 // float32 normal (Triangle.Normal = crossProduct().Normalize(), i.e.
 // c.Scale(1 / c.Norm()), primitives.go:27-33, coords.go:201-203, :379-381)
 // and vertices, then two zero bytes.  Records are 2-byte aligned.
-__global__ void k_encode_stl(const double* verts, const int32_t* tris, long long n, uint8_t* out) {
+// Record r holds triangle order[r] (r itself when order is null).
+__global__ void k_encode_stl(const double* verts, const int32_t* tris, const int32_t* order, long long n, uint8_t* out) {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const long long src = order ? order[t] : t;
         P3 v[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const long long i = tris[3 * t + k];
+            const long long i = tris[3 * src + k];
             v[k] = P3{verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]};
         }
         const double ax = D_SUB(v[1].x, v[0].x), ay = D_SUB(v[1].y, v[0].y), az = D_SUB(v[1].z, v[0].z);
@@ -2048,6 +2051,8 @@ struct mc_ctx {
     DevBuf nonempty;  // indices of the chunks with crossed edges (k_scan_chunks -> k_emit_list)
     DevBuf pts, pout;
     DevBuf inner, xsteps, stl;  // interior points of the last search; steps of mc_result_transform; STL bytes
+    DevBuf gorder, mesh_v, mesh_t;   // GroupTriangles order; a caller's mesh for mc_mesh_group / _stl_grouped
+    GroupScratch* group = nullptr;   // the grouping's own buffers, made on first use
     bool has_interior = false;
     unsigned long long* h_pin = nullptr;  // pinned: [0, 2) totals, [2, 4) errs (as ints), [4] non-empty chunks, [8, 8 + ST_N) stats
     // Device buffers of destroyed solids, reused by the next mc_solid_create
@@ -2243,8 +2248,10 @@ void mc_destroy(mc_ctx* ctx) {
     ctx->plan.reset();
     for (DevBuf* b : {&ctx->grid, &ctx->bits, &ctx->packed, &ctx->blocksum, &ctx->blockoff,
                       &ctx->prefv, &ctx->preft, &ctx->keys, &ctx->verts, &ctx->tris, &ctx->stats, &ctx->errs,
-                      &ctx->totals, &ctx->nonempty, &ctx->pts, &ctx->pout, &ctx->inner, &ctx->xsteps, &ctx->stl})
+                      &ctx->totals, &ctx->nonempty, &ctx->pts, &ctx->pout, &ctx->inner, &ctx->xsteps, &ctx->stl,
+                      &ctx->gorder, &ctx->mesh_v, &ctx->mesh_t})
         b->release();
+    group_scratch_free(ctx->group);
     for (auto& e : ctx->ev)
         if (e) cudaEventDestroy(e);
     for (auto& e : ctx->cev)
@@ -2831,9 +2838,10 @@ mc_status mc_result_transform(mc_ctx* ctx, const mc_node* steps, size_t n_steps,
     return MC_OK;
 }
 
-mc_status mc_result_stl(mc_ctx* ctx, uint8_t* out, size_t cap, size_t* n_bytes) {
-    if (!ctx || !n_bytes) return MC_ERR_ARG;
-    const long long T = ctx->last_T;
+// EncodeSTL of T triangles on the device, records in `order` (device, or
+// null for the triangles' own order), copied to out.
+mc_status encode_stl(mc_ctx* ctx, const double* dv, const int32_t* dt, const int32_t* dorder, long long T, uint8_t* out,
+                     size_t cap, size_t* n_bytes) {
     if (T > 0xffffffffLL) return fail(ctx, MC_ERR_ARG, "too many triangles for STL format");
     const size_t bytes = 84 + 50 * (size_t)T;
     *n_bytes = bytes;
@@ -2848,13 +2856,95 @@ mc_status mc_result_stl(mc_ctx* ctx, uint8_t* out, size_t cap, size_t* n_bytes) 
     CK(cudaMemcpyAsync(d, head, 84, cudaMemcpyHostToDevice, ctx->stream));
     if (T > 0) {
         k_encode_stl<<<(int)std::min<long long>((T + 255) / 256, (long long)ctx->sm_count * 16), 256, 0, ctx->stream>>>(
-            ctx->verts.as<double>(), ctx->tris.as<int32_t>(), T, d);
+            dv, dt, dorder, T, d);
         CK(cudaGetLastError());
     }
     prefault(out, bytes);
     CK(cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return MC_OK;
+}
+
+mc_status mc_result_stl(mc_ctx* ctx, uint8_t* out, size_t cap, size_t* n_bytes) {
+    if (!ctx || !n_bytes) return MC_ERR_ARG;
+    return encode_stl(ctx, ctx->verts.as<double>(), ctx->tris.as<int32_t>(), nullptr, ctx->last_T, out, cap, n_bytes);
+}
+
+// GroupTriangles order of T device triangles into ctx->gorder.
+mc_status group_order(mc_ctx* ctx, const double* dv, const int32_t* dt, long long T) {
+    CK(cudaSetDevice(ctx->device));
+    if (!ctx->group) ctx->group = group_scratch_new();
+    CK(ctx->gorder.ensure((size_t)std::max<long long>(T, 1) * 4));
+    bool bad = false;
+    CK(group_triangles_device(ctx->group, dv, dt, T, ctx->gorder.as<int32_t>(), ctx->stream, ctx->sm_count, &bad));
+    if (bad) return fail(ctx, MC_ERR_CUDA, "GroupTriangles: a device consistency check failed");
+    return MC_OK;
+}
+
+mc_status mc_result_group(mc_ctx* ctx, int32_t* order) {
+    if (!ctx || (!order && ctx->last_T)) return MC_ERR_ARG;
+    const long long T = ctx->last_T;
+    if (T == 0) return MC_OK;
+    mc_status s = group_order(ctx, ctx->verts.as<double>(), ctx->tris.as<int32_t>(), T);
+    if (s != MC_OK) return s;
+    CK(cudaMemcpyAsync(order, ctx->gorder.p, (size_t)T * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MC_OK;
+}
+
+mc_status mc_result_stl_grouped(mc_ctx* ctx, uint8_t* out, size_t cap, size_t* n_bytes) {
+    if (!ctx || !n_bytes) return MC_ERR_ARG;
+    const long long T = ctx->last_T;
+    if (out && T > 0 && T <= 0xffffffffLL && cap >= 84 + 50 * (size_t)T) {
+        mc_status s = group_order(ctx, ctx->verts.as<double>(), ctx->tris.as<int32_t>(), T);
+        if (s != MC_OK) return s;
+    }
+    return encode_stl(ctx, ctx->verts.as<double>(), ctx->tris.as<int32_t>(), ctx->gorder.as<int32_t>(), T, out, cap,
+                      n_bytes);
+}
+
+// A caller's indexed mesh onto the device (ctx->mesh_v / mesh_t), indices
+// checked on the host first.
+mc_status upload_mesh(mc_ctx* ctx, const double* vertices, int64_t V, const int32_t* triangles, int64_t T) {
+    if (V < 0 || T < 0 || (V > 0 && !vertices) || (T > 0 && !triangles)) return fail(ctx, MC_ERR_ARG, "bad mesh");
+    if (T >= ((int64_t)1 << 31)) return fail(ctx, MC_ERR_ARG, "mesh exceeds 2^31 triangles");
+    for (int64_t i = 0; i < 3 * T; i++)
+        if (triangles[i] < 0 || triangles[i] >= V) return fail(ctx, MC_ERR_ARG, "triangle index out of range");
+    CK(cudaSetDevice(ctx->device));
+    CK(ctx->mesh_v.ensure((size_t)std::max<int64_t>(V, 1) * 24));
+    CK(ctx->mesh_t.ensure((size_t)std::max<int64_t>(T, 1) * 12));
+    if (V > 0) CK(cudaMemcpyAsync(ctx->mesh_v.p, vertices, (size_t)V * 24, cudaMemcpyHostToDevice, ctx->stream));
+    if (T > 0) CK(cudaMemcpyAsync(ctx->mesh_t.p, triangles, (size_t)T * 12, cudaMemcpyHostToDevice, ctx->stream));
+    return MC_OK;
+}
+
+mc_status mc_mesh_group(mc_ctx* ctx, const double* vertices, int64_t n_vertices, const int32_t* triangles,
+                        int64_t n_triangles, int32_t* order) {
+    if (!ctx || (!order && n_triangles > 0)) return MC_ERR_ARG;
+    mc_status s = upload_mesh(ctx, vertices, n_vertices, triangles, n_triangles);
+    if (s != MC_OK || n_triangles == 0) return s;
+    s = group_order(ctx, ctx->mesh_v.as<double>(), ctx->mesh_t.as<int32_t>(), n_triangles);
+    if (s != MC_OK) return s;
+    CK(cudaMemcpyAsync(order, ctx->gorder.p, (size_t)n_triangles * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MC_OK;
+}
+
+mc_status mc_mesh_stl_grouped(mc_ctx* ctx, const double* vertices, int64_t n_vertices, const int32_t* triangles,
+                              int64_t n_triangles, uint8_t* out, size_t cap, size_t* n_bytes) {
+    if (!ctx || !n_bytes) return MC_ERR_ARG;
+    if (n_triangles > 0xffffffffLL) return fail(ctx, MC_ERR_ARG, "too many triangles for STL format");
+    *n_bytes = 84 + 50 * (size_t)std::max<int64_t>(n_triangles, 0);
+    if (!out) return MC_OK;
+    if (cap < *n_bytes) return fail(ctx, MC_ERR_ARG, "STL buffer too small");
+    mc_status s = upload_mesh(ctx, vertices, n_vertices, triangles, n_triangles);
+    if (s != MC_OK) return s;
+    if (n_triangles > 0) {
+        s = group_order(ctx, ctx->mesh_v.as<double>(), ctx->mesh_t.as<int32_t>(), n_triangles);
+        if (s != MC_OK) return s;
+    }
+    return encode_stl(ctx, ctx->mesh_v.as<double>(), ctx->mesh_t.as<int32_t>(), ctx->gorder.as<int32_t>(), n_triangles,
+                      out, cap, n_bytes);
 }
 
 mc_status mc_search(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters, const mc_opts* opts,

@@ -176,6 +176,45 @@ class Mesh:
         t = self.TriangleSoup().reshape(-1, 3, 3)
         return float(abs(np.linalg.det(t).sum() / 6.0)) if len(t) else 0.0
 
+    def _arrays(self):
+        v = np.ascontiguousarray(self.vertices, dtype=np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(self.triangles, dtype=np.int32).reshape(-1, 3)
+        return v, t
+
+    def EncodeGroupedSTL(self, ctx: Optional["Context"] = None) -> bytes:
+        """The bytes SaveGroupedSTL writes (model3d/mesh.go:724-742): the
+        triangles in GroupTriangles order (ties in the midpoint sorts keep
+        this mesh's triangle order), binary STL records (export.go:28-60).
+        Grouped and encoded on the device."""
+        ctx = ctx or default_context()
+        v, t = self._arrays()
+        L = N.lib()
+        n = ctypes.c_size_t()
+        _check(L.mc_mesh_stl_grouped(ctx.ptr, v.ctypes.data, len(v), t.ctypes.data, len(t), None, 0,
+                                     ctypes.byref(n)), ctx.ptr)
+        buf = np.empty(n.value, dtype=np.uint8)
+        _check(L.mc_mesh_stl_grouped(ctx.ptr, v.ctypes.data, len(v), t.ctypes.data, len(t), buf.ctypes.data,
+                                     n.value, ctypes.byref(n)), ctx.ptr)
+        return buf.tobytes()
+
+    def SaveGroupedSTL(self, path: str, ctx: Optional["Context"] = None) -> None:
+        """Mesh.SaveGroupedSTL (model3d/mesh.go:724-742)."""
+        data = self.EncodeGroupedSTL(ctx)
+        with open(path, "wb") as f:
+            f.write(data)
+
+
+def GroupTriangles(mesh: Mesh, *, ctx: Optional["Context"] = None) -> np.ndarray:
+    """GroupTriangles (model3d/bvh.go:118-217) of a mesh's triangles on the
+    device: order[i] is the triangle SaveGroupedSTL writes i-th.  Each
+    midpoint sort is stable over the mesh's triangle order (the reference's
+    sort.Slice over a slice in map order breaks ties arbitrarily)."""
+    ctx = ctx or default_context()
+    v, t = mesh._arrays()
+    order = np.empty(len(t), dtype=np.int32)
+    _check(N.lib().mc_mesh_group(ctx.ptr, v.ctypes.data, len(v), t.ctypes.data, len(t), order.ctypes.data), ctx.ptr)
+    return order
+
 
 def _opts(precision="fp32", cull=True, tile_y=0, tile_z=0, z_range=None):
     o = N.MCOpts()
@@ -303,6 +342,26 @@ def MarchingCubesSearchSTL(solid, delta: float, iters: int, *, precision: str = 
     _check(L.mc_result_stl(ctx.ptr, None, 0, ctypes.byref(n)), ctx.ptr)
     buf = np.empty(n.value, dtype=np.uint8)
     _check(L.mc_result_stl(ctx.ptr, buf.ctypes.data, n.value, ctypes.byref(n)), ctx.ptr)
+    return buf.tobytes()
+
+
+def MarchingCubesSearchGroupedSTL(solid, delta: float, iters: int, *, precision: str = "fp32",
+                                  cull: bool = True, ctx: Optional[Context] = None) -> bytes:
+    """model3d.MarchingCubesSearch(...) then SaveGroupedSTL's bytes
+    (model3d/mesh.go:724-742), the mesh never leaving the device: search,
+    GroupTriangles and the STL encoding all run there."""
+    ctx = ctx or (solid.ctx if isinstance(solid, DeviceSolid) else default_context())
+    ds = _as_device_solid(solid, ctx)
+    o = _opts(precision, cull)
+    V, T = ctypes.c_int64(), ctypes.c_int64()
+    st = N.MCStats()
+    L = N.lib()
+    _check(L.mc_search_device(ctx.ptr, ds.ptr, float(delta), int(iters), ctypes.byref(o),
+                              ctypes.byref(V), ctypes.byref(T), ctypes.byref(st)), ctx.ptr)
+    n = ctypes.c_size_t()
+    _check(L.mc_result_stl_grouped(ctx.ptr, None, 0, ctypes.byref(n)), ctx.ptr)
+    buf = np.empty(n.value, dtype=np.uint8)
+    _check(L.mc_result_stl_grouped(ctx.ptr, buf.ctypes.data, n.value, ctypes.byref(n)), ctx.ptr)
     return buf.tobytes()
 
 

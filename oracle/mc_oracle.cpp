@@ -1296,6 +1296,22 @@ void oracle_mesh_free(oracle_mesh* m) {
     m->interior = nullptr;
 }
 
+// GroupTriangles (model3d/bvh.go:118-217) of a triangle soup (T x 9
+// float64, in the given order): out[i] = the index of the triangle that
+// SaveGroupedSTL (model3d/mesh.go:724-742) writes i-th.  Ties in the three
+// midpoint sorts keep the input order (the deviation noted at the top).
+void oracle_group_triangles(const double* tris, int64_t T, int32_t* out) {
+    std::vector<Tri> t((size_t)T);
+    for (int64_t i = 0; i < T; i++) {
+        const double* p = tris + 9 * i;
+        t[(size_t)i].p[0] = xyz(p[0], p[1], p[2]);
+        t[(size_t)i].p[1] = xyz(p[3], p[4], p[5]);
+        t[(size_t)i].p[2] = xyz(p[6], p[7], p[8]);
+    }
+    std::vector<int> o = group_triangles(t);
+    for (int64_t i = 0; i < T; i++) out[i] = o[(size_t)i];
+}
+
 // EncodeSTL (model3d/export.go:20-66, fileformats/stl.go:27-58) of a
 // triangle soup (T x 9 float64, in the given order): 80 zero bytes, uint32
 // LE count, then per triangle float32(Normal()), float32 vertices, 2 zero

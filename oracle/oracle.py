@@ -61,6 +61,7 @@ def lib():
         L.oracle_apply_transform.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                              ctypes.c_void_p, ctypes.c_int64]
         L.oracle_encode_stl.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+        L.oracle_group_triangles.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
         L.oracle_mesh_free.argtypes = [ctypes.POINTER(OracleMesh)]
         L.oracle_contains.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                       ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int64,
@@ -163,6 +164,16 @@ def encode_stl(tris):
     out = np.zeros(84 + 50 * len(t), dtype=np.uint8)
     lib().oracle_encode_stl(t.ctypes.data, len(t), out.ctypes.data)
     return out.tobytes()
+
+
+def group_triangles(tris):
+    """GroupTriangles (model3d/bvh.go:118-217) of a (T, 9) triangle soup:
+    the permutation SaveGroupedSTL writes the triangles in (ties in the
+    midpoint sorts keep the input order)."""
+    t = np.ascontiguousarray(tris, dtype=np.float64).reshape(-1, 9)
+    out = np.zeros(len(t), dtype=np.int32)
+    lib().oracle_group_triangles(t.ctypes.data, len(t), out.ctypes.data)
+    return out
 
 
 def apply_transform(steps, pts, inverse=False):

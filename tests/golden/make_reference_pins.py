@@ -18,6 +18,11 @@ in the build container, and never at test time):
   resolution.  reference_meshes.json keeps the triangle count, the SHA-256 of
   the 9 x float32 vertex bit patterns with rows sorted (vertex order inside a
   triangle kept), and the SHA-256 of the float32 normals in that row order.
+  The file's record order is SaveGroupedSTL's GroupTriangles order, which
+  the reference leaves to Go map order and an unstable sort on ties; what
+  it fixes is the top of the hierarchy: the axes along which the halves of
+  the nodes above depth 3 are separated by triangle midpoint, and the
+  midpoint centroids of the eight depth-3 nodes (file coordinates).
 * non_intersecting_hook.stl is a 19,584-triangle INPUT mesh
   (model3d/primitives_test.go:273-285).  It is stored as an indexed float32
   mesh in non_intersecting_hook.npz (unique vertices + faces); expanding it
@@ -57,6 +62,27 @@ def f32_digests(tris: np.ndarray, normals: np.ndarray):
             hashlib.sha256(np.ascontiguousarray(nrm).tobytes()).hexdigest())
 
 
+def grouping_signature(tris, depth=3):
+    """Top of a GroupTriangles hierarchy of (T, 9) triangles in grouped
+    order: per node above `depth` (preorder), the axes whose midpoints
+    separate its halves; per node at `depth`, its midpoint centroid."""
+    t = tris.reshape(-1, 3, 3)
+    mid = (t.min(1) + t.max(1)) * 0.5
+    axes, cents = [], []
+
+    def rec(lo, n, d):
+        if d == depth:
+            cents.append([float(x) for x in mid[lo:lo + n].mean(0)])
+            return
+        h = n // 2
+        axes.append([a for a in range(3) if mid[lo:lo + h, a].max() <= mid[lo + h:lo + n, a].min()])
+        rec(lo, h, d + 1)
+        rec(lo + h, n - h, d + 1)
+
+    rec(0, len(mid), 0)
+    return {"depth": depth, "separating_axes": axes, "centroids": cents}
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     data = os.path.join(ref, "model3d", "test_data")
@@ -70,6 +96,8 @@ def main():
         "delta": 0.03, "iters": 2, "triangles": int(len(h)),
         "sha256_f32_triangles": tri_sha, "sha256_f32_normals": nrm_sha,
     }
+
+    out["hierarchy_test_grouping"] = grouping_signature(np.ascontiguousarray(h["v"]).astype(np.float64))
 
     k = read_stl(open(os.path.join(data, "non_intersecting_hook.stl"), "rb").read())
     v = np.ascontiguousarray(k["v"]).reshape(-1, 3)
