@@ -348,7 +348,8 @@ def other_configs(ctx, torch, flush, single_rate, count=16):
     after a warm-up): unit sphere (delta 0.01), the 1,048,820-triangle
     displaced icosphere collider on a ~256^3 grid, 512 CSG solids in one
     batched launch (graph replay) next to the same solids one call at a
-    time, a 64-ball metaball, and batched colliders.  A configuration that
+    time, a 64-ball metaball, batched colliders, and SaveGroupedSTL of the
+    headline mesh (wall time, host bytes out).  A configuration that
     fails is reported under its name with the error, without losing the
     others or the headline line."""
     out = {}
@@ -356,13 +357,64 @@ def other_configs(ctx, torch, flush, single_rate, count=16):
              ("collider_icosphere_1048820_tris_256cubed", lambda: collider_line(ctx, torch, flush)),
              ("batch_512_csg", lambda: batch_line(ctx, torch, flush, single_rate)),
              ("metaball_blob64_quartic_delta0.005", lambda: metaball_line(ctx, torch, flush)),
-             ("batch_colliders", lambda: collider_batch_line(ctx, count, torch))]
+             ("batch_colliders", lambda: collider_batch_line(ctx, count, torch)),
+             ("save_grouped_stl_headline", lambda: grouped_stl_line(ctx, torch))]
     for name, f in lines:
         try:
             out.update(f())
         except Exception as e:  # noqa: BLE001 - reported in the JSON line
             out[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
     return out
+
+
+def grouped_stl_line(ctx, torch):
+    """SaveGroupedSTL of the headline mesh (4.17M triangles): GroupTriangles
+    and the STL encoding on the device over the search result, bytes copied
+    to the host (wall time, best of 3 after a warm-up), next to the plain
+    EncodeSTL of the same result; and end to end from the resident solid
+    (search + group + encode + copy, MarchingCubesSearchGroupedSTL)."""
+    import ctypes
+    import time
+    import numpy as np
+    from model3d_gb300 import DeviceSolid, MarchingCubesSearchGroupedSTL
+    from model3d_gb300 import _native as N
+    from model3d_gb300.workloads import csg_tree
+    L = N.lib()
+    ds = DeviceSolid(csg_tree(SEED, N_POS, N_NEG), ctx)
+    o = N.MCOpts()
+    o.precision = N.MC_PREC_FP32_FILTERED
+    o.cull = 1
+    V, T = ctypes.c_int64(), ctypes.c_int64()
+    st = N.MCStats()
+    if L.mc_search_device(ctx.ptr, ds.ptr, DELTA, ITERS, ctypes.byref(o), ctypes.byref(V), ctypes.byref(T),
+                          ctypes.byref(st)) != 0:
+        raise RuntimeError(L.mc_last_error(ctx.ptr).decode())
+    n = ctypes.c_size_t()
+    L.mc_result_stl(ctx.ptr, None, 0, ctypes.byref(n))
+    buf = np.empty(n.value, dtype=np.uint8)
+
+    def wall(f, reps=3):
+        best = None
+        for _ in range(reps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            f()
+            dt = (time.perf_counter() - t0) * 1e3
+            best = dt if best is None else min(best, dt)
+        return best
+
+    def call(fn):
+        if fn(ctx.ptr, buf.ctypes.data, n.value, ctypes.byref(n)) != 0:
+            raise RuntimeError(L.mc_last_error(ctx.ptr).decode())
+
+    ms_grouped = wall(lambda: call(L.mc_result_stl_grouped))
+    ms_plain = wall(lambda: call(L.mc_result_stl))
+    ms_e2e = wall(lambda: MarchingCubesSearchGroupedSTL(ds, DELTA, ITERS, ctx=ctx))
+    return {"save_grouped_stl_headline": {
+        "triangles": T.value, "stl_bytes": n.value,
+        "ms_group_encode_copy": ms_grouped, "ms_plain_encode_copy": ms_plain,
+        "ms_search_group_encode_copy": ms_e2e,
+        "triangles_per_s_grouped": T.value / (ms_grouped / 1e3)}}
 
 
 def sphere_line(ctx, torch, flush):

@@ -42,7 +42,10 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kPerThread = 16;
 constexpr int kTile = kThreads * kPerThread;  // positions per CTA in the tiled kernels
-constexpr int kWarpMax = 1024;                // largest node one warp splits
+#ifndef MC_GROUP_WARP_MAX
+#define MC_GROUP_WARP_MAX 1024
+#endif
+constexpr int kWarpMax = MC_GROUP_WARP_MAX;   // largest node one warp splits
 constexpr int kThreadMax = 32;                // largest node one thread finishes
 // (node, half) segments one tile of a wide depth can touch: its halves hold
 // at least kWarpMax / 2 triangles.
@@ -220,53 +223,80 @@ __global__ void __launch_bounds__(kThreads) k_rs_count(RsPass rp, long long T, i
     cnt[((size_t)a * 256 + threadIdx.x) * nb + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive prefix sum, in place, of n counts per axis (one CTA per axis).
+// Exclusive prefix sums of counts, in place.  One CTA of 1024 threads scans
+// a chunk of up to kScanChunk counts (8 a thread); longer arrays are scanned
+// chunk by chunk in parallel, then the chunk totals, then the offsets added.
+constexpr int kScanE = 8;
+constexpr long long kScanChunk = 1024LL * kScanE;
+
+// Scans d[0, n) (n <= kScanChunk), adding `add`; returns the chunk's total.
+__device__ unsigned cta_scan_chunk(unsigned int* __restrict__ d, long long n, unsigned add) {
+    __shared__ unsigned int ws[32];
+    __shared__ unsigned int total;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned v[kScanE], s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanE; k++) {
+        const long long i = (long long)threadIdx.x * kScanE + k;
+        v[k] = i < n ? d[i] : 0u;
+        s += v[k];
+    }
+    unsigned x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        ws[lane] = w;
+        if (lane == 31) total = w;
+    }
+    __syncthreads();
+    unsigned e = add + (warp ? ws[warp - 1] : 0u) + x - s;
+#pragma unroll
+    for (int k = 0; k < kScanE; k++) {
+        const long long i = (long long)threadIdx.x * kScanE + k;
+        if (i < n) d[i] = e;
+        e += v[k];
+    }
+    const unsigned t = total;
+    __syncthreads();  // ws and total are reused by the next call
+    return t;
+}
+
+// n counts per axis (blockIdx.x), one CTA each, chunk after chunk.
 __global__ void __launch_bounds__(1024) k_gt_scan(unsigned int* __restrict__ data, long long n, Act3 act) {
     if (!act.a[blockIdx.x]) return;
     unsigned int* dd = data + (size_t)blockIdx.x * n;
-    __shared__ unsigned int ws[32];
-    __shared__ unsigned int carry;
-    constexpr int E = 8;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (long long base = 0; base < n; base += 1024LL * E) {
-        unsigned v[E], s = 0;
-#pragma unroll
-        for (int k = 0; k < E; k++) {
-            const long long i = base + (long long)threadIdx.x * E + k;
-            v[k] = i < n ? dd[i] : 0u;
-            s += v[k];
-        }
-        unsigned x = s;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) ws[warp] = x;
-        __syncthreads();
-        if (warp == 0) {
-            unsigned w = ws[lane];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += y;
-            }
-            ws[lane] = w;
-        }
-        __syncthreads();
-        unsigned e = carry + (warp ? ws[warp - 1] : 0u) + x - s;
-#pragma unroll
-        for (int k = 0; k < E; k++) {
-            const long long i = base + (long long)threadIdx.x * E + k;
-            if (i < n) dd[i] = e;
-            e += v[k];
-        }
-        __syncthreads();
-        if (threadIdx.x == 1023) carry = e;
-        __syncthreads();
-    }
+    unsigned carry = 0;
+    for (long long base = 0; base < n; base += kScanChunk)
+        carry += cta_scan_chunk(dd + base, min(kScanChunk, n - base), carry);
+}
+
+// Chunk c of axis blockIdx.y scanned on its own; its total to tot[axis][c].
+__global__ void __launch_bounds__(1024) k_gt_scan_part(unsigned int* __restrict__ data, long long n, Act3 act,
+                                                       unsigned int* __restrict__ tot, long long nchunk) {
+    if (!act.a[blockIdx.y]) return;
+    const long long base = (long long)blockIdx.x * kScanChunk;
+    const unsigned t = cta_scan_chunk(data + (size_t)blockIdx.y * n + base, min(kScanChunk, n - base), 0u);
+    if (threadIdx.x == 0) tot[(size_t)blockIdx.y * nchunk + blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(1024) k_gt_scan_add(unsigned int* __restrict__ data, long long n, Act3 act,
+                                                      const unsigned int* __restrict__ tot, long long nchunk) {
+    if (!act.a[blockIdx.y]) return;
+    const unsigned add = tot[(size_t)blockIdx.y * nchunk + blockIdx.x];
+    unsigned int* d = data + (size_t)blockIdx.y * n + (long long)blockIdx.x * kScanChunk;
+    const long long m = min(kScanChunk, n - (long long)blockIdx.x * kScanChunk);
+    for (long long i = threadIdx.x; i < m; i += blockDim.x) d[i] += add;
 }
 
 // Stable scatter of one digit pass: warps take consecutive 512-key runs of
@@ -334,8 +364,37 @@ __global__ void k_gt_acc_init(unsigned long long* __restrict__ acc, long long n)
         acc[i] = (i % 6) < 3 ? ~0ull : 0ull;
 }
 
+// A triangle's box (min x y z, max x y z) in three 16-byte loads.
+__device__ __forceinline__ void load_box(const double* __restrict__ box, int32_t t, double b[6]) {
+    const double2* q = reinterpret_cast<const double2*>(box + 6 * (size_t)t);
+    const double2 u = q[0], v = q[1], w = q[2];
+    b[0] = u.x;
+    b[1] = u.y;
+    b[2] = v.x;
+    b[3] = v.y;
+    b[4] = w.x;
+    b[5] = w.y;
+}
+
+__device__ __forceinline__ void box_empty(double b[6]) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        b[c] = g_inf();
+        b[3 + c] = -g_inf();
+    }
+}
+
+__device__ __forceinline__ void box_widen(double b[6], const double q[6]) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (q[c] < b[c]) b[c] = q[c];
+        if (q[3 + c] > b[3 + c]) b[3 + c] = q[3 + c];
+    }
+}
+
 // multipleBoundsArea's boxes (bvh.go:257-287) of every node half, one axis'
-// order per blockIdx.y.
+// order per blockIdx.y.  A thread reduces 16 consecutive positions and
+// flushes each half it met into the tile's shared slots.
 __global__ void __launch_bounds__(kThreads) k_gt_reduce(const int32_t* __restrict__ ord, const double* __restrict__ box,
                                                         long long T, int L, unsigned long long* __restrict__ acc,
                                                         int* __restrict__ err) {
@@ -355,7 +414,7 @@ __global__ void __launch_bounds__(kThreads) k_gt_reduce(const int32_t* __restric
     long long p = p0 + (long long)threadIdx.x * kPerThread;
     const long long pe = min(p + kPerThread, T);
     long long seg_end = -1, key = 0;
-    double mn[3], mx[3];
+    double bx[6];
     bool have = false;
     auto flush = [&]() {
         const long long sl = key - key0;
@@ -365,8 +424,8 @@ __global__ void __launch_bounds__(kThreads) k_gt_reduce(const int32_t* __restric
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            atomicMin(&s[sl * 6 + c], okey(mn[c]));
-            atomicMax(&s[sl * 6 + 3 + c], okey(mx[c]));
+            atomicMin(&s[sl * 6 + c], okey(bx[c]));
+            atomicMax(&s[sl * 6 + 3 + c], okey(bx[3 + c]));
         }
     };
     for (; p < pe; p++) {
@@ -378,20 +437,12 @@ __global__ void __launch_bounds__(kThreads) k_gt_reduce(const int32_t* __restric
             const int half = (p - lo) >= h ? 1 : 0;
             key = 2 * k + half;
             seg_end = half ? lo + n : lo + h;
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                mn[c] = g_inf();
-                mx[c] = -g_inf();
-            }
+            box_empty(bx);
             have = true;
         }
-        const double* b = box + 6 * (size_t)o[p];
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const double lo_c = b[c], hi_c = b[3 + c];
-            if (lo_c < mn[c]) mn[c] = lo_c;
-            if (hi_c > mx[c]) mx[c] = hi_c;
-        }
+        double b[6];
+        load_box(box, o[p], b);
+        box_widen(bx, b);
     }
     if (have) flush();
     __syncthreads();
@@ -510,14 +561,6 @@ __global__ void __launch_bounds__(kThreads) k_gt_pscatter(const int32_t* __restr
 
 // ---------------------------------------------------------------- warp depths
 
-__device__ __forceinline__ void box_widen(double b[6], const double* q) {
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        if (q[c] < b[c]) b[c] = q[c];
-        if (q[3 + c] > b[3 + c]) b[3 + c] = q[3 + c];
-    }
-}
-
 __device__ __forceinline__ void box_warp_reduce(double b[6]) {
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
@@ -531,10 +574,12 @@ __device__ __forceinline__ void box_warp_reduce(double b[6]) {
 }
 
 // One warp per node of 33..1024 triangles: axis choice, flags, and the
-// stable partition of all three orders (ballot ranks) into oout.
+// stable partition of all three orders (ballot ranks) into oout.  Lanes take
+// four positions a round, loads first, for memory-level parallelism.
 __global__ void __launch_bounds__(kThreads) k_gt_warp(const int32_t* __restrict__ oin, int32_t* __restrict__ oout,
                                                       const double* __restrict__ box, uint8_t* __restrict__ lower,
                                                       long long T, int L, long long NL) {
+    constexpr int U = 4;
     const int lane = threadIdx.x & 31;
     const long long k = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (k >= NL) return;  // warp-uniform
@@ -545,12 +590,23 @@ __global__ void __launch_bounds__(kThreads) k_gt_warp(const int32_t* __restrict_
     double best = 0;
     for (int a = 0; a < 3; a++) {
         const int32_t* o = oin + (size_t)a * T + lo;
-        double b0[6] = {g_inf(), g_inf(), g_inf(), -g_inf(), -g_inf(), -g_inf()};
-        double b1[6] = {g_inf(), g_inf(), g_inf(), -g_inf(), -g_inf(), -g_inf()};
-        for (int i = lane; i < m; i += 32) {
-            const double* q = box + 6 * (size_t)o[i];
-            if (i < h) box_widen(b0, q);
-            else box_widen(b1, q);
+        double b0[6], b1[6];
+        box_empty(b0);
+        box_empty(b1);
+        for (int i0 = lane; i0 < m; i0 += 32 * U) {
+            int32_t t[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) t[u] = i0 + 32 * u < m ? o[i0 + 32 * u] : -1;
+            double q[U][6];
+#pragma unroll
+            for (int u = 0; u < U; u++)
+                if (t[u] >= 0) load_box(box, t[u], q[u]);
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (t[u] < 0) continue;
+                if (i0 + 32 * u < h) box_widen(b0, q[u]);
+                else box_widen(b1, q[u]);
+            }
         }
         box_warp_reduce(b0);
         box_warp_reduce(b1);
@@ -568,42 +624,49 @@ __global__ void __launch_bounds__(kThreads) k_gt_warp(const int32_t* __restrict_
         const int32_t* o = oin + (size_t)a * T + lo;
         int32_t* w = oout + (size_t)a * T + lo;
         int cl = 0, cu = 0;
-        for (int base = 0; base < m; base += 32) {
-            const int i = base + lane;
-            const bool ok = i < m;
-            const int32_t t = ok ? o[i] : 0;
-            const bool f = ok && lower[t];
-            const unsigned bl = __ballot_sync(0xffffffffu, f), bv = __ballot_sync(0xffffffffu, ok);
-            if (ok) w[f ? cl + __popc(bl & lt) : h + cu + __popc(bv & ~bl & lt)] = t;
-            cl += __popc(bl);
-            cu += __popc(bv & ~bl);
+        for (int base = 0; base < m; base += 32 * U) {
+            int32_t t[U];
+            bool f[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) t[u] = base + 32 * u + lane < m ? o[base + 32 * u + lane] : -1;
+#pragma unroll
+            for (int u = 0; u < U; u++) f[u] = t[u] >= 0 && lower[t[u]];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const bool ok = t[u] >= 0;
+                const unsigned bl = __ballot_sync(0xffffffffu, f[u]), bv = __ballot_sync(0xffffffffu, ok);
+                if (ok) w[f[u] ? cl + __popc(bl & lt) : h + cu + __popc(bv & ~bl & lt)] = t[u];
+                cl += __popc(bl);
+                cu += __popc(bv & ~bl);
+            }
         }
     }
 }
 
 // ---------------------------------------------------------------- finish
 
+constexpr int kFinishThreads = 128;
+
 // multipleBoundsArea (bvh.go:257-287) of n local items.
 __device__ double local_area(const double* __restrict__ box, const int32_t* id, const uint8_t* s, int n) {
-    const double* b = box + 6 * (size_t)id[s[0]];
-    double x0 = b[0], y0 = b[1], z0 = b[2], x1 = b[3], y1 = b[4], z1 = b[5];
+    double b[6];
+    load_box(box, id[s[0]], b);
     for (int i = 1; i < n; i++) {
-        b = box + 6 * (size_t)id[s[i]];
-        if (b[0] < x0) x0 = b[0];
-        if (b[1] < y0) y0 = b[1];
-        if (b[2] < z0) z0 = b[2];
-        if (b[3] > x1) x1 = b[3];
-        if (b[4] > y1) y1 = b[4];
-        if (b[5] > z1) z1 = b[5];
+        double q[6];
+        load_box(box, id[s[i]], q);
+        box_widen(b, q);
     }
-    return bounds_area(x0, y0, z0, x1, y1, z1);
+    return bounds_area(b[0], b[1], b[2], b[3], b[4], b[5]);
 }
 
 // One thread per node of at most 32 triangles: the rest of groupBounders
 // (bvh.go:135-156) depth first, writing the final order of its positions.
-__global__ void __launch_bounds__(128) k_gt_finish(const int32_t* __restrict__ oin, const double* __restrict__ box,
-                                                   int32_t* __restrict__ loc, long long T, int L, long long NL,
-                                                   int32_t* __restrict__ order, int* __restrict__ err) {
+// (Boxes staged in shared memory measured slower: 48 KB per 32 threads
+// leaves four warps an SM.)
+__global__ void __launch_bounds__(kFinishThreads) k_gt_finish(const int32_t* __restrict__ oin,
+                                                              const double* __restrict__ box, int32_t* __restrict__ loc,
+                                                              long long T, int L, long long NL,
+                                                              int32_t* __restrict__ order, int* __restrict__ err) {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= NL) return;
     long long lo, n;
@@ -669,15 +732,34 @@ __global__ void __launch_bounds__(128) k_gt_finish(const int32_t* __restrict__ o
 }  // namespace
 
 struct GroupScratch {
-    GBuf box, keys[2], vals[2], hist, cnt, lower, acc, axis, before, pcnt, loc, err;
+    GBuf box, keys[2], vals[2], hist, cnt, lower, acc, axis, before, pcnt, loc, err, stot;
     ~GroupScratch() {
         for (GBuf* b : {&box, &keys[0], &keys[1], &vals[0], &vals[1], &hist, &cnt, &lower, &acc, &axis, &before,
-                        &pcnt, &loc, &err})
+                        &pcnt, &loc, &err, &stot})
             b->release();
     }
 };
 
 GroupScratch* group_scratch_new() { return new GroupScratch(); }
+
+namespace {
+
+// Exclusive scan of n counts for each active axis (data: 3 x n).
+cudaError_t scan3(GroupScratch* g, unsigned int* data, long long n, Act3 act, cudaStream_t st) {
+    if (n <= kScanChunk) {
+        k_gt_scan<<<3, 1024, 0, st>>>(data, n, act);
+        return cudaGetLastError();
+    }
+    const long long nchunk = (n + kScanChunk - 1) / kScanChunk;
+    cudaError_t e = g->stot.ensure((size_t)3 * nchunk * 4);
+    if (e != cudaSuccess) return e;
+    k_gt_scan_part<<<dim3((unsigned)nchunk, 3), 1024, 0, st>>>(data, n, act, g->stot.as<unsigned int>(), nchunk);
+    k_gt_scan<<<3, 1024, 0, st>>>(g->stot.as<unsigned int>(), nchunk, act);
+    k_gt_scan_add<<<dim3((unsigned)nchunk, 3), 1024, 0, st>>>(data, n, act, g->stot.as<unsigned int>(), nchunk);
+    return cudaGetLastError();
+}
+
+}  // namespace
 void group_scratch_free(GroupScratch* g) { delete g; }
 
 cudaError_t group_triangles_device(GroupScratch* g, const double* verts, const int32_t* tris, long long T,
@@ -735,8 +817,7 @@ cudaError_t group_triangles_device(GroupScratch* g, const double* verts, const i
         if (!any) continue;
         k_rs_count<<<dim3((unsigned)nb, 3), kThreads, 0, st>>>(rp, T, d, nb, g->cnt.as<unsigned int>());
         GK(cudaGetLastError());
-        k_gt_scan<<<3, 1024, 0, st>>>(g->cnt.as<unsigned int>(), 256 * nb, act);
-        GK(cudaGetLastError());
+        GK(scan3(g, g->cnt.as<unsigned int>(), 256 * nb, act, st));
         k_rs_scatter<<<dim3((unsigned)nb, 3), kThreads, 0, st>>>(rp, T, d, nb, g->cnt.as<unsigned int>());
         GK(cudaGetLastError());
         for (int a = 0; a < 3; a++) cur[a] ^= act.a[a];
@@ -775,8 +856,8 @@ cudaError_t group_triangles_device(GroupScratch* g, const double* verts, const i
         const long long NL = 1LL << L;
         const long long nmax = (T + NL - 1) / NL;
         if (nmax <= kThreadMax) {
-            k_gt_finish<<<(unsigned)((NL + 127) / 128), 128, 0, st>>>(oin, g->box.as<double>(), g->loc.as<int32_t>(), T,
-                                                                    L, NL, order, err);
+            k_gt_finish<<<(unsigned)((NL + kFinishThreads - 1) / kFinishThreads), kFinishThreads, 0, st>>>(
+                oin, g->box.as<double>(), g->loc.as<int32_t>(), T, L, NL, order, err);
             GK(cudaGetLastError());
             break;
         }
@@ -791,7 +872,7 @@ cudaError_t group_triangles_device(GroupScratch* g, const double* verts, const i
             k_gt_flag<<<grid_t, kThreads, 0, st>>>(oin, T, L, g->axis.as<uint8_t>(), g->lower.as<uint8_t>());
             k_gt_pcount<<<dim3((unsigned)nb, 3), kThreads, 0, st>>>(oin, g->lower.as<uint8_t>(), T, nb,
                                                                      g->pcnt.as<unsigned int>());
-            k_gt_scan<<<3, 1024, 0, st>>>(g->pcnt.as<unsigned int>(), nb, Act3{{1, 1, 1}});
+            GK(scan3(g, g->pcnt.as<unsigned int>(), nb, Act3{{1, 1, 1}}, st));
             k_gt_pscatter<<<dim3((unsigned)nb, 3), kThreads, 0, st>>>(oin, oout, g->lower.as<uint8_t>(), T, L,
                                                                        g->pcnt.as<unsigned int>(), nb,
                                                                        g->before.as<long long>() + before_at[L]);

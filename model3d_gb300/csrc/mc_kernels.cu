@@ -700,6 +700,15 @@ __device__ __forceinline__ bool cull_overlap(const double* c, const double lo[3]
 
 // ------------------------------------------------------------ k_classify
 
+__device__ __forceinline__ float warp_minf(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_maxf(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
 struct ClassifyArgs {
     uint32_t* bits;
     int* err;
@@ -713,7 +722,17 @@ struct ClassifyArgs {
     int ty, tz;  // tile height / depth (rows per tile = ty * tz)
     int ntx, nty, ntz;
     int nxs;  // x segments per column (0 or 1: one item walks the whole column)
+    // Collider programs: work items are ray-aligned lines of 32 corners
+    // (classify_line) instead of tile columns; shear_y/z(31) of the line.
+    int shear;
+    int sy_max, sz_max;
 };
+
+// The lane offsets of a ray-aligned line: corner (32 bx + i, y' + shear_y(i),
+// z' + shear_z(i)) lies within half a grid step (in y and z) of the
+// collider ray (collisions.go:124) through lane 0's corner.
+__host__ __device__ __forceinline__ int shear_y(int i) { return (int)rint(RAYGRID_KY * i); }
+__host__ __device__ __forceinline__ int shear_z(int i) { return (int)rint(RAYGRID_KZ * i); }
 
 __device__ __forceinline__ bool cull_overlap_f(const float* c, const float lo[3], const float hi[3]) {
     return !(hi[0] < c[0] || lo[0] > c[3] || hi[1] < c[1] || lo[1] > c[4] || hi[2] < c[2] || lo[2] > c[5]);
@@ -863,6 +882,75 @@ __device__ __forceinline__ void classify_column(const GridView& g, const ProgVie
     }
 }
 
+// Work item of a collider program: the ray-aligned line (bx, y', z') =
+// item decomposed with y' fastest, corners (32 bx + i, y' + shear_y(i),
+// z' + shear_z(i)) for lane i.  For each x the shear is a shift of (y, z),
+// so the lines cover every corner once.  A collider query projects a corner
+// along the ray onto the ray grid (collider_point), so the line's corners
+// fall within half a step of one ray-grid point: the warp's queries walk
+// the same or neighbouring cells' candidate lists and test the same
+// triangles, where a row of 32 x-consecutive corners spreads over 27 grid
+// steps of the grid's b axis.  Bits are set with atomicOr (the bit array is
+// zeroed before the launch).
+template <int PREC>
+__device__ __forceinline__ void classify_line(const GridView& g, const ProgView& P, const ClassifyArgs& a, int item,
+                                              uint32_t* q, uint32_t* cur, Counts& cnt, unsigned long long& nconst) {
+    const int lane = threadIdx.x & 31;
+    const int nyl = g.ny + a.sy_max, nzl = g.nz + a.sz_max;
+    const int yy = item % nyl - a.sy_max;
+    const int rest = item / nyl;
+    const int zz = rest % nzl - a.sz_max;
+    const int bx = rest / nzl;
+    const int x = bx * 32 + lane, y = yy + shear_y(lane), z = zz + shear_z(lane);
+    const bool in = x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz;
+    if (!__any_sync(0xffffffffu, in)) return;
+    int len = P.n_ops;
+    const uint32_t* prog = P.ops;
+    if (a.cull) {
+        const float lo[3] = {warp_minf(in ? __double2float_rd(g.xs[x]) : CUDART_INF_F),
+                             warp_minf(in ? __double2float_rd(g.ys[y]) : CUDART_INF_F),
+                             warp_minf(in ? __double2float_rd(g.zs[z]) : CUDART_INF_F)};
+        const float hi[3] = {warp_maxf(in ? __double2float_ru(g.xs[x]) : -CUDART_INF_F),
+                             warp_maxf(in ? __double2float_ru(g.ys[y]) : -CUDART_INF_F),
+                             warp_maxf(in ? __double2float_ru(g.zs[z]) : -CUDART_INF_F)};
+        const int nw = (P.n_leaves + 31) >> 5;
+        uint32_t any = 0;
+        for (int k = 0; k < nw; k++) {
+            const int l = 32 * k + lane;
+            const bool on = l < P.n_leaves && cull_overlap_f(P.cull_f + 6 * (size_t)l, lo, hi);
+            const uint32_t w = __ballot_sync(0xffffffffu, on);
+            any |= w;
+            if (lane == 0) cur[k] = w;
+        }
+        if (!any) {
+            len = P.n_ops_allfalse;
+            prog = P.ops_allfalse;
+        } else {
+            int L = 0;
+            __syncwarp();
+            if (lane == 0) L = fold_program(P.ops, P.n_ops, cur, q);
+            len = __shfl_sync(0xffffffffu, L, 0);
+            prog = q;
+        }
+        __syncwarp();
+    }
+    if (len < 0) nconst++;
+    bool b = false;
+    if (in) {
+        if (len == FOLD_TRUE) b = true;
+        else if (len != FOLD_FALSE)
+            b = eval_program<PREC>(P, prog, len, P3{g.xs[x], g.ys[y], g.zs[z]}, F3{a.xf[x], a.yf[y], a.zf[z]}, cnt,
+                                   a.err);
+    }
+    if (b) {
+        atomicOr(&a.bits[((size_t)z * g.ny + y) * g.W + bx], 1u << lane);
+        // solid is true outside of bounds (mc.go:687-689)
+        if (x == 0 || x == g.nx - 1 || y == 0 || y == g.ny - 1 || (z == 0 && g.zb0) || (z == g.nz - 1 && g.zb1))
+            atomicOr(&a.err[ER_BORDER], 1);
+    }
+    __syncwarp();
+}
+
 // One warp per work item, items handed out by an atomic counter.
 template <int PREC>
 __device__ __forceinline__ void classify_items(const GridView& g, const ProgView& P, const ClassifyArgs& a) {
@@ -875,13 +963,15 @@ __device__ __forceinline__ void classify_items(const GridView& g, const ProgView
     uint32_t* prev = cur + nw;
     Counts cnt;
     unsigned long long nconst = 0;
-    const int nitems = a.nty * a.ntz * (a.nxs > 1 ? a.nxs : 1);
+    const int nitems = a.shear ? a.ntx * (g.ny + a.sy_max) * (g.nz + a.sz_max)
+                               : a.nty * a.ntz * (a.nxs > 1 ? a.nxs : 1);
     for (;;) {
         int item = 0;
         if (lane == 0) item = (int)atomicAdd(a.work, 1u);
         item = __shfl_sync(0xffffffffu, item, 0);
         if (item >= nitems) break;
-        classify_column<PREC>(g, P, a, item, q, cur, prev, cnt, nconst);
+        if (a.shear) classify_line<PREC>(g, P, a, item, q, cur, cnt, nconst);
+        else classify_column<PREC>(g, P, a, item, q, cur, prev, cnt, nconst);
     }
     flush_counts(cnt, a.stats, ST_FLOPS_CLASSIFY);
     if (lane == 0 && nconst) atomicAdd(&a.stats[ST_TILES_CONST], nconst);
@@ -1398,14 +1488,6 @@ struct SearchArgs {
     double* interior;  // V x 3 interior points, or null
 };
 
-__device__ __forceinline__ float warp_minf(float v) {
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-__device__ __forceinline__ float warp_maxf(float v) {
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
 __device__ __forceinline__ double warp_min(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
@@ -1766,7 +1848,8 @@ __global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify_batch(
         const JobD& J = b.jobs[b.sched_job[k]];
         const int nw = (J.P.n_leaves + 31) >> 5;
         uint32_t* cur = base + J.P.fold_cap;
-        classify_column<PREC>(J.g, J.P, J.ca, (int)(item - b.sched_off[k]), base, cur, cur + nw, cnt, nconst);
+        if (J.ca.shear) classify_line<PREC>(J.g, J.P, J.ca, (int)(item - b.sched_off[k]), base, cur, cnt, nconst);
+        else classify_column<PREC>(J.g, J.P, J.ca, (int)(item - b.sched_off[k]), base, cur, cur + nw, cnt, nconst);
     }
     flush_counts(cnt, b.stats, ST_FLOPS_CLASSIFY);
     if (lane == 0 && nconst) atomicAdd(&b.stats[ST_TILES_CONST], nconst);
@@ -2126,6 +2209,13 @@ void pick_tiles(const mc_opts* user, const HostProgram& H, int tuned_ty, int tun
         *ty = cand[k][0];
         *tz = cand[k][1];
     }
+}
+
+// Collider programs classify ray-aligned lines (classify_line) unless the
+// caller fixed a tile shape; the item count must fit an int.
+bool use_lines(const mc_opts* user, const HostProgram& H, int ntx, int ny, int nz) {
+    if (!H.has_collider || (user && (user->tile_y > 0 || user->tile_z > 0))) return false;
+    return (long long)ntx * (ny + shear_y(31)) * (nz + shear_z(31)) < (1LL << 31) - 1;
 }
 
 // Classification work items: each tile column splits along x into segments
@@ -2539,6 +2629,12 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
     const long long cols = (long long)ca.nty * ca.ntz;
     ca.nxs = pick_xsegments(cols, ca.ntx, warps_c, P.has_metaball);
     long long items = cols * ca.nxs;
+    if (use_lines(opts_in, H, ca.ntx, ny, nz)) {
+        ca.shear = 1;
+        ca.sy_max = shear_y(31);
+        ca.sz_max = shear_z(31);
+        items = (long long)ca.ntx * (ny + ca.sy_max) * (nz + ca.sz_max);
+    }
     int grid_c = (int)std::max<long long>(1, std::min<long long>((items + 7) / 8, (long long)ctx->sm_count * std::max(occ, 1)));
     kc<<<grid_c, 256, smem_c, sm>>>(g, P, ca);
     CK(cudaGetLastError());
@@ -3215,6 +3311,12 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             L.bits = nbits_total;
             nbits_total += L.nbits;
             L.items = (long long)J.ca.nty * J.ca.ntz;
+            if (use_lines(opts_in, jobs[i].solid->host, J.ca.ntx, ny, nz)) {
+                J.ca.shear = 1;
+                J.ca.sy_max = shear_y(31);
+                J.ca.sz_max = shear_z(31);
+                L.items = (long long)J.ca.ntx * (ny + J.ca.sy_max) * (nz + J.ca.sz_max);
+            }
             L.cost = (long long)nx * ny * nz;
             const int nw = (J.P.n_leaves + 31) / 32;
             fold_words = std::max(fold_words, (J.P.fold_cap + 2 * nw + 3) & ~3);
