@@ -371,8 +371,10 @@ def grouped_stl_line(ctx, torch):
     """SaveGroupedSTL of the headline mesh (4.17M triangles): GroupTriangles
     and the STL encoding on the device over the search result, bytes copied
     to the host (wall time, best of 3 after a warm-up), next to the plain
-    EncodeSTL of the same result; and end to end from the resident solid
-    (search + group + encode + copy, MarchingCubesSearchGroupedSTL)."""
+    EncodeSTL of the same result; end to end from the resident solid
+    (search + group + encode + copy into a reused buffer); and the Python
+    call MarchingCubesSearchGroupedSTL, whose fresh 208 MB buffer is
+    page-faulted on every call."""
     import ctypes
     import time
     import numpy as np
@@ -407,13 +409,22 @@ def grouped_stl_line(ctx, torch):
         if fn(ctx.ptr, buf.ctypes.data, n.value, ctypes.byref(n)) != 0:
             raise RuntimeError(L.mc_last_error(ctx.ptr).decode())
 
+    def search_group():
+        s2 = N.MCStats()
+        if L.mc_search_device(ctx.ptr, ds.ptr, DELTA, ITERS, ctypes.byref(o), ctypes.byref(V), ctypes.byref(T),
+                              ctypes.byref(s2)) != 0:
+            raise RuntimeError(L.mc_last_error(ctx.ptr).decode())
+        call(L.mc_result_stl_grouped)
+
     ms_grouped = wall(lambda: call(L.mc_result_stl_grouped))
     ms_plain = wall(lambda: call(L.mc_result_stl))
-    ms_e2e = wall(lambda: MarchingCubesSearchGroupedSTL(ds, DELTA, ITERS, ctx=ctx))
+    ms_e2e = wall(search_group)
+    ms_py = wall(lambda: MarchingCubesSearchGroupedSTL(ds, DELTA, ITERS, ctx=ctx), reps=1)
     return {"save_grouped_stl_headline": {
         "triangles": T.value, "stl_bytes": n.value,
         "ms_group_encode_copy": ms_grouped, "ms_plain_encode_copy": ms_plain,
         "ms_search_group_encode_copy": ms_e2e,
+        "ms_python_call_fresh_buffer": ms_py,
         "triangles_per_s_grouped": T.value / (ms_grouped / 1e3)}}
 
 

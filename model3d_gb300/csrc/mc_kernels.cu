@@ -40,7 +40,7 @@
 // Resident blocks per SM the classification (256 threads) and search (128
 // threads) kernels are compiled for; they set the register budget per thread.
 #ifndef MC_CLASSIFY_MIN_BLOCKS
-#define MC_CLASSIFY_MIN_BLOCKS 3
+#define MC_CLASSIFY_MIN_BLOCKS 4
 #endif
 #ifndef MC_CLASSIFY_WIDE_MIN_BLOCKS
 #define MC_CLASSIFY_WIDE_MIN_BLOCKS 2
@@ -984,9 +984,11 @@ __global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify(GridVi
 
 // The same with a larger register budget (fewer resident blocks): faster for
 // CSG programs, whose tiles spill at the tighter budget (headline tree:
-// 0.427 -> 0.401 ms).  A collider row costs a ray query per corner and a
-// metaball corner a sum over the balls; both want the resident warps
-// (1M-triangle collider 2.53 -> 2.97 ms, 64-ball metaball 9.2 -> 11.7 ms).
+// 0.427 -> 0.401 ms).  A collider corner costs a ray query and a metaball
+// corner a sum over the balls; both want the resident warps: at two blocks
+// instead of three the 1M-triangle collider took 2.53 -> 2.97 ms and the
+// 64-ball metaball 9.2 -> 11.7 ms, and at four (64 registers, with spills)
+// instead of three 1.80 -> 1.67 ms (ray-aligned lines) and 9.20 -> 8.56 ms.
 template <int PREC>
 __global__ void __launch_bounds__(256, MC_CLASSIFY_WIDE_MIN_BLOCKS) k_classify_wide(GridView g, ProgView P,
                                                                                    ClassifyArgs a) {

@@ -74,6 +74,11 @@ class Solid:
     def Max(self) -> Coord3D:
         raise NotImplementedError
 
+    def _bounds(self):
+        """(Min(), Max()) with the same float64 operations; the primitives
+        and boolean nodes share work between the two (one tree walk)."""
+        return self.Min(), self.Max()
+
 
 class Sphere(Solid):
     """model3d/shapes.go:13-31."""
@@ -86,6 +91,9 @@ class Sphere(Solid):
 
     def Max(self):
         return self.Center.AddScalar(self.Radius)
+
+    def _bounds(self):
+        return self.Center.AddScalar(-self.Radius), self.Center.AddScalar(self.Radius)
 
 
 class Rect(Solid):
@@ -125,6 +133,12 @@ class Cylinder(Solid):
         axis = self.P2.Sub(self.P1)
         return maxCenter.Add(_circle_axis_offset(axis, 1.0, self.Radius))
 
+    def _bounds(self):
+        # circleAxisBound is odd in its sign argument, exactly: every
+        # operation of _circle_axis_offset commutes with negation.
+        off = _circle_axis_offset(self.P2.Sub(self.P1), 1.0, self.Radius)
+        return self.P1.Min(self.P2).Add(XYZ(-off.X, -off.Y, -off.Z)), self.P1.Max(self.P2).Add(off)
+
 
 class Capsule(Solid):
     """model3d/shapes.go:348-368."""
@@ -137,6 +151,9 @@ class Capsule(Solid):
 
     def Max(self):
         return self.P1.Max(self.P2).AddScalar(self.Radius)
+
+    def _bounds(self):
+        return self.P1.Min(self.P2).AddScalar(-self.Radius), self.P1.Max(self.P2).AddScalar(self.Radius)
 
 
 class Torus(Solid):
@@ -179,6 +196,13 @@ class JoinedSolid(Solid):
             m = m.Max(s.Max())
         return m
 
+    def _bounds(self):
+        lo, hi = self.solids[0]._bounds()
+        for s in self.solids[1:]:
+            a, b = s._bounds()
+            lo, hi = lo.Min(a), hi.Max(b)
+        return lo, hi
+
     def Optimize(self) -> Solid:
         """JoinedSolid.Optimize (model3d/solid.go:100-118)."""
         grouped = GroupBounders(list(self.solids))
@@ -205,6 +229,9 @@ class SubtractedSolid(Solid):
     def Max(self):
         return self.Positive.Max()
 
+    def _bounds(self):
+        return self.Positive._bounds()
+
 
 def Subtract(x: Solid, y: Solid) -> SubtractedSolid:
     return SubtractedSolid(x, y)
@@ -229,6 +256,13 @@ class IntersectedSolid(Solid):
         for s in self.solids[1:]:
             b = b.Min(s.Max())
         return b.Max(self.Min())
+
+    def _bounds(self):
+        lo, hi = self.solids[0]._bounds()
+        for s in self.solids[1:]:
+            a, b = s._bounds()
+            lo, hi = lo.Max(a), hi.Min(b)
+        return lo, hi.Max(lo)
 
 
 # ------------------------------------------------------------- transforms
@@ -529,7 +563,8 @@ def serialize(solid: Solid):
 
     def node(kind, s=None, n_children=0, n_steps=0, mesh=0, p=()):
         if s is not None and (not recs or kind in (COLLIDER, TRANSFORM, CHECKED, METABALL)):
-            mn, mx = s.Min().Array(), s.Max().Array()
+            lo, hi = s._bounds()
+            mn, mx = lo.Array(), hi.Array()
         else:
             mn = mx = zero3
         recs.append(_NODE_PACK.pack(kind, n_children, n_steps, mesh, *mn, *mx, *p, *_ZEROS[len(p):]))
