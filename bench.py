@@ -10,8 +10,11 @@ One step = one MarchingCubesSearch of the solid resident on the device
 (corner classification, cube classification + prefix sums, emission, edge
 bisection).  L2 is flushed (a 256 MiB write) before every timed step; step
 time is the library's CUDA-event time on its own stream.  Under torchrun
-each rank runs an independent replica (the path does not shard: replicas
-only) and ``value`` sums all ranks' corners over the slowest rank's time.
+every rank meshes the headline solid (weak scaling: one solid a rank) and
+``value`` sums all ranks' corners over the slowest rank's time; the batched
+configurations (512 CSG solids, 64 colliders) are split across the ranks by
+solid, largest first (model3d_gb300/shard.py), with no collective on the
+data path.
 """
 from __future__ import annotations
 
