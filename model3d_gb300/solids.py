@@ -79,6 +79,12 @@ class Solid:
         and boolean nodes share work between the two (one tree walk)."""
         return self.Min(), self.Max()
 
+    def _own_bounds(self, cls) -> bool:
+        """Whether Min and Max are cls's own (not overridden by a subclass),
+        so that cls's _bounds computes what they would."""
+        t = type(self)
+        return t.Min is cls.Min and t.Max is cls.Max
+
 
 class Sphere(Solid):
     """model3d/shapes.go:13-31."""
@@ -93,6 +99,8 @@ class Sphere(Solid):
         return self.Center.AddScalar(self.Radius)
 
     def _bounds(self):
+        if not self._own_bounds(Sphere):
+            return self.Min(), self.Max()
         return self.Center.AddScalar(-self.Radius), self.Center.AddScalar(self.Radius)
 
 
@@ -134,6 +142,8 @@ class Cylinder(Solid):
         return maxCenter.Add(_circle_axis_offset(axis, 1.0, self.Radius))
 
     def _bounds(self):
+        if not self._own_bounds(Cylinder):
+            return self.Min(), self.Max()
         # circleAxisBound is odd in its sign argument, exactly: every
         # operation of _circle_axis_offset commutes with negation.
         off = _circle_axis_offset(self.P2.Sub(self.P1), 1.0, self.Radius)
@@ -153,6 +163,8 @@ class Capsule(Solid):
         return self.P1.Max(self.P2).AddScalar(self.Radius)
 
     def _bounds(self):
+        if not self._own_bounds(Capsule):
+            return self.Min(), self.Max()
         return self.P1.Min(self.P2).AddScalar(-self.Radius), self.P1.Max(self.P2).AddScalar(self.Radius)
 
 
@@ -197,6 +209,8 @@ class JoinedSolid(Solid):
         return m
 
     def _bounds(self):
+        if not self._own_bounds(JoinedSolid):
+            return self.Min(), self.Max()
         lo, hi = self.solids[0]._bounds()
         for s in self.solids[1:]:
             a, b = s._bounds()
@@ -230,6 +244,8 @@ class SubtractedSolid(Solid):
         return self.Positive.Max()
 
     def _bounds(self):
+        if not self._own_bounds(SubtractedSolid):
+            return self.Min(), self.Max()
         return self.Positive._bounds()
 
 
@@ -258,6 +274,8 @@ class IntersectedSolid(Solid):
         return b.Max(self.Min())
 
     def _bounds(self):
+        if not self._own_bounds(IntersectedSolid):
+            return self.Min(), self.Max()
         lo, hi = self.solids[0]._bounds()
         for s in self.solids[1:]:
             a, b = s._bounds()

@@ -178,3 +178,19 @@ def test_digest_follows_every_byte():
     moved = tris.copy()
     moved[7, 4] = math.nextafter(moved[7, 4], 9.0)
     assert check_program(NewColliderSolid(MeshToCollider(moved)))["digest"] != d0
+
+
+def test_overridden_bounds_are_serialised():
+    """A subclass that overrides Min/Max (as the batch's border-panic test
+    does) is serialised with its own bounds, inside a tree as at the root."""
+    class Lying(Sphere):
+        def Min(self):
+            return XYZ(-0.5, -0.5, -0.5)
+
+        def Max(self):
+            return XYZ(0.5, 0.5, 0.5)
+
+    for s in (Lying(XYZ(0, 0, 0), 1.0), JoinedSolid([Lying(XYZ(0, 0, 0), 1.0), Sphere(XYZ(0, 0, 0), 0.2)]),
+              SubtractedSolid(Lying(XYZ(0.1, 0, 0), 1.0), Sphere(XYZ(0, 0, 0), 0.2))):
+        _assert_root_bounds(check_program(s), s)
+        assert s.Max().Array() == [0.5, 0.5, 0.5]
