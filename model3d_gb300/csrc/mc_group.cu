@@ -132,9 +132,15 @@ __device__ __forceinline__ long long gt_find(long long T, int L, long long p, lo
 // ---------------------------------------------------------------- boxes
 
 // Triangle.Min / Max (primitives.go:36-43) and the midpoint keys
-// (Coord3D.Mid, the sort key of sortBounders).
+// (Coord3D.Mid, the sort key of sortBounders).  Boxes are kept as
+// order-preserving keys (okey): the reductions and comparisons of the
+// splits then run on the integer pipes instead of the float64 pipe (1/60 of
+// the float32 rate on this part); min and max commute with okey, and the
+// areas decode them (-0 and +0 share a key: only the sign of a zero
+// difference changes, which no comparison sees).
 __global__ void k_gt_boxes(const double* __restrict__ verts, const int32_t* __restrict__ tris, long long T,
-                           double* __restrict__ box, unsigned long long* __restrict__ keys, int32_t* __restrict__ vals) {
+                           unsigned long long* __restrict__ box, unsigned long long* __restrict__ keys,
+                           int32_t* __restrict__ vals) {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < T; t += (long long)gridDim.x * blockDim.x) {
         double p[3][3];
 #pragma unroll
@@ -149,8 +155,8 @@ __global__ void k_gt_boxes(const double* __restrict__ verts, const int32_t* __re
             mn = p[2][c] < mn ? p[2][c] : mn;
             double mx = p[1][c] > p[0][c] ? p[1][c] : p[0][c];
             mx = p[2][c] > mx ? p[2][c] : mx;
-            box[6 * t + c] = mn;
-            box[6 * t + 3 + c] = mx;
+            box[6 * t + c] = okey(mn);
+            box[6 * t + 3 + c] = okey(mx);
             keys[c * T + t] = okey(G_MUL(G_ADD(mn, mx), 0.5));
             vals[c * T + t] = (int32_t)t;
         }
@@ -364,10 +370,11 @@ __global__ void k_gt_acc_init(unsigned long long* __restrict__ acc, long long n)
         acc[i] = (i % 6) < 3 ? ~0ull : 0ull;
 }
 
-// A triangle's box (min x y z, max x y z) in three 16-byte loads.
-__device__ __forceinline__ void load_box(const double* __restrict__ box, int32_t t, double b[6]) {
-    const double2* q = reinterpret_cast<const double2*>(box + 6 * (size_t)t);
-    const double2 u = q[0], v = q[1], w = q[2];
+// A triangle's box (min x y z, max x y z, as okeys) in three 16-byte loads.
+__device__ __forceinline__ void load_box(const unsigned long long* __restrict__ box, int32_t t,
+                                         unsigned long long b[6]) {
+    const ulonglong2* q = reinterpret_cast<const ulonglong2*>(box + 6 * (size_t)t);
+    const ulonglong2 u = q[0], v = q[1], w = q[2];
     b[0] = u.x;
     b[1] = u.y;
     b[2] = v.x;
@@ -376,26 +383,32 @@ __device__ __forceinline__ void load_box(const double* __restrict__ box, int32_t
     b[5] = w.y;
 }
 
-__device__ __forceinline__ void box_empty(double b[6]) {
+__device__ __forceinline__ void box_empty(unsigned long long b[6]) {
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        b[c] = g_inf();
-        b[3 + c] = -g_inf();
+        b[c] = ~0ull;
+        b[3 + c] = 0ull;
     }
 }
 
-__device__ __forceinline__ void box_widen(double b[6], const double q[6]) {
+__device__ __forceinline__ void box_widen(unsigned long long b[6], const unsigned long long q[6]) {
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        if (q[c] < b[c]) b[c] = q[c];
-        if (q[3 + c] > b[3 + c]) b[3 + c] = q[3 + c];
+        b[c] = min(b[c], q[c]);
+        b[3 + c] = max(b[3 + c], q[3 + c]);
     }
+}
+
+// boundsArea of a box of okeys.
+__device__ __forceinline__ double key_area(const unsigned long long b[6]) {
+    return bounds_area(odec(b[0]), odec(b[1]), odec(b[2]), odec(b[3]), odec(b[4]), odec(b[5]));
 }
 
 // multipleBoundsArea's boxes (bvh.go:257-287) of every node half, one axis'
 // order per blockIdx.y.  A thread reduces 16 consecutive positions and
 // flushes each half it met into the tile's shared slots.
-__global__ void __launch_bounds__(kThreads) k_gt_reduce(const int32_t* __restrict__ ord, const double* __restrict__ box,
+__global__ void __launch_bounds__(kThreads) k_gt_reduce(const int32_t* __restrict__ ord,
+                                                        const unsigned long long* __restrict__ box,
                                                         long long T, int L, unsigned long long* __restrict__ acc,
                                                         int* __restrict__ err) {
     const int a = blockIdx.y;
@@ -414,7 +427,7 @@ __global__ void __launch_bounds__(kThreads) k_gt_reduce(const int32_t* __restric
     long long p = p0 + (long long)threadIdx.x * kPerThread;
     const long long pe = min(p + kPerThread, T);
     long long seg_end = -1, key = 0;
-    double bx[6];
+    unsigned long long bx[6];
     bool have = false;
     auto flush = [&]() {
         const long long sl = key - key0;
@@ -424,8 +437,8 @@ __global__ void __launch_bounds__(kThreads) k_gt_reduce(const int32_t* __restric
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            atomicMin(&s[sl * 6 + c], okey(bx[c]));
-            atomicMax(&s[sl * 6 + 3 + c], okey(bx[3 + c]));
+            atomicMin(&s[sl * 6 + c], bx[c]);
+            atomicMax(&s[sl * 6 + 3 + c], bx[3 + c]);
         }
     };
     for (; p < pe; p++) {
@@ -440,7 +453,7 @@ __global__ void __launch_bounds__(kThreads) k_gt_reduce(const int32_t* __restric
             box_empty(bx);
             have = true;
         }
-        double b[6];
+        unsigned long long b[6];
         load_box(box, o[p], b);
         box_widen(bx, b);
     }
@@ -464,8 +477,7 @@ __global__ void k_gt_axis(const unsigned long long* __restrict__ acc, long long 
         double best = 0;
         for (int a = 0; a < 3; a++) {
             const unsigned long long* q = acc + acc_at(2 * k, a);
-            const double v = G_ADD(bounds_area(odec(q[0]), odec(q[1]), odec(q[2]), odec(q[3]), odec(q[4]), odec(q[5])),
-                                   bounds_area(odec(q[6]), odec(q[7]), odec(q[8]), odec(q[9]), odec(q[10]), odec(q[11])));
+            const double v = G_ADD(key_area(q), key_area(q + 6));
             if (a == 0 || v < best) {
                 best = v;
                 ax = a;
@@ -561,14 +573,13 @@ __global__ void __launch_bounds__(kThreads) k_gt_pscatter(const int32_t* __restr
 
 // ---------------------------------------------------------------- warp depths
 
-__device__ __forceinline__ void box_warp_reduce(double b[6]) {
+__device__ __forceinline__ void box_warp_reduce(unsigned long long b[6]) {
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            const double lo = __shfl_xor_sync(0xffffffffu, b[c], o), hi = __shfl_xor_sync(0xffffffffu, b[3 + c], o);
-            if (lo < b[c]) b[c] = lo;
-            if (hi > b[3 + c]) b[3 + c] = hi;
+            b[c] = min(b[c], __shfl_xor_sync(0xffffffffu, b[c], o));
+            b[3 + c] = max(b[3 + c], __shfl_xor_sync(0xffffffffu, b[3 + c], o));
         }
     }
 }
@@ -577,8 +588,8 @@ __device__ __forceinline__ void box_warp_reduce(double b[6]) {
 // stable partition of all three orders (ballot ranks) into oout.  Lanes take
 // four positions a round, loads first, for memory-level parallelism.
 __global__ void __launch_bounds__(kThreads) k_gt_warp(const int32_t* __restrict__ oin, int32_t* __restrict__ oout,
-                                                      const double* __restrict__ box, uint8_t* __restrict__ lower,
-                                                      long long T, int L, long long NL) {
+                                                      const unsigned long long* __restrict__ box,
+                                                      uint8_t* __restrict__ lower, long long T, int L, long long NL) {
     constexpr int U = 4;
     const int lane = threadIdx.x & 31;
     const long long k = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -590,14 +601,14 @@ __global__ void __launch_bounds__(kThreads) k_gt_warp(const int32_t* __restrict_
     double best = 0;
     for (int a = 0; a < 3; a++) {
         const int32_t* o = oin + (size_t)a * T + lo;
-        double b0[6], b1[6];
+        unsigned long long b0[6], b1[6];
         box_empty(b0);
         box_empty(b1);
         for (int i0 = lane; i0 < m; i0 += 32 * U) {
             int32_t t[U];
 #pragma unroll
             for (int u = 0; u < U; u++) t[u] = i0 + 32 * u < m ? o[i0 + 32 * u] : -1;
-            double q[U][6];
+            unsigned long long q[U][6];
 #pragma unroll
             for (int u = 0; u < U; u++)
                 if (t[u] >= 0) load_box(box, t[u], q[u]);
@@ -610,8 +621,7 @@ __global__ void __launch_bounds__(kThreads) k_gt_warp(const int32_t* __restrict_
         }
         box_warp_reduce(b0);
         box_warp_reduce(b1);
-        const double v = G_ADD(bounds_area(b0[0], b0[1], b0[2], b0[3], b0[4], b0[5]),
-                               bounds_area(b1[0], b1[1], b1[2], b1[3], b1[4], b1[5]));
+        const double v = G_ADD(key_area(b0), key_area(b1));
         if (a == 0 || v < best) {
             best = v;
             ax = a;
@@ -648,15 +658,15 @@ __global__ void __launch_bounds__(kThreads) k_gt_warp(const int32_t* __restrict_
 constexpr int kFinishThreads = 128;
 
 // multipleBoundsArea (bvh.go:257-287) of n local items.
-__device__ double local_area(const double* __restrict__ box, const int32_t* id, const uint8_t* s, int n) {
-    double b[6];
+__device__ double local_area(const unsigned long long* __restrict__ box, const int32_t* id, const uint8_t* s, int n) {
+    unsigned long long b[6];
     load_box(box, id[s[0]], b);
     for (int i = 1; i < n; i++) {
-        double q[6];
+        unsigned long long q[6];
         load_box(box, id[s[i]], q);
         box_widen(b, q);
     }
-    return bounds_area(b[0], b[1], b[2], b[3], b[4], b[5]);
+    return key_area(b);
 }
 
 // One thread per node of at most 32 triangles: the rest of groupBounders
@@ -664,7 +674,8 @@ __device__ double local_area(const double* __restrict__ box, const int32_t* id, 
 // (Boxes staged in shared memory measured slower: 48 KB per 32 threads
 // leaves four warps an SM.)
 __global__ void __launch_bounds__(kFinishThreads) k_gt_finish(const int32_t* __restrict__ oin,
-                                                              const double* __restrict__ box, int32_t* __restrict__ loc,
+                                                              const unsigned long long* __restrict__ box,
+                                                              int32_t* __restrict__ loc,
                                                               long long T, int L, long long NL,
                                                               int32_t* __restrict__ order, int* __restrict__ err) {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -789,7 +800,7 @@ cudaError_t group_triangles_device(GroupScratch* g, const double* verts, const i
     const int grid_t = (int)std::min<long long>((T + kThreads - 1) / kThreads, (long long)sm_count * 16);
 
     // Boxes, midpoint keys and the three stable sorts.
-    k_gt_boxes<<<grid_t, kThreads, 0, st>>>(verts, tris, T, g->box.as<double>(), g->keys[0].as<unsigned long long>(),
+    k_gt_boxes<<<grid_t, kThreads, 0, st>>>(verts, tris, T, g->box.as<unsigned long long>(), g->keys[0].as<unsigned long long>(),
                                             g->vals[0].as<int32_t>());
     GK(cudaGetLastError());
     GK(cudaMemsetAsync(g->hist.p, 0, 3 * 2048 * 4, st));
@@ -857,7 +868,7 @@ cudaError_t group_triangles_device(GroupScratch* g, const double* verts, const i
         const long long nmax = (T + NL - 1) / NL;
         if (nmax <= kThreadMax) {
             k_gt_finish<<<(unsigned)((NL + kFinishThreads - 1) / kFinishThreads), kFinishThreads, 0, st>>>(
-                oin, g->box.as<double>(), g->loc.as<int32_t>(), T, L, NL, order, err);
+                oin, g->box.as<unsigned long long>(), g->loc.as<int32_t>(), T, L, NL, order, err);
             GK(cudaGetLastError());
             break;
         }
@@ -867,7 +878,7 @@ cudaError_t group_triangles_device(GroupScratch* g, const double* verts, const i
             unsigned long long* acc = g->acc.as<unsigned long long>();
             const int ga = (int)std::min<long long>((NL * 36 + 255) / 256, (long long)sm_count * 16);
             k_gt_acc_init<<<ga, 256, 0, st>>>(acc, NL * 36);
-            k_gt_reduce<<<dim3((unsigned)nb, 3), kThreads, 0, st>>>(oin, g->box.as<double>(), T, L, acc, err);
+            k_gt_reduce<<<dim3((unsigned)nb, 3), kThreads, 0, st>>>(oin, g->box.as<unsigned long long>(), T, L, acc, err);
             k_gt_axis<<<(unsigned)((NL + 255) / 256), 256, 0, st>>>(acc, NL, g->axis.as<uint8_t>());
             k_gt_flag<<<grid_t, kThreads, 0, st>>>(oin, T, L, g->axis.as<uint8_t>(), g->lower.as<uint8_t>());
             k_gt_pcount<<<dim3((unsigned)nb, 3), kThreads, 0, st>>>(oin, g->lower.as<uint8_t>(), T, nb,
@@ -879,7 +890,7 @@ cudaError_t group_triangles_device(GroupScratch* g, const double* verts, const i
             GK(cudaGetLastError());
         } else {
             k_gt_warp<<<(unsigned)((NL * 32 + kThreads - 1) / kThreads), kThreads, 0, st>>>(
-                oin, oout, g->box.as<double>(), g->lower.as<uint8_t>(), T, L, NL);
+                oin, oout, g->box.as<unsigned long long>(), g->lower.as<uint8_t>(), T, L, NL);
             GK(cudaGetLastError());
         }
         std::swap(oin, oout);

@@ -586,9 +586,14 @@ __device__ __noinline__ uint32_t metaball_rows(const ProgView& P, int id, const 
 
 template <int PREC>
 __device__ __forceinline__ uint32_t leaf_rows(const ProgView& P, int id, const RowCtx& rc, Counts& cnt, int* err) {
+    // As in eval_leaf: the float constants load with the kind (headline
+    // classification 0.406 -> 0.376 ms).
+    const float4* f4 = reinterpret_cast<const float4*>(P.leaf_f + (size_t)id * LEAF_F);
+    const float4 a0 = __ldg(f4), a1 = __ldg(f4 + 1), a2 = __ldg(f4 + 2), a3 = __ldg(f4 + 3);
     const int kind = P.leaf_kind[id];
     const double* d = P.leaf_d + (size_t)id * LEAF_D;
-    const float* f = P.leaf_f + (size_t)id * LEAF_F;
+    const float f[16] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w,
+                         a2.x, a2.y, a2.z, a2.w, a3.x, a3.y, a3.z, a3.w};
     cnt.leaf += rc.nrows;
     cnt.flops += rc.nrows * leaf_flops(kind);
     constexpr bool f32 = mode_f32(PREC);
