@@ -114,13 +114,23 @@ __device__ __noinline__ bool collider_point(const ProgView& P, const double* d, 
     auto test = [&](int i) {
         cnt.tris++;
         int h = 2;
+        const int par = P.tri_parent[i];
         if (filt) {
-            h = ray_tri_32(P.tris_f[i], pf);
+            // The whole record in seven 8-byte loads issued together, before
+            // the validity test and the early exits that read it field by
+            // field (1M-triangle collider 4.02 -> 3.94 ms).
+            static_assert(sizeof(TriF) == 56, "TriF is seven 8-byte words");
+            const float2* src = reinterpret_cast<const float2*>(P.tris_f + i);
+            float2 w[7];
+#pragma unroll
+            for (int k = 0; k < 7; k++) w[k] = __ldg(src + k);
+            TriF tf;
+            memcpy(&tf, w, sizeof(TriF));
+            h = ray_tri_32(tf, pf);
             if (h == 2) cnt.esc++;
         }
         if (h == 2) h = ray_tri_64(P.tris[i], p);
         if (!h) return;
-        const int par = P.tri_parent[i];
         if (par < 0) {
             hits++;
             return;
@@ -1846,7 +1856,7 @@ struct BatchArgs {
 };
 
 template <int PREC>
-__global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify_batch(BatchArgs b) {
+__device__ __forceinline__ void classify_batch_items(const BatchArgs& b) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t* base = (uint32_t*)smem + (size_t)warp * b.fold_words;
@@ -1866,6 +1876,11 @@ __global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify_batch(
     }
     flush_counts(cnt, b.stats, ST_FLOPS_CLASSIFY);
     if (lane == 0 && nconst) atomicAdd(&b.stats[ST_TILES_CONST], nconst);
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(256, MC_CLASSIFY_MIN_BLOCKS) k_classify_batch(BatchArgs b) {
+    classify_batch_items<PREC>(b);
 }
 
 __global__ void __launch_bounds__(256) k_count_batch(BatchArgs b, uint32_t* packed, uint32_t* blocksum) {
