@@ -230,17 +230,26 @@ __device__ __noinline__ bool leaf64_point(const ProgView& P, int id, P3 p, Count
     }
 }
 
+// The leaf tables a predicate reads first (kinds and float constants),
+// passed by value: kernel parameters in the single-solid kernels, registers
+// loaded once per job in the batch search (instead of a load of the pointer
+// from the job array ahead of every leaf's constants).
+struct LeafTabs {
+    const int32_t* kind;
+    const float* f;
+};
+
 template <int PREC>
-__device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf, Counts& cnt, int* err) {
+__device__ __forceinline__ bool eval_leaf(const ProgView& P, LeafTabs T, int id, P3 p, F3 pf, Counts& cnt, int* err) {
     cnt.leaf++;
-    cnt.flops += leaf_flops(P.leaf_kind[id]);
+    cnt.flops += leaf_flops(T.kind[id]);
     if (mode_f32(PREC)) {
         // The leaf's 16 float constants in four 16-byte loads issued with
         // the kind's, before the branch on the kind: one load latency a
         // leaf instead of two (headline search 0.518 -> 0.493 ms).
-        const float4* f4 = reinterpret_cast<const float4*>(P.leaf_f + (size_t)id * LEAF_F);
+        const float4* f4 = reinterpret_cast<const float4*>(T.f + (size_t)id * LEAF_F);
         const float4 a0 = __ldg(f4), a1 = __ldg(f4 + 1), a2 = __ldg(f4 + 2), a3 = __ldg(f4 + 3);
-        const int kind = P.leaf_kind[id];
+        const int kind = T.kind[id];
         if (kind <= LK_TORUS) {
             const float f[16] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w,
                                  a2.x, a2.y, a2.z, a2.w, a3.x, a3.y, a3.z, a3.w};
@@ -263,7 +272,8 @@ __device__ __forceinline__ bool eval_leaf(const ProgView& P, int id, P3 p, F3 pf
 
 // Evaluate a (possibly folded) postfix program at p.  Bit stack: top = bit 0.
 template <int PREC>
-__device__ bool eval_program(const ProgView& P, const uint32_t* q, int nq, P3 p, F3 pf, Counts& cnt, int* err) {
+__device__ bool eval_program(const ProgView& P, LeafTabs T, const uint32_t* q, int nq, P3 p, F3 pf, Counts& cnt,
+                             int* err) {
     uint32_t st = 0;
     P3 saved[MAX_XDEPTH];
     int sp = 0;
@@ -290,7 +300,7 @@ __device__ bool eval_program(const ProgView& P, const uint32_t* q, int nq, P3 p,
                 const bool isor = code != OP_ALEAVES;
                 bool v = !isor;
                 for (uint32_t k = 0; k < count; k++)
-                    if (eval_leaf<PREC>(P, list ? list[k] : first + k, p, pf, cnt, err) == isor) {
+                    if (eval_leaf<PREC>(P, T, list ? list[k] : first + k, p, pf, cnt, err) == isor) {
                         v = isor;
                         break;
                     }
@@ -336,6 +346,12 @@ __device__ bool eval_program(const ProgView& P, const uint32_t* q, int nq, P3 p,
         }
     }
     return st & 1u;
+}
+
+template <int PREC>
+__device__ __forceinline__ bool eval_program(const ProgView& P, const uint32_t* q, int nq, P3 p, F3 pf, Counts& cnt,
+                                             int* err) {
+    return eval_program<PREC>(P, LeafTabs{P.leaf_kind, P.leaf_f}, q, nq, p, pf, cnt, err);
 }
 
 
@@ -1597,8 +1613,9 @@ __device__ __forceinline__ int vertex_setup(const GridView& g, const uint32_t* b
 // mcSearchPoint (mc.go:223-258) against a (folded) program; only the axis
 // coordinate moves, so the float point is updated in place.
 template <int PREC>
-__device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, int len, P3 cpt, int axis, double lo,
-                                     double hi, int iters, int hi_bit, Counts& cnt, int* err, double* true_point) {
+__device__ __forceinline__ P3 bisect(const ProgView& P, LeafTabs T, const uint32_t* prog, int len, P3 cpt, int axis,
+                                     double lo, double hi, int iters, int hi_bit, Counts& cnt, int* err,
+                                     double* true_point) {
     F3 pf = to_f3(cpt);
     auto contains_f = [&](P3 pt, float vf) -> bool {
         if (len == FOLD_FALSE) return false;
@@ -1606,7 +1623,7 @@ __device__ __forceinline__ P3 bisect(const ProgView& P, const uint32_t* prog, in
         if (axis == 0) pf.x = vf;
         else if (axis == 1) pf.y = vf;
         else pf.z = vf;
-        return eval_program<PREC>(P, prog, len, pt, pf, cnt, err);
+        return eval_program<PREC>(P, T, prog, len, pt, pf, cnt, err);
     };
     double fp = lo, tp = hi;
     P3 t = cpt;
@@ -1729,7 +1746,9 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search(GridView g
         if (a.cull && __any_sync(0xffffffffu, work)) search_cull(P, work, cpt, axis, lo, hi, q, cur, prev, have_prev, prog, len);
         if (live && status == 0) {
             double tpt = 0;
-            const P3 out = work ? bisect<PREC>(P, prog, len, cpt, axis, lo, hi, a.iters, hi_bit, cnt, a.err, &tpt) : cpt;
+            const P3 out = work ? bisect<PREC>(P, LeafTabs{P.leaf_kind, P.leaf_f}, prog, len, cpt, axis, lo, hi, a.iters,
+                                               hi_bit, cnt, a.err, &tpt)
+                                : cpt;
             a.verts[3 * v] = out.x;
             a.verts[3 * v + 1] = out.y;
             a.verts[3 * v + 2] = out.z;
@@ -1983,6 +2002,7 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(Batc
     int prev_job = -1;
     const uint32_t* prog = nullptr;
     int len = 0;
+    LeafTabs job_tabs{nullptr, nullptr};
     int cj = 0;  // this lane's job and its vertex range (vertices only grow along the run)
     long long cj_lo = 0, cj_hi = -1;
     for (long long bt = b_begin; bt < b_end; bt++) {
@@ -2014,6 +2034,7 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(Batc
         const ProgView* Pp = &Jp->P;
         const uint32_t* pr = Jp->P.ops;
         int ln = Jp->P.n_ops;
+        LeafTabs tabs{Jp->P.leaf_kind, Jp->P.leaf_f};
         if (uniform) {
             const ProgView& P = b.jobs[j0].P;
             if (j0 != prev_job) {
@@ -2021,7 +2042,9 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(Batc
                 prev_job = j0;
                 prog = P.ops;
                 len = P.n_ops;
+                job_tabs = LeafTabs{P.leaf_kind, P.leaf_f};
             }
+            tabs = job_tabs;
             const int nw = (P.n_leaves + 31) >> 5;
             uint32_t* cur = q + P.fold_cap;
             if (b.cull && __any_sync(0xffffffffu, work))
@@ -2033,7 +2056,8 @@ __global__ void __launch_bounds__(128, MC_SEARCH_MIN_BLOCKS) k_search_batch(Batc
             prev_job = -1;
         }
         if (live && status == 0) {
-            const P3 out = work ? bisect<PREC>(*Pp, pr, ln, cpt, axis, lo, hi, Jp->iters, hi_bit, cnt, Jp->ca.err, &tpt)
+            const P3 out = work ? bisect<PREC>(*Pp, tabs, pr, ln, cpt, axis, lo, hi, Jp->iters, hi_bit, cnt, Jp->ca.err,
+                                               &tpt)
                                 : cpt;
             verts[3 * v] = out.x;
             verts[3 * v + 1] = out.y;
