@@ -634,7 +634,7 @@ def collider_batch_line(ctx, count, torch):
 # summarised in profiles/launches_csg48_delta0.004.md (same kernels as this
 # source).  Below the algorithmic bytes where a kernel reads what the previous
 # one left in the 129 MB L2 (keys, corner bits) or its writes stay in L2.
-NCU_TRAFFIC = {"k_count": 29755648, "k_emit": 50160128, "k_search": 45513216}
+NCU_TRAFFIC = {"k_count": 29754624, "k_emit": 50758656, "k_search": 45146880}
 
 
 def algorithmic_bytes(kernel, st):

@@ -2217,9 +2217,9 @@ struct mc_ctx {
     std::vector<mc_solid*> solids;  // live solids; mc_destroy detaches them
     int64_t last_V = 0, last_T = 0;
     int sm_count = 152;
-    // Size hints of the last search (vertices, non-empty chunks) and the
-    // buffer capacities a launch that ran ahead was checked against.
-    long long hint_v = 0, hint_ne = 0;
+    // Vertex count of the last search (0 before the first), and the buffer
+    // capacities a launch that ran ahead was checked against.
+    long long hint_v = 0;
     bool ran_ahead = false;
     long long ahead_cap_v = 0, ahead_cap_t = 0;
 };
@@ -2594,8 +2594,8 @@ namespace {
 // Everything up to the search kernel and the read-back of stats and error
 // words is enqueued; the host has waited only for the mesh totals, which
 // are in st->vertices / st->triangles.  search_finish waits for the rest.
-// ahead: when earlier calls left the vertex and triangle buffers and the
-// size hints, emit and search are launched without waiting for the totals
+// ahead: when earlier calls left the vertex and triangle buffers, emit and
+// search are launched without waiting for the totals
 // (they read the counts from device memory and write nothing if the mesh
 // does not fit); search_finish then asks for a redo that waits.
 mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters, const mc_opts* opts_in,
@@ -2767,15 +2767,15 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
         CK(ctx->keys.ensure(std::max<long long>(V, 1) * 8));
         CK(ctx->verts.ensure(std::max<long long>(V, 1) * 24));
         CK(ctx->tris.ensure(std::max<long long>(T, 1) * 12));
-        ctx->hint_ne = (long long)hp[4];
     }
     CK(cudaEventRecord(ctx->ev[2], sm));
     if (nchunks > 0 && (go || V > 0 || T > 0)) {
         EmitArgs ea{ctx->bits.as<uint32_t>(), ctx->packed.as<uint32_t>(), ctx->prefv.as<uint32_t>(),
                     ctx->preft.as<uint32_t>(), ctx->keys.as<unsigned long long>(), ctx->tris.as<int32_t>(), nchunks};
-        // Without the count, one thread per non-empty chunk of the last call
-        // (grid-stride over the rest).
-        const long long n_ne = go ? std::max<long long>(ctx->hint_ne, 1) : std::min<long long>((long long)hp[4], nchunks);
+        // Without the count the grid covers every chunk (the list's bound;
+        // threads past its end return at once): the last call's count could
+        // be far smaller than this one's.
+        const long long n_ne = go ? nchunks : std::min<long long>((long long)hp[4], nchunks);
         if (n_ne > 0)
             k_emit_list<<<(int)std::min<long long>((n_ne + 255) / 256, (long long)ctx->sm_count * 64), 256, 0, sm>>>(
                 g, ea, ctx->nonempty.as<uint32_t>(), go ? nchunks : n_ne,
@@ -2808,10 +2808,11 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
         if (smem_s > 48 * 1024)
             CK(cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s));
         if (go) {
-            // Sized by the last call's vertex count; any grid is correct.
+            // Sized by the buffers' capacity, a bound of this call's vertex
+            // count (warps past the count return at once); any grid is correct.
             ctx->n_chunks = 1;
             ctx->chunk_end[0] = 0;
-            ks<<<search_blocks(ctx->hint_v, ctx->sm_count), 128, smem_s, sm>>>(g, P, sa);
+            ks<<<search_blocks(cap_v, ctx->sm_count), 128, smem_s, sm>>>(g, P, sa);
             CK(cudaGetLastError());
         } else {
             // Vertex ranges (multiples of 32) searched by consecutive launches,
@@ -2863,7 +2864,6 @@ mc_status search_finish(mc_ctx* ctx, mc_stats* stats, bool* redo = nullptr) {
         const long long V = (long long)hp[0], T = (long long)hp[1];
         if (V >= ((long long)1 << 31) || T >= ((long long)1 << 31))
             return fail(ctx, MC_ERR_LIMIT, "mesh exceeds 2^31 vertices or triangles");
-        ctx->hint_ne = (long long)hp[4];
         if (V > ctx->ahead_cap_v || T > ctx->ahead_cap_t) {
             ctx->hint_v = V;
             if (redo) *redo = true;
