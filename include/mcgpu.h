@@ -269,7 +269,10 @@ void mc_mesh_free(mc_mesh* mesh);
 
 /* Same as mc_search, but the mesh stays in device memory owned by the
  * context (valid until the next call on it); *n_vertices / *n_triangles and
- * *stats (may be NULL) are filled. */
+ * *stats (may be NULL) are filled.  Once an earlier call on the context has
+ * sized its mesh buffers, the call does not wait mid-way for the mesh's size:
+ * if the mesh outgrew the buffers, the call runs again with waiting (same
+ * result); stats then describe the second run. */
 mc_status mc_search_device(mc_ctx* ctx, const mc_solid* solid, double delta, int32_t iters,
                            const mc_opts* opts, int64_t* n_vertices, int64_t* n_triangles,
                            mc_stats* stats);

@@ -2170,6 +2170,7 @@ struct BatchPlan {
     long long nitems = 0, nchunks = 0;
     int nblk = 0, fold_words = 0, grid_c = 1, grid_s = 1, grid_e = 1, prec = 1;
     bool has_metaball = false;
+    bool all_csg = true;  // no job has colliders or metaballs
     bool use_list = false;  // emit over the list of non-empty chunks
     size_t smem_c = 0, smem_s = 0;
     long long cap_V = -1, cap_T = -1;
@@ -3460,6 +3461,7 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
             fold_words = std::max(fold_words, (J.P.fold_cap + 2 * nw + 3) & ~3);
             lay.push_back(L);
             pl->has_metaball = pl->has_metaball || J.P.has_metaball;
+            pl->all_csg = pl->all_csg && jobs[i].solid->host.trees.empty() && jobs[i].solid->host.metas.empty();
             pl->hjobs.push_back(J);
         }
         const int nd = (int)pl->hjobs.size();
@@ -3626,7 +3628,12 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         CK(pl->keys.ensure(std::max<long long>(V, 1) * 8));
         CK(pl->verts.ensure(std::max<long long>(V, 1) * 24));
         CK(pl->tris.ensure(std::max<long long>(T, 1) * 12));
-        pl->grid_s = std::max(ctx->sm_count * 16, search_blocks(V, ctx->sm_count));
+        // Four 32-vertex batches per warp for CSG-only batches (fewer refolds of
+        // the warp's program: 20.9 -> 20.5 ms for 512 CSG jobs), two where a
+        // job has colliders or metaballs, whose vertices want the resident
+        // warps (16 colliders: 20.6 ms at two, 22.8 ms at four).
+        pl->grid_s = pl->all_csg ? (int)std::max<long long>(ctx->sm_count * 16, (V + 511) / 512)
+                                 : std::max(ctx->sm_count * 16, search_blocks(V, ctx->sm_count));
         pl->grid_e = (int)std::max<long long>(1, std::min<long long>(((long long)htot[2] + 255) / 256, 1LL << 30));
         CK(back());
         CK(cudaEventRecord(ctx->ev[4], sm));
