@@ -607,24 +607,24 @@ def serialize(solid: Solid):
         elif isinstance(s, JoinedSolid):
             node(JOIN, s, n_children=len(s.solids))
             for c in s.solids:
-                emit(c)
+                fast(c)
         elif isinstance(s, IntersectedSolid):
             node(INTERSECT, s, n_children=len(s.solids))
             for c in s.solids:
-                emit(c)
+                fast(c)
         elif isinstance(s, SubtractedSolid):
             node(SUBTRACT, s, n_children=2)
-            emit(s.Positive)
-            emit(s.Negative)
+            fast(s.Positive)
+            fast(s.Negative)
         elif isinstance(s, _TransformedSolid):
             steps = s.transform._steps()
             node(TRANSFORM, s, n_children=1, n_steps=len(steps))
             for kind, p in steps:
                 node(kind, None, p=p)
-            emit(s.solid)
+            fast(s.solid)
         elif isinstance(s, _CheckedSolid):
             node(CHECKED, s, n_children=1)
-            emit(s.solid)
+            fast(s.solid)
         elif isinstance(s, MetaballSolidT):
             f = s.falloff
             if f.kind == 0 or (f.kind == FALLOFF_POWER and
@@ -636,9 +636,73 @@ def serialize(solid: Solid):
                 node(BALL, None, n_children=1, n_steps=len(steps), p=[w])
                 for kind, p in steps:
                     node(kind, None, p=p)
-                emit(prim)
+                fast(prim)
         else:
             raise NotLowerable(f"{type(s).__name__} has no device lowering")
 
-    emit(solid)
+    pack = _NODE_PACK.pack
+    z = 0.0
+
+    # Exact-type fast paths for the common nodes (a subclass takes the
+    # isinstance chain above): the same records, packed without the
+    # intermediate lists.  Bounds are serialised for the root only.
+    def fast_sphere(s):
+        if not recs:
+            return emit(s)
+        c = s.Center
+        recs.append(pack(SPHERE, 0, 0, 0, z, z, z, z, z, z, c.X, c.Y, c.Z, s.Radius, z, z, z, z, z, z, z, z))
+
+    def fast_rect(s):
+        if not recs:
+            return emit(s)
+        a, b = s.MinVal, s.MaxVal
+        recs.append(pack(RECT, 0, 0, 0, z, z, z, z, z, z, a.X, a.Y, a.Z, b.X, b.Y, b.Z, z, z, z, z, z, z))
+
+    def fast_segment(kind):
+        def f(s):
+            if not recs:
+                return emit(s)
+            a, b = s.P1, s.P2
+            recs.append(pack(kind, 0, 0, 0, z, z, z, z, z, z, a.X, a.Y, a.Z, b.X, b.Y, b.Z, s.Radius,
+                             z, z, z, z, z))
+        return f
+
+    def fast_join(kind):
+        def f(s):
+            if not recs:
+                return emit_node_children(kind, s)
+            recs.append(pack(kind, len(s.solids), 0, 0, z, z, z, z, z, z, *_ZEROS))
+            for c in s.solids:
+                fast(c)
+        return f
+
+    def fast_subtract(s):
+        if not recs:
+            return emit_node_children(SUBTRACT, s)
+        recs.append(pack(SUBTRACT, 2, 0, 0, z, z, z, z, z, z, *_ZEROS))
+        fast(s.Positive)
+        fast(s.Negative)
+
+    def emit_node_children(kind, s):
+        if kind == SUBTRACT:
+            node(SUBTRACT, s, n_children=2)
+            fast(s.Positive)
+            fast(s.Negative)
+        else:
+            node(kind, s, n_children=len(s.solids))
+            for c in s.solids:
+                fast(c)
+
+    handlers = {Sphere: fast_sphere, Rect: fast_rect, Cylinder: fast_segment(CYLINDER),
+                Capsule: fast_segment(CAPSULE), JoinedSolid: fast_join(JOIN),
+                IntersectedSolid: fast_join(INTERSECT), SubtractedSolid: fast_subtract}
+
+    def fast(s):
+        h = handlers.get(type(s))
+        if h is None:
+            emit(s)
+        else:
+            h(s)
+
+    fast(solid)
     return np.frombuffer(bytearray(b"".join(recs)), dtype=NODE_DTYPE), sets
