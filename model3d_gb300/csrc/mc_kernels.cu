@@ -2341,6 +2341,13 @@ int search_blocks(long long n, int sm_count) {
     return (int)std::max<long long>(1, std::max(two, one));
 }
 
+// Collider programs search one 32-vertex batch per warp: a vertex is a
+// chain of dependent ray queries, and more resident warps hide more of it
+// (1M-triangle collider search 2.178 -> 2.160 ms).
+int search_grid(const HostProgram& H, long long n, int sm_count) {
+    return H.has_collider ? (int)std::max<long long>(1, (n + 127) / 128) : search_blocks(n, sm_count);
+}
+
 size_t search_smem(const ProgView& P) {
     const size_t nw = ((size_t)P.n_leaves + 31) / 32;
     return 4 * 4 * ((size_t)P.fold_cap + 2 * nw);
@@ -2813,7 +2820,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
             // count (warps past the count return at once); any grid is correct.
             ctx->n_chunks = 1;
             ctx->chunk_end[0] = 0;
-            ks<<<search_blocks(cap_v, ctx->sm_count), 128, smem_s, sm>>>(g, P, sa);
+            ks<<<search_grid(H, cap_v, ctx->sm_count), 128, smem_s, sm>>>(g, P, sa);
             CK(cudaGetLastError());
         } else {
             // Vertex ranges (multiples of 32) searched by consecutive launches,
@@ -2829,7 +2836,7 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
                 if (sa.interior) sc.interior = sa.interior + 3 * v0;
                 sc.nverts = v1 - v0;
                 if (sc.nverts > 0) {
-                    ks<<<search_blocks(sc.nverts, ctx->sm_count), 128, smem_s, sm>>>(g, P, sc);
+                    ks<<<search_grid(H, sc.nverts, ctx->sm_count), 128, smem_s, sm>>>(g, P, sc);
                     CK(cudaGetLastError());
                 }
                 if (nch > 1) CK(cudaEventRecord(ctx->cev[c], sm));
@@ -3629,11 +3636,11 @@ mc_status mc_search_batch(mc_ctx* ctx, const mc_job* jobs, size_t n, const mc_op
         CK(pl->verts.ensure(std::max<long long>(V, 1) * 24));
         CK(pl->tris.ensure(std::max<long long>(T, 1) * 12));
         // Four 32-vertex batches per warp for CSG-only batches (fewer refolds of
-        // the warp's program: 20.9 -> 20.5 ms for 512 CSG jobs), two where a
+        // the warp's program: 20.9 -> 20.5 ms for 512 CSG jobs), one where a
         // job has colliders or metaballs, whose vertices want the resident
-        // warps (16 colliders: 20.6 ms at two, 22.8 ms at four).
+        // warps (16 colliders: 20.0 ms at one, 20.8 at two, 22.8 at four).
         pl->grid_s = pl->all_csg ? (int)std::max<long long>(ctx->sm_count * 16, (V + 511) / 512)
-                                 : std::max(ctx->sm_count * 16, search_blocks(V, ctx->sm_count));
+                                 : (int)std::max<long long>(ctx->sm_count * 16, (V + 127) / 128);
         pl->grid_e = (int)std::max<long long>(1, std::min<long long>(((long long)htot[2] + 255) / 256, 1LL << 30));
         CK(back());
         CK(cudaEventRecord(ctx->ev[4], sm));
