@@ -2341,11 +2341,12 @@ int search_blocks(long long n, int sm_count) {
     return (int)std::max<long long>(1, std::max(two, one));
 }
 
-// Collider programs search one 32-vertex batch per warp: a vertex is a
-// chain of dependent ray queries, and more resident warps hide more of it
-// (1M-triangle collider search 2.178 -> 2.160 ms).
+// Collider and metaball programs search one 32-vertex batch per warp: a
+// vertex is a chain of dependent ray queries or ball sums, and more resident
+// warps hide more of it (1M-triangle collider search 2.178 -> 2.160 ms,
+// 64-ball metaball 5.006 -> 4.947 ms).
 int search_grid(const HostProgram& H, long long n, int sm_count) {
-    return H.has_collider ? (int)std::max<long long>(1, (n + 127) / 128) : search_blocks(n, sm_count);
+    return H.has_collider || !H.metas.empty() ? (int)std::max<long long>(1, (n + 127) / 128) : search_blocks(n, sm_count);
 }
 
 size_t search_smem(const ProgView& P) {
