@@ -145,7 +145,7 @@ __global__ void k_gt_boxes(const double* __restrict__ verts, const int32_t* __re
         double p[3][3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const long long i = tris[3 * t + k];
+            const long long i = tris ? (long long)tris[3 * t + k] : 3 * t + k;  // null: a triangle soup
 #pragma unroll
             for (int c = 0; c < 3; c++) p[k][c] = verts[3 * i + c];
         }

@@ -13,7 +13,8 @@ GroupScratch* group_scratch_new();
 void group_scratch_free(GroupScratch* g);
 
 // The GroupTriangles permutation of T triangles (vertex-index triples into
-// verts, float64 x y z): order[i] = the triangle placed i-th.  Each midpoint
+// verts, float64 x y z; with tris null, triangle t is vertices 3t..3t+2):
+// order[i] = the triangle placed i-th.  Each midpoint
 // sort is stable, so ties keep the input order.  Runs on `stream`, waiting
 // for it to pick the sort passes and at the end; *internal_error is set when
 // a kernel's own consistency check failed (order is then not valid).

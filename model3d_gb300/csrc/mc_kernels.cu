@@ -26,6 +26,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -2448,6 +2449,61 @@ void mc_destroy(mc_ctx* ctx) {
     delete ctx;
 }
 
+// Triangle sets of at least kDeviceGroupMin ungrouped triangles are grouped
+// on the device (GroupTriangles, mc_group.cu) and copied in that order into
+// *grouped, which *out's entries point at (marked grouped); smaller sets and
+// grouped ones pass through.  *out stays empty when no set qualifies.
+constexpr int64_t kDeviceGroupMin = 1 << 15;
+
+mc_status pregroup_sets(mc_ctx* ctx, const mc_tri_set* sets, size_t n_sets, std::vector<mc_tri_set>* out,
+                        std::vector<std::vector<double>>* grouped) {
+    bool any = false;
+    for (size_t i = 0; i < n_sets; i++) any = any || (!sets[i].grouped && sets[i].n >= kDeviceGroupMin && sets[i].tris);
+    if (!any) return MC_OK;
+    CK(cudaSetDevice(ctx->device));
+    if (!ctx->group) ctx->group = group_scratch_new();
+    out->assign(sets, sets + n_sets);
+    grouped->resize(n_sets);
+    for (size_t i = 0; i < n_sets; i++) {
+        const mc_tri_set& ts = sets[i];
+        if (ts.grouped || ts.n < kDeviceGroupMin || !ts.tris) continue;
+        if (ts.n >= ((int64_t)1 << 31)) return fail(ctx, MC_ERR_LIMIT, "triangle set exceeds 2^31 triangles");
+        const size_t bytes = (size_t)ts.n * 72;
+        CK(ctx->mesh_v.ensure(bytes));
+        CK(ctx->gorder.ensure((size_t)ts.n * 4));
+        CK(cudaMemcpyAsync(ctx->mesh_v.p, ts.tris, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        bool bad = false;
+        CK(group_triangles_device(ctx->group, ctx->mesh_v.as<double>(), nullptr, ts.n, ctx->gorder.as<int32_t>(),
+                                  ctx->stream, ctx->sm_count, &bad));
+        if (bad) return fail(ctx, MC_ERR_CUDA, "GroupTriangles: a device consistency check failed");
+        std::vector<int32_t> order((size_t)ts.n);
+        CK(cudaMemcpyAsync(order.data(), ctx->gorder.p, (size_t)ts.n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        std::vector<double>& g = (*grouped)[i];
+        g.resize((size_t)ts.n * 9);
+        // The gather in grouped order, in up to 16 chunks on host threads.
+        const size_t n = (size_t)ts.n;
+        const size_t parts = n >= (1u << 18) ? std::max(1u, std::min(16u, std::thread::hardware_concurrency())) : 1;
+        auto copy = [&](size_t w) {
+            for (size_t k = n * w / parts; k < n * (w + 1) / parts; k++)
+                std::memcpy(&g[9 * k], ts.tris + 9 * (size_t)order[k], 72);
+        };
+        std::vector<std::thread> th;
+        for (size_t w = 1; w < parts; w++) {
+            try {
+                th.emplace_back(copy, w);
+            } catch (const std::system_error&) {
+                copy(w);  // no thread to be had: this one copies the part
+            }
+        }
+        copy(0);
+        for (auto& t : th) t.join();
+        (*out)[i].tris = g.data();
+        (*out)[i].grouped = 1;
+    }
+    return MC_OK;
+}
+
 mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, const mc_tri_set* sets,
                           size_t n_sets, mc_solid** out) {
     if (!ctx || !out) return MC_ERR_ARG;
@@ -2457,7 +2513,15 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
     s->serial = ++g_serial;
     s->ctx = ctx;
     try {
-        lower_scene(nodes, n_nodes, sets, n_sets, &s->host);
+        // MeshToCollider's GroupTriangles of large sets on the device; the
+        // lowering then takes them as grouped (GroupedTrianglesToCollider),
+        // which gives the same program (the order is the host grouping's:
+        // both sort stably by midpoint and split alike).
+        std::vector<mc_tri_set> gsets;
+        std::vector<std::vector<double>> grouped;
+        mc_status gs = pregroup_sets(ctx, sets, n_sets, &gsets, &grouped);
+        if (gs != MC_OK) return gs;
+        lower_scene(nodes, n_nodes, gsets.empty() ? sets : gsets.data(), n_sets, &s->host);
     } catch (const LowerError& e) {
         return fail(ctx, e.status, e.what());
     } catch (const std::exception& e) {
