@@ -10,6 +10,7 @@
 #include "mc_lower.h"
 
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <cfloat>
 #include <cmath>
@@ -282,41 +283,57 @@ std::vector<int> group_triangles(const std::vector<Tri>& t) {  // GroupTriangles
     return out;
 }
 
-// Tree under construction: JoinedCollider nodes with flattened child lists
-// (NewJoinedCollider, model3d/collisions.go:217-253).
-struct BNode {
-    D3 mn, mx;
-    std::vector<int> ch;  // >= 0 node, < 0: triangle (-c-1)
-};
-
-struct TreeBuilder {
+// GroupedTrianglesToCollider (collisions.go:169-181) over a grouped order:
+// the halving tree of the order, where NewJoinedCollider
+// (collisions.go:217-253) absorbs a child whose bounds equal its parent's
+// (its children take its place, in order).  Internal node k of the
+// recursion (post-order numbering, as the recursion creates them) has
+// children ch1[k], ch2[k] (>= 0 node, < 0 triangle -(t+1)) and bounds
+// mn[k], mx[k]; absorbed[k] marks a node whose bounds equal its parent's.
+// Flat arrays instead of a child vector per node; the bounds are computed
+// bottom up with the upper levels' halves on two threads.
+struct FlatTree {
     const std::vector<Tri>& tris;
-    std::vector<BNode> nodes;  // reserve n - 1 before build(): one node per pair merged
-    // Returns a child reference: node index, or -(tri+1).
-    int build(const int* order, size_t n) {  // GroupedTrianglesToCollider, collisions.go:169-181
-        if (n == 1) return -(order[0] + 1);
-        size_t mid = n / 2;
-        int c1 = build(order, mid);
-        int c2 = build(order + mid, n - mid);
-        BNode j;
-        j.mn = bounds_min(c1);
-        j.mx = bounds_max(c1);
-        j.mn = vmin3(j.mn, bounds_min(c2));
-        j.mx = vmax3(j.mx, bounds_max(c2));
-        for (int c : {c1, c2}) {
-            if (c >= 0 && veq(nodes[c].mn, j.mn) && veq(nodes[c].mx, j.mx)) {
-                // Absorbed: nothing refers to node c afterwards, so its list moves.
-                std::vector<int> cc = std::move(nodes[c].ch);
-                j.ch.insert(j.ch.end(), cc.begin(), cc.end());
-            } else {
-                j.ch.push_back(c);
+    const int* order;
+    std::vector<D3> mn, mx;
+    std::vector<int> ch1, ch2;
+    std::vector<uint8_t> absorbed;
+    static constexpr size_t kParallel = 1 << 15;
+
+    FlatTree(const std::vector<Tri>& t, const int* o, size_t n)
+        : tris(t), order(o), mn(n - 1), mx(n - 1), ch1(n - 1), ch2(n - 1), absorbed(n - 1, 0) {}
+
+    D3 bmin(int c) const { return c >= 0 ? mn[c] : tris[-c - 1].mn; }
+    D3 bmax(int c) const { return c >= 0 ? mx[c] : tris[-c - 1].mx; }
+
+    // The subtree of positions [lo, lo + n) whose internal nodes take the
+    // post-order numbers start .. start + n - 2; returns its reference.
+    int build(size_t lo, size_t n, int start, int spawn_depth) {
+        if (n == 1) return -(order[lo] + 1);
+        const size_t mid = n / 2;
+        int c1 = 0, c2 = 0;
+        std::thread right;
+        if (spawn_depth > 0 && n >= kParallel) {
+            try {
+                right = std::thread([&] { c2 = build(lo + mid, n - mid, start + (int)mid - 1, spawn_depth - 1); });
+            } catch (const std::system_error&) {
             }
         }
-        nodes.push_back(std::move(j));
-        return (int)nodes.size() - 1;
+        c1 = build(lo, mid, start, right.joinable() ? spawn_depth - 1 : 0);
+        if (right.joinable()) right.join();
+        else c2 = build(lo + mid, n - mid, start + (int)mid - 1, 0);
+        const int k = start + (int)n - 2;
+        D3 a = bmin(c1), b = bmax(c1);
+        a = vmin3(a, bmin(c2));
+        b = vmax3(b, bmax(c2));
+        mn[k] = a;
+        mx[k] = b;
+        ch1[k] = c1;
+        ch2[k] = c2;
+        for (int c : {c1, c2})
+            if (c >= 0 && veq(mn[c], a) && veq(mx[c], b)) absorbed[c] = 1;
+        return k;
     }
-    D3 bounds_min(int c) { return c >= 0 ? nodes[c].mn : tris[-c - 1].mn; }
-    D3 bounds_max(int c) { return c >= 0 ? nodes[c].mx : tris[-c - 1].mx; }
 };
 
 // f(lo, hi) over contiguous chunks of [0, n) on up to 16 host threads, at
@@ -343,6 +360,48 @@ void parallel_chunks(size_t n, size_t min_per_thread, F&& f) {
     }
     f((size_t)0, n / T);
     for (std::thread& x : th) x.join();
+}
+
+// Sort of distinct 64-bit keys: chunks sorted on host threads, then merged
+// pairwise, each round's merges on host threads.  The result is the sorted
+// sequence whatever the split.
+void parallel_sort_u64(std::vector<uint64_t>& v) {
+    const size_t n = v.size();
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    size_t parts = 1;
+    while (parts * 2 <= std::min<size_t>(hw, 16) && n / (parts * 2) >= 65536) parts *= 2;
+    if (parts == 1) {
+        std::sort(v.begin(), v.end());
+        return;
+    }
+    std::vector<size_t> cut(parts + 1);
+    for (size_t k = 0; k <= parts; k++) cut[k] = n * k / parts;
+    auto run = [&](size_t count, const std::function<void(size_t)>& f) {
+        std::vector<std::thread> th;
+        for (size_t k = 1; k < count; k++) {
+            try {
+                th.emplace_back(f, k);
+            } catch (const std::system_error&) {
+                f(k);
+            }
+        }
+        f(0);
+        for (auto& t : th) t.join();
+    };
+    run(parts, [&](size_t k) { std::sort(v.begin() + cut[k], v.begin() + cut[k + 1]); });
+    std::vector<uint64_t> tmp(n);
+    std::vector<uint64_t>* src = &v;
+    std::vector<uint64_t>* dst = &tmp;
+    for (size_t width = 1; width < parts; width *= 2) {
+        const size_t merges = (parts + 2 * width - 1) / (2 * width);
+        run(merges, [&](size_t m) {
+            const size_t a = cut[std::min(parts, 2 * width * m)], b = cut[std::min(parts, 2 * width * m + width)],
+                         c = cut[std::min(parts, 2 * width * m + 2 * width)];
+            std::merge(src->begin() + a, src->begin() + b, src->begin() + b, src->begin() + c, dst->begin() + a);
+        });
+        std::swap(src, dst);
+    }
+    if (src != &v) v.swap(*src);
 }
 
 // ---------------------------------------------------------------- ray grid
@@ -464,9 +523,27 @@ void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, in
     const size_t ncell = (size_t)ga * gb;
     // Each cell lists its boxes by (maxt, triangle), a strict order (a box
     // enters a cell once).  Filling the cells from the boxes in that order
-    // leaves every cell sorted without a sort per cell.
-    std::sort(boxes.begin(), boxes.end(),
-              [](const Box& x, const Box& y) { return x.maxt < y.maxt || (x.maxt == y.maxt && x.tri < y.tri); });
+    // leaves every cell sorted without a sort per cell.  The order is sorted
+    // as 64-bit keys (order-preserving float bits of maxt, -0 folded into
+    // +0, then the triangle), in chunks on host threads merged pairwise.
+    {
+        std::vector<uint64_t> key(boxes.size());
+        parallel_chunks(boxes.size(), 65536, [&](size_t lo, size_t hi) {
+            for (size_t i = lo; i < hi; i++) {
+                uint32_t u;
+                const float m = boxes[i].maxt + 0.0f;
+                std::memcpy(&u, &m, 4);
+                u = (u >> 31) ? ~u : (u | 0x80000000u);
+                key[i] = ((uint64_t)u << 32) | (uint32_t)i;  // box index: triangles are in box order
+            }
+        });
+        parallel_sort_u64(key);
+        std::vector<Box> sorted(boxes.size());
+        parallel_chunks(boxes.size(), 65536, [&](size_t lo, size_t hi) {
+            for (size_t i = lo; i < hi; i++) sorted[i] = boxes[(uint32_t)key[i]];
+        });
+        boxes.swap(sorted);
+    }
     // Counting and filling run on bands of cell rows: a band's cells belong to
     // one thread, which walks every box in the sorted order.
     const size_t band_rows = boxes.size() >= 65536 ? 1 : (size_t)gb;
@@ -501,7 +578,11 @@ void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, in
     });
     tree->cell_base = (int32_t)P->cell_start.size();
     tree->n_cells = (int32_t)ncell;
-    for (size_t c = 0; c <= ncell; c++) P->cell_start.push_back((int32_t)(base + cnt[c]));
+    const size_t cs0 = P->cell_start.size();
+    P->cell_start.resize(cs0 + ncell + 1);
+    parallel_chunks(ncell + 1, 1 << 18, [&](size_t lo, size_t hi) {
+        for (size_t c = lo; c < hi; c++) P->cell_start[cs0 + c] = (int32_t)(base + cnt[c]);
+    });
     tree->all_first = (int32_t)P->ents.size();
     tree->all_count = (int32_t)all.size();
     for (int i : all) P->ents.push_back(RayEnt{INFINITY, i});
@@ -869,46 +950,73 @@ struct Lowerer {
         });
         P->tri_parent.resize(P->tris.size(), -1);
         if (ts.n > 1) {
-            TreeBuilder tb{t, {}};
-            tb.nodes.reserve(order.size() - 1);
-            int root = tb.build(order.data(), order.size());
+            FlatTree ft(t, order.data(), order.size());
+            const unsigned hw = std::thread::hardware_concurrency();
+            int depth = 0;  // 2^depth threads at the deepest split, up to the host's threads
+            while (depth < 4 && (2u << depth) <= std::max(1u, hw)) depth++;
+            const int root = ft.build(0, order.size(), 0, depth);
             int node_base = (int)P->nodes.size();
-            // Breadth-first order keeps the upper levels together.
-            std::vector<int> label(tb.nodes.size(), -1), queue = {root};
-            label[root] = 0;
-            for (size_t qi = 0; qi < queue.size(); qi++)
-                for (int c : tb.nodes[queue[qi]].ch)
-                    if (c >= 0) {
-                        label[c] = (int)queue.size();
+            // Breadth first over the surviving nodes; a node's children are its
+            // two subtrees' references, an absorbed node replaced by its own
+            // children, in order (a stack of pending references).
+            std::vector<int> queue = {root};
+            queue.reserve(order.size());
+            std::vector<int> stack;
+            for (size_t qi = 0; qi < queue.size(); qi++) {
+                const int u = queue[qi];
+                stack.assign({ft.ch2[u], ft.ch1[u]});
+                while (!stack.empty()) {
+                    const int c = stack.back();
+                    stack.pop_back();
+                    if (c < 0) {
+                        P->tri_parent[tri_base + pos_of[-c - 1]] = node_base + (int)qi;
+                    } else if (ft.absorbed[c]) {
+                        stack.push_back(ft.ch2[c]);
+                        stack.push_back(ft.ch1[c]);
+                    } else {
                         queue.push_back(c);
                     }
+                }
+            }
             P->nodes.resize(node_base + queue.size());
             P->nodes_f.resize(node_base + queue.size());
-            for (size_t qi = 0; qi < queue.size(); qi++) {
-                const BNode& b = tb.nodes[queue[qi]];
-                BvhNodeD nd{};
-                BvhNodeF nf{};
-                for (int k = 0; k < 3; k++) {
-                    nd.lo[k] = b.mn.v[k];
-                    nd.hi[k] = b.mx.v[k];
-                    nf.lo[k] = f_down(b.mn.v[k]);
-                    nf.hi[k] = f_up(b.mx.v[k]);
+            parallel_chunks(queue.size(), 65536, [&](size_t lo, size_t hi) {
+                for (size_t qi = lo; qi < hi; qi++) {
+                    const int u = queue[qi];
+                    BvhNodeD nd{};
+                    BvhNodeF nf{};
+                    for (int k = 0; k < 3; k++) {
+                        nd.lo[k] = ft.mn[u].v[k];
+                        nd.hi[k] = ft.mx[u].v[k];
+                        nf.lo[k] = f_down(ft.mn[u].v[k]);
+                        nf.hi[k] = f_up(ft.mx[u].v[k]);
+                    }
+                    P->nodes[node_base + qi] = nd;
+                    P->nodes_f[node_base + qi] = nf;
                 }
-                for (int c : b.ch)
-                    if (c < 0) P->tri_parent[tri_base + pos_of[-c - 1]] = node_base + (int)qi;
-                P->nodes[node_base + qi] = nd;
-                P->nodes_f[node_base + qi] = nf;
-            }
+            });
         }
         tree.kind = ts.n > 0 ? 1 : 0;
         // Coordinate magnitude bound for the FP32 ray-box filter and the pads.
         double R = 0;
-        for (int a = 0; a < 3; a++) {
-            double m = 0;
-            for (const Tri& tr : t)
-                m = std::max(m, std::max(std::fabs(tr.mn.v[a]), std::fabs(tr.mx.v[a])));
-            tree.mbox[a] = f_up(m);
-            R = std::max(R, m);
+        {
+            // Per-axis maxima of |coordinate| over every box, in chunks on
+            // host threads (max is exact in any order).
+            std::vector<std::array<double, 3>> part(16, std::array<double, 3>{0, 0, 0});
+            std::atomic<int> next{0};
+            parallel_chunks(t.size(), 65536, [&](size_t lo, size_t hi) {
+                std::array<double, 3> m{0, 0, 0};
+                for (size_t i = lo; i < hi; i++)
+                    for (int a = 0; a < 3; a++)
+                        m[a] = std::max(m[a], std::max(std::fabs(t[i].mn.v[a]), std::fabs(t[i].mx.v[a])));
+                part[next++] = m;
+            });
+            for (int a = 0; a < 3; a++) {
+                double m = 0;
+                for (const auto& q : part) m = std::max(m, q[a]);
+                tree.mbox[a] = f_up(m);
+                R = std::max(R, m);
+            }
         }
         build_ray_grid(t, order, tri_base, R, P, &tree);
         int id = (int)P->trees.size();
