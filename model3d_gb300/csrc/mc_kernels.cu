@@ -2456,7 +2456,7 @@ void mc_destroy(mc_ctx* ctx) {
 constexpr int64_t kDeviceGroupMin = 1 << 15;
 
 mc_status pregroup_sets(mc_ctx* ctx, const mc_tri_set* sets, size_t n_sets, std::vector<mc_tri_set>* out,
-                        std::vector<std::vector<double>>* grouped) {
+                        std::vector<bulk_vector<double>>* grouped) {
     bool any = false;
     for (size_t i = 0; i < n_sets; i++) any = any || (!sets[i].grouped && sets[i].n >= kDeviceGroupMin && sets[i].tris);
     if (!any) return MC_OK;
@@ -2479,7 +2479,7 @@ mc_status pregroup_sets(mc_ctx* ctx, const mc_tri_set* sets, size_t n_sets, std:
         std::vector<int32_t> order((size_t)ts.n);
         CK(cudaMemcpyAsync(order.data(), ctx->gorder.p, (size_t)ts.n * 4, cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
-        std::vector<double>& g = (*grouped)[i];
+        bulk_vector<double>& g = (*grouped)[i];  // every element written by the gather
         g.resize((size_t)ts.n * 9);
         // The gather in grouped order, in up to 16 chunks on host threads.
         const size_t n = (size_t)ts.n;
@@ -2518,7 +2518,7 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
         // which gives the same program (the order is the host grouping's:
         // both sort stably by midpoint and split alike).
         std::vector<mc_tri_set> gsets;
-        std::vector<std::vector<double>> grouped;
+        std::vector<bulk_vector<double>> grouped;
         mc_status gs = pregroup_sets(ctx, sets, n_sets, &gsets, &grouped);
         if (gs != MC_OK) return gs;
         lower_scene(nodes, n_nodes, gsets.empty() ? sets : gsets.data(), n_sets, &s->host);
@@ -2575,10 +2575,15 @@ mc_status mc_solid_create(mc_ctx* ctx, const mc_node* nodes, size_t n_nodes, con
         }
     }
     CK(s->buf.ensure(total));
-    std::vector<unsigned char> staging(total, 0);
+    // The allocation zeroed on the device (the gaps between pieces included),
+    // then one copy per piece straight from the host program's arrays: no
+    // host staging copy of the (for a large collider, several hundred MB)
+    // program.
+    CK(cudaMemsetAsync(s->buf.p, 0, total, ctx->stream));
     for (auto& p : pcs)
-        if (p.bytes) std::memcpy(staging.data() + p.off, p.src, p.bytes);
-    CK(cudaMemcpyAsync(s->buf.p, staging.data(), total, cudaMemcpyHostToDevice, ctx->stream));
+        if (p.bytes)
+            CK(cudaMemcpyAsync((unsigned char*)s->buf.p + p.off, p.src, p.bytes, cudaMemcpyHostToDevice,
+                               ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     unsigned char* b = (unsigned char*)s->buf.p;
     ProgView& v = s->view;

@@ -245,7 +245,7 @@ struct Grouper {
     static constexpr size_t kParallelGroup = 1 << 16;
 };
 
-std::vector<int> group_triangles(const std::vector<Tri>& t) {  // GroupTriangles, bvh.go:118-133
+std::vector<int> group_triangles(const bulk_vector<Tri>& t) {  // GroupTriangles, bvh.go:118-133
     const size_t n = t.size();
     std::vector<int> out(n);
     if (n == 0) return out;
@@ -293,14 +293,14 @@ std::vector<int> group_triangles(const std::vector<Tri>& t) {  // GroupTriangles
 // Flat arrays instead of a child vector per node; the bounds are computed
 // bottom up with the upper levels' halves on two threads.
 struct FlatTree {
-    const std::vector<Tri>& tris;
+    const bulk_vector<Tri>& tris;
     const int* order;
     std::vector<D3> mn, mx;
     std::vector<int> ch1, ch2;
     std::vector<uint8_t> absorbed;
     static constexpr size_t kParallel = 1 << 15;
 
-    FlatTree(const std::vector<Tri>& t, const int* o, size_t n)
+    FlatTree(const bulk_vector<Tri>& t, const int* o, size_t n)
         : tris(t), order(o), mn(n - 1), mx(n - 1), ch1(n - 1), ch2(n - 1), absorbed(n - 1, 0) {}
 
     D3 bmin(int c) const { return c >= 0 ? mn[c] : tris[-c - 1].mn; }
@@ -362,6 +362,28 @@ void parallel_chunks(size_t n, size_t min_per_thread, F&& f) {
     for (std::thread& x : th) x.join();
 }
 
+// Runs f(k) for every k in [0, n) on up to 16 host threads, each thread
+// taking the next k from a shared counter (tasks of uneven size balance).
+// Tasks must touch disjoint data.
+template <class F>
+void parallel_tasks(size_t n, F&& f) {
+    std::atomic<size_t> next{0};
+    auto worker = [&] {
+        for (size_t k; (k = next.fetch_add(1)) < n;) f(k);
+    };
+    const size_t T = std::min<size_t>({(size_t)std::max(1u, std::thread::hardware_concurrency()), 16, n});
+    std::vector<std::thread> th;
+    for (size_t k = 1; k < T; k++) {
+        try {
+            th.emplace_back(worker);
+        } catch (const std::system_error&) {
+            break;  // the caller's thread takes what is left
+        }
+    }
+    worker();
+    for (std::thread& x : th) x.join();
+}
+
 // Sort of distinct 64-bit keys: chunks sorted on host threads, then merged
 // pairwise, each round's merges on host threads.  The result is the sorted
 // sequence whatever the split.
@@ -415,7 +437,7 @@ void parallel_sort_u64(std::vector<uint64_t>& v) {
 // error of det and kappa2 = max |e| / |e projected| over the edges; the pads
 // below are 8 and 20 times larger.  Triangles with 7 eps kappa1 > 1e-3,
 // whose det sign the float64 test may get wrong, are tested by every ray.
-void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, int tri_base, double R,
+void build_ray_grid(const bulk_vector<Tri>& t, const std::vector<int>& order, int tri_base, double R,
                     HostProgram* P, TreeD* tree) {
     const double eps = DBL_EPSILON / 2;
     const D3 dh = vnormalize(kRay);
@@ -544,44 +566,115 @@ void build_ray_grid(const std::vector<Tri>& t, const std::vector<int>& order, in
         });
         boxes.swap(sorted);
     }
-    // Counting and filling run on bands of cell rows: a band's cells belong to
-    // one thread, which walks every box in the sorted order.
-    const size_t band_rows = boxes.size() >= 65536 ? 1 : (size_t)gb;
-    std::vector<int64_t> cnt(ncell + 1, 0);
-    parallel_chunks((size_t)gb, band_rows, [&](size_t y_lo, size_t y_hi) {
-        for (const Box& b : boxes) {
-            int a0, a1, b0, b1;
-            cell_range(b.alo, b.ahi, amin_f, ga, &a0, &a1);
-            cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
-            b0 = std::max(b0, (int)y_lo);
-            b1 = std::min(b1, (int)y_hi - 1);
-            for (int y = b0; y <= b1; y++)
-                for (int x = a0; x <= a1; x++) cnt[(size_t)y * ga + x + 1]++;
-        }
-    });
-    for (size_t c = 0; c < ncell; c++) cnt[c + 1] += cnt[c];
+    // Counting and filling run on bands of cell rows, each band on one thread.
+    // The boxes meeting a band are listed per band first (in the sorted
+    // order), so a band walks only its own boxes and writes only its own,
+    // contiguous, stretch of the entries.
     const int64_t base = (int64_t)P->ents.size();
-    if (base + cnt[ncell] + (int64_t)all.size() >= ((int64_t)1 << 31))
-        throw LowerError(MC_ERR_LIMIT, "collider ray grid exceeds 2^31 entries");
-    P->ents.resize(base + cnt[ncell]);
-    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
-    parallel_chunks((size_t)gb, band_rows, [&](size_t y_lo, size_t y_hi) {
-        for (const Box& b : boxes) {
-            int a0, a1, b0, b1;
-            cell_range(b.alo, b.ahi, amin_f, ga, &a0, &a1);
-            cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
-            b0 = std::max(b0, (int)y_lo);
-            b1 = std::min(b1, (int)y_hi - 1);
-            for (int y = b0; y <= b1; y++)
-                for (int x = a0; x <= a1; x++) P->ents[base + fill[(size_t)y * ga + x]++] = RayEnt{b.maxt, b.tri};
+    const size_t nband = std::min<size_t>((size_t)gb, boxes.size() >= 65536 ? 256 : 1);
+    auto band_of = [&](int row) { return (size_t)row * nband / (size_t)gb; };
+    auto band_rows = [&](size_t k, int* r0, int* r1) {
+        *r0 = (int)((k * (size_t)gb + nband - 1) / nband);  // first row r with band_of(r) == k
+        *r1 = (int)(((k + 1) * (size_t)gb + nband - 1) / nband) - 1;
+    };
+    // Per band, the indices of its boxes: counts per (chunk, band), offsets,
+    // then each chunk writes its boxes at its offsets (order kept).
+    const size_t nchunk = boxes.size() >= 65536 ? std::min<size_t>(16, std::max(1u, std::thread::hardware_concurrency())) : 1;
+    std::vector<size_t> ccount(nchunk * nband, 0);
+    auto box_bands = [&](const Box& b, size_t* k0, size_t* k1) {
+        int b0, b1;
+        cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
+        if (b0 > b1) return false;
+        *k0 = band_of(b0);
+        *k1 = band_of(b1);
+        return true;
+    };
+    parallel_tasks(nchunk, [&](size_t c) {
+        const size_t lo = boxes.size() * c / nchunk, hi = boxes.size() * (c + 1) / nchunk;
+        for (size_t i = lo; i < hi; i++) {
+            size_t k0, k1;
+            if (box_bands(boxes[i], &k0, &k1))
+                for (size_t k = k0; k <= k1; k++) ccount[c * nband + k]++;
         }
     });
+    std::vector<size_t> band_start(nband + 1, 0), coff(nchunk * nband);
+    {
+        size_t at = 0;
+        for (size_t k = 0; k < nband; k++) {
+            band_start[k] = at;
+            for (size_t c = 0; c < nchunk; c++) {
+                coff[c * nband + k] = at;
+                at += ccount[c * nband + k];
+            }
+        }
+        band_start[nband] = at;
+    }
+    bulk_vector<uint32_t> band_box(band_start[nband]);
+    parallel_tasks(nchunk, [&](size_t c) {
+        const size_t lo = boxes.size() * c / nchunk, hi = boxes.size() * (c + 1) / nchunk;
+        std::vector<size_t> at(coff.begin() + c * nband, coff.begin() + (c + 1) * nband);
+        for (size_t i = lo; i < hi; i++) {
+            size_t k0, k1;
+            if (box_bands(boxes[i], &k0, &k1))
+                for (size_t k = k0; k <= k1; k++) band_box[at[k]++] = (uint32_t)i;
+        }
+    });
+    // Walks the cells of band k that box j (an index into band_box) covers.
+    auto band_cells = [&](size_t k, size_t j, auto&& visit) {
+        int y_lo, y_hi, a0, a1, b0, b1;
+        band_rows(k, &y_lo, &y_hi);
+        const Box& b = boxes[band_box[j]];
+        cell_range(b.alo, b.ahi, amin_f, ga, &a0, &a1);
+        cell_range(b.blo, b.bhi, bmin_f, gb, &b0, &b1);
+        b0 = std::max(b0, y_lo);
+        b1 = std::min(b1, y_hi);
+        for (int y = b0; y <= b1; y++)
+            for (int x = a0; x <= a1; x++) visit((size_t)y * ga + x, b);
+    };
+    // A band's cells are its rows, contiguous: each band zeroes and counts
+    // its own cells and sums them.
+    bulk_vector<uint32_t> cnt(ncell);
+    std::vector<int64_t> band_total(nband + 1, 0);
+    parallel_tasks(nband, [&](size_t k) {
+        int y_lo, y_hi;
+        band_rows(k, &y_lo, &y_hi);
+        const size_t c_lo = (size_t)y_lo * ga, c_hi = (size_t)(y_hi + 1) * ga;
+        std::fill(cnt.begin() + c_lo, cnt.begin() + c_hi, 0u);
+        for (size_t j = band_start[k]; j < band_start[k + 1]; j++)
+            band_cells(k, j, [&](size_t c, const Box&) { cnt[c]++; });
+        int64_t sum = 0;
+        for (size_t c = c_lo; c < c_hi; c++) sum += cnt[c];
+        band_total[k] = sum;
+    });
+    int64_t total = 0;
+    for (size_t k = 0; k < nband; k++) {
+        const int64_t t = band_total[k];
+        band_total[k] = total;
+        total += t;
+    }
+    if (base + total + (int64_t)all.size() >= ((int64_t)1 << 31))
+        throw LowerError(MC_ERR_LIMIT, "collider ray grid exceeds 2^31 entries");
+    P->ents.resize(base + total);
     tree->cell_base = (int32_t)P->cell_start.size();
     tree->n_cells = (int32_t)ncell;
     const size_t cs0 = P->cell_start.size();
     P->cell_start.resize(cs0 + ncell + 1);
-    parallel_chunks(ncell + 1, 1 << 18, [&](size_t lo, size_t hi) {
-        for (size_t c = lo; c < hi; c++) P->cell_start[cs0 + c] = (int32_t)(base + cnt[c]);
+    P->cell_start[cs0 + ncell] = (int32_t)(base + total);
+    // Each band turns its counts into cell offsets (from the band's own
+    // offset), records them, and fills its cells using the offsets as cursors.
+    parallel_tasks(nband, [&](size_t k) {
+        int y_lo, y_hi;
+        band_rows(k, &y_lo, &y_hi);
+        const size_t c_lo = (size_t)y_lo * ga, c_hi = (size_t)(y_hi + 1) * ga;
+        uint32_t at = (uint32_t)band_total[k];
+        for (size_t c = c_lo; c < c_hi; c++) {
+            const uint32_t n_c = cnt[c];
+            cnt[c] = at;
+            P->cell_start[cs0 + c] = (int32_t)(base + at);
+            at += n_c;
+        }
+        for (size_t j = band_start[k]; j < band_start[k + 1]; j++)
+            band_cells(k, j, [&](size_t c, const Box& b) { P->ents[base + cnt[c]++] = RayEnt{b.maxt, b.tri}; });
     });
     tree->all_first = (int32_t)P->ents.size();
     tree->all_count = (int32_t)all.size();
@@ -895,13 +988,15 @@ struct Lowerer {
         if (it != tree_of_set.end()) return it->second;
         const mc_tri_set& ts = sets[set];
         if (ts.n < 0 || (ts.n > 0 && !ts.tris)) fail("bad triangle set");
-        std::vector<Tri> t(ts.n);
-        for (int64_t i = 0; i < ts.n; i++) {
-            for (int k = 0; k < 3; k++)
-                t[i].p[k] = d3(ts.tris[i * 9 + 3 * k], ts.tris[i * 9 + 3 * k + 1], ts.tris[i * 9 + 3 * k + 2]);
-            t[i].mn = vmin3(vmin3(t[i].p[0], t[i].p[1]), t[i].p[2]);  // Triangle.Min, primitives.go:36-38
-            t[i].mx = vmax3(vmax3(t[i].p[0], t[i].p[1]), t[i].p[2]);
-        }
+        bulk_vector<Tri> t(ts.n);
+        parallel_chunks(t.size(), 65536, [&](size_t lo, size_t hi) {
+            for (size_t i = lo; i < hi; i++) {
+                for (int k = 0; k < 3; k++)
+                    t[i].p[k] = d3(ts.tris[i * 9 + 3 * k], ts.tris[i * 9 + 3 * k + 1], ts.tris[i * 9 + 3 * k + 2]);
+                t[i].mn = vmin3(vmin3(t[i].p[0], t[i].p[1]), t[i].p[2]);  // Triangle.Min, primitives.go:36-38
+                t[i].mx = vmax3(vmax3(t[i].p[0], t[i].p[1]), t[i].p[2]);
+            }
+        });
         std::vector<int> order;
         if (ts.grouped) {
             order.resize(ts.n);
@@ -1448,8 +1543,8 @@ struct Digest {
             word(w);
         }
     }
-    template <class T>
-    void vec(const std::vector<T>& v) { bytes(v.data(), v.size() * sizeof(T)); }
+    template <class T, class A>
+    void vec(const std::vector<T, A>& v) { bytes(v.data(), v.size() * sizeof(T)); }
 };
 
 uint64_t program_digest(const mcgpu::HostProgram& P) {

@@ -2,8 +2,11 @@
 // device program layout of mc_internal.h.
 #pragma once
 
+#include <memory>
+#include <new>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/mcgpu.h"
@@ -15,6 +18,31 @@ struct LowerError : std::runtime_error {
     mc_status status;
     LowerError(mc_status s, const std::string& m) : std::runtime_error(m), status(s) {}
 };
+
+// Allocator whose default construction leaves elements uninitialised: the
+// large arrays of a lowering are sized once and every element is then
+// written by host threads, so the serial zero fill (and first touch of every
+// page on one thread) is skipped.  Construction from a value is as usual.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <class U>
+    NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+    template <class U>
+    void construct(U* p) noexcept {
+        ::new ((void*)p) U;
+    }
+    template <class U, class... A>
+    void construct(U* p, A&&... a) {
+        ::new ((void*)p) U(std::forward<A>(a)...);
+    }
+};
+template <class T>
+using bulk_vector = std::vector<T, NoInitAlloc<T>>;
 
 // Host copy of a lowered solid; uploaded once by mc_solid_create.
 struct HostProgram {
@@ -29,13 +57,13 @@ struct HostProgram {
     std::vector<XBoxD> xbox;
     std::vector<XStepD> xstep;
     std::vector<TreeD> trees;
-    std::vector<BvhNodeD> nodes;
-    std::vector<BvhNodeF> nodes_f;
+    bulk_vector<BvhNodeD> nodes;
+    bulk_vector<BvhNodeF> nodes_f;
     std::vector<int32_t> tri_parent;
-    std::vector<int32_t> cell_start;
-    std::vector<RayEnt> ents;
-    std::vector<TriD> tris;
-    std::vector<TriF> tris_f;
+    bulk_vector<int32_t> cell_start;
+    bulk_vector<RayEnt> ents;
+    bulk_vector<TriD> tris;
+    bulk_vector<TriF> tris_f;
     std::vector<MetaD> metas;
     std::vector<MetaF> metas_f;
     std::vector<BallD> balls;
