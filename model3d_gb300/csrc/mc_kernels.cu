@@ -2894,8 +2894,16 @@ mc_status search_launch(mc_ctx* ctx, const mc_solid* solid, double delta, int32_
             CK(cudaGetLastError());
         } else {
             // Vertex ranges (multiples of 32) searched by consecutive launches,
-            // each followed by an event for the caller's read-back.
-            const int nch = copy_chunks > 1 && V >= (1 << 17) ? std::min(copy_chunks, mc_ctx::kCopyChunks) : 1;
+            // each followed by an event for the caller's read-back.  Not for
+            // collider or metaball programs: their searches (one vertex batch
+            // a warp, long chains of dependent loads) are bound by their
+            // slowest warps, so split launches run those latencies one after
+            // another, while their vertices take a small part of the time to
+            // copy back.
+            const bool latency_bound = H.has_collider || !H.metas.empty();
+            const int nch = copy_chunks > 1 && V >= (1 << 17) && !latency_bound
+                                ? std::min(copy_chunks, mc_ctx::kCopyChunks)
+                                : 1;
             ctx->n_chunks = nch;
             long long v0 = 0;
             for (int c = 0; c < nch; c++) {
