@@ -452,9 +452,9 @@ void build_ray_grid(const bulk_vector<Tri>& t, const std::vector<int>& order, in
     // extent still counts towards the cell size.  Then boxes, `all` and the
     // extents are collected in triangle order.
     const size_t n = order.size();
-    std::vector<Box> cand(n);
+    bulk_vector<Box> cand(n);       // read only where kind is 1
     std::vector<uint8_t> kind(n, 0);
-    std::vector<double> extent(n, 0.0);
+    bulk_vector<double> extent(n);  // read only where kind is 1 or 3
     parallel_chunks(n, 16384, [&](size_t lo, size_t hi) {
         for (size_t i = lo; i < hi; i++) {
             if (!P->tris[tri_base + i].valid) continue;  // parallel or det == 0: never hit
@@ -499,26 +499,58 @@ void build_ray_grid(const bulk_vector<Tri>& t, const std::vector<int>& order, in
             kind[i] = 1;
         }
     });
-    std::vector<Box> boxes;
-    boxes.reserve(n);
-    std::vector<int> all;
-    std::vector<double> sizes;
-    sizes.reserve(n);
-    for (size_t i = 0; i < n; i++) {
-        if (kind[i] == 1 || kind[i] == 3) sizes.push_back(extent[i]);
-        if (kind[i] == 1) boxes.push_back(cand[i]);
-        if (kind[i] == 2 || kind[i] == 3) all.push_back(tri_base + (int)i);
+    // Boxes, the every-ray list and the extents collected in triangle order,
+    // with the boxes' bounds: per-chunk counts, offsets, then each chunk
+    // writes its own stretch.  The chunks' bounds are combined in chunk
+    // order, so each bound is the first of its equal values, as in one pass.
+    const size_t nck = n >= 65536 ? std::min<size_t>(16, std::max(1u, std::thread::hardware_concurrency())) : 1;
+    std::vector<size_t> nb(nck + 1, 0), na(nck + 1, 0), ns(nck + 1, 0);
+    parallel_tasks(nck, [&](size_t c) {
+        size_t b = 0, a = 0, z = 0;
+        for (size_t i = n * c / nck; i < n * (c + 1) / nck; i++) {
+            b += kind[i] == 1;
+            a += kind[i] == 2 || kind[i] == 3;
+            z += kind[i] == 1 || kind[i] == 3;
+        }
+        nb[c + 1] = b;
+        na[c + 1] = a;
+        ns[c + 1] = z;
+    });
+    for (size_t c = 0; c < nck; c++) {
+        nb[c + 1] += nb[c];
+        na[c + 1] += na[c];
+        ns[c + 1] += ns[c];
     }
-    std::vector<Box>().swap(cand);
+    bulk_vector<Box> boxes(nb[nck]);
+    std::vector<int> all(na[nck]);
+    std::vector<double> sizes(ns[nck]);
+    std::vector<std::array<double, 4>> part(nck, std::array<double, 4>{DBL_MAX, -DBL_MAX, DBL_MAX, -DBL_MAX});
+    parallel_tasks(nck, [&](size_t c) {
+        size_t b = nb[c], a = na[c], z = ns[c];
+        std::array<double, 4>& m = part[c];
+        for (size_t i = n * c / nck; i < n * (c + 1) / nck; i++) {
+            if (kind[i] == 1 || kind[i] == 3) sizes[z++] = extent[i];
+            if (kind[i] == 1) {
+                const Box& x = cand[i];
+                boxes[b++] = x;
+                m[0] = std::min(m[0], x.alo);
+                m[1] = std::max(m[1], x.ahi);
+                m[2] = std::min(m[2], x.blo);
+                m[3] = std::max(m[3], x.bhi);
+            }
+            if (kind[i] == 2 || kind[i] == 3) all[a++] = tri_base + (int)i;
+        }
+    });
+    bulk_vector<Box>().swap(cand);
     double amin = 0, amax = 0, bmin = 0, bmax = 0;
     if (!boxes.empty()) {
         amin = bmin = DBL_MAX;
         amax = bmax = -DBL_MAX;
-        for (const Box& b : boxes) {
-            amin = std::min(amin, b.alo);
-            amax = std::max(amax, b.ahi);
-            bmin = std::min(bmin, b.blo);
-            bmax = std::max(bmax, b.bhi);
+        for (const auto& m : part) {
+            amin = std::min(amin, m[0]);
+            amax = std::max(amax, m[1]);
+            bmin = std::min(bmin, m[2]);
+            bmax = std::max(bmax, m[3]);
         }
     }
     // Cell edge: a quarter of the median triangle extent (measured fastest
@@ -560,7 +592,7 @@ void build_ray_grid(const bulk_vector<Tri>& t, const std::vector<int>& order, in
             }
         });
         parallel_sort_u64(key);
-        std::vector<Box> sorted(boxes.size());
+        bulk_vector<Box> sorted(boxes.size());
         parallel_chunks(boxes.size(), 65536, [&](size_t lo, size_t hi) {
             for (size_t i = lo; i < hi; i++) sorted[i] = boxes[(uint32_t)key[i]];
         });
