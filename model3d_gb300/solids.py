@@ -452,14 +452,11 @@ class MeshCollider:
     def _bound(self, red, op):
         if len(self.tris) == 0:
             return Coord3D()  # nullCollider (model3d/collisions.go:358-366)
-        v = self.tris.reshape(-1, 3, 3)
+        v = self.tris.reshape(-1, 3)
         out = []
         for a in range(3):
-            col = v[:, :, a].ravel()
-            if np.isnan(col).any():
-                out.append(math.nan)
-                continue
-            r = float(red(col))
+            col = v[:, a]  # a strided view: no copy
+            r = float(red(col))  # NaN when any coordinate is NaN (np.min/np.max propagate it)
             if r == 0.0:  # -0 wins in Min, +0 in Max, as math.Min/Max order them
                 neg = np.signbit(col[col == 0]).any()
                 pos = (~np.signbit(col[col == 0])).any()
