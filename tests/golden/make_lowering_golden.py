@@ -13,6 +13,8 @@ import json
 import os
 import sys
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
@@ -23,8 +25,24 @@ from model3d_gb300.workloads import (box_triangles, csg_tree, displaced_icospher
                                      icosphere_triangles, metaball_blob)
 
 
+def _soup(n, seed, scale=0.05):
+    """n random small triangles around points of [-1, 1]^3 (seeded)."""
+    r = np.random.default_rng(seed)
+    c = r.uniform(-1, 1, (n, 1, 3))
+    return (c + r.normal(0, scale, (n, 3, 3))).reshape(-1, 9)
+
+
+def _degenerate(n, seed):
+    """A soup with every 7th triangle's second vertex repeated (det 0) and
+    every 11th (from the 2nd) collinear."""
+    t = _soup(n, seed)
+    t[::7, 3:6] = t[::7, 0:3]
+    t[1::11, 6:9] = 2 * t[1::11, 3:6] - t[1::11, 0:3]
+    return t
+
+
 def scenes():
-    """name -> solid.  Sizes stay small enough to lower in about a second in all."""
+    """name -> solid.  Sizes stay small enough to lower in a few seconds in all."""
     ico = NewColliderSolid(MeshToCollider(icosphere_triangles(40)))
     return {
         "csg_tree_48_16": csg_tree(1),
@@ -40,6 +58,11 @@ def scenes():
         "collider_box_with_csg": JoinedSolid([
             NewColliderSolid(MeshToCollider(box_triangles((2.0, -0.5, -0.5), (3.0, 0.5, 0.5)))),
             ico, Sphere(XYZ(0, 3, 0), 0.5)]),
+        # Just above the size at which the ray grid is counted and filled in
+        # bands of cell rows; degenerate triangles; many equal midpoints.
+        "collider_soup_65537": NewColliderSolid(MeshToCollider(_soup(65537, 65537))),
+        "collider_degenerate_70000": NewColliderSolid(MeshToCollider(_degenerate(70000, 1))),
+        "collider_lattice_90000": NewColliderSolid(MeshToCollider(np.round(_soup(90000, 3) * 8) / 8)),
         "metaball_blob_12": metaball_blob(2, 12),
         "metaball_blob_wyvill_8": metaball_blob(4, 8, falloff=WyvillMetaballFalloffFunc(0.6)),
     }
