@@ -181,11 +181,7 @@ class Mesh:
         t = np.ascontiguousarray(self.triangles, dtype=np.int32).reshape(-1, 3)
         return v, t
 
-    def EncodeGroupedSTL(self, ctx: Optional["Context"] = None) -> bytes:
-        """The bytes SaveGroupedSTL writes (model3d/mesh.go:724-742): the
-        triangles in GroupTriangles order (ties in the midpoint sorts keep
-        this mesh's triangle order), binary STL records (export.go:28-60).
-        Grouped and encoded on the device."""
+    def _grouped_stl(self, ctx: Optional["Context"]) -> np.ndarray:
         ctx = ctx or default_context()
         v, t = self._arrays()
         L = N.lib()
@@ -195,13 +191,22 @@ class Mesh:
         buf = np.empty(n.value, dtype=np.uint8)
         _check(L.mc_mesh_stl_grouped(ctx.ptr, v.ctypes.data, len(v), t.ctypes.data, len(t), buf.ctypes.data,
                                      n.value, ctypes.byref(n)), ctx.ptr)
-        return buf.tobytes()
+        return buf
+
+    def EncodeGroupedSTL(self, ctx: Optional["Context"] = None) -> bytes:
+        """The bytes SaveGroupedSTL writes (model3d/mesh.go:724-742): the
+        triangles in GroupTriangles order (ties in the midpoint sorts keep
+        this mesh's triangle order), binary STL records (export.go:28-60).
+        Grouped and encoded on the device."""
+        return self._grouped_stl(ctx).tobytes()
 
     def SaveGroupedSTL(self, path: str, ctx: Optional["Context"] = None) -> None:
-        """Mesh.SaveGroupedSTL (model3d/mesh.go:724-742)."""
-        data = self.EncodeGroupedSTL(ctx)
+        """Mesh.SaveGroupedSTL (model3d/mesh.go:724-742).  The encoded
+        records are written from the array they were copied into, without
+        a copy into a bytes object."""
+        data = self._grouped_stl(ctx)
         with open(path, "wb") as f:
-            f.write(data)
+            f.write(memoryview(data))
 
 
 def GroupTriangles(mesh: Mesh, *, ctx: Optional["Context"] = None) -> np.ndarray:
