@@ -457,7 +457,11 @@ class MeshCollider:
         for a in range(3):
             col = v[:, a]  # a strided view: no copy
             r = float(red(col))  # NaN when any coordinate is NaN (np.min/np.max propagate it)
-            if r == 0.0:  # -0 wins in Min, +0 in Max, as math.Min/Max order them
+            if r != r:  # but math.Min lets -Inf win over NaN, math.Max +Inf
+                inf = -math.inf if op is go_min else math.inf
+                if (col == inf).any():
+                    r = inf
+            elif r == 0.0:  # -0 wins in Min, +0 in Max, as math.Min/Max order them
                 neg = np.signbit(col[col == 0]).any()
                 pos = (~np.signbit(col[col == 0])).any()
                 r = -0.0 if (op is go_min and neg) or (op is go_max and not pos) else 0.0

@@ -7,6 +7,7 @@ The root bounds it reports are the serialised `Min()/Max()` of the root
 Python mirror bit for bit.  Malformed record arrays come back as statuses.
 """
 import ctypes
+import math
 
 import numpy as np
 import pytest
@@ -108,6 +109,30 @@ def _status(nodes, sets=()):
     st = N.lib().mc_program_check(nodes.ctypes.data if len(nodes) else None, len(nodes),
                                   ctypes.addressof(arr), len(sets), ctypes.byref(info), err, len(err))
     return st, err.value.decode()
+
+
+def test_collider_bounds_follow_math_min_max():
+    """MeshCollider.Min/Max equal the fold of math.Min / math.Max over every
+    vertex coordinate (Triangle.Min and the joined colliders' bounds,
+    model3d/primitives.go:36-42, collisions.go:217-253): -Inf wins over NaN,
+    NaN over numbers, -0 over +0 in Min and +0 over -0 in Max."""
+    import functools
+    from model3d_gb300.geometry import go_max, go_min
+    from model3d_gb300.solids import MeshCollider
+    rng = np.random.default_rng(5)
+    specials = [0.0, -0.0, math.nan, math.inf, -math.inf, 1.5, -2.25]
+    for trial in range(300):
+        n = int(rng.integers(1, 6))
+        t = rng.choice([0.0, -0.0, 0.5, -0.5], size=(n, 9))
+        for _ in range(int(rng.integers(0, 4))):
+            t[rng.integers(0, n), rng.integers(0, 9)] = specials[rng.integers(0, len(specials))]
+        c = MeshCollider(t, grouped=False)
+        v = t.reshape(-1, 3)
+        for got, op in ((c.Min(), go_min), (c.Max(), go_max)):
+            for a, g in enumerate(got.Array()):
+                want = functools.reduce(op, [float(x) for x in v[:, a]])
+                assert (g != g and want != want) or (g == want and math.copysign(1, g) == math.copysign(1, want)), \
+                    (trial, a, g, want)
 
 
 def test_malformed_records_are_rejected():
